@@ -1,0 +1,192 @@
+/*
+ * xbach.h — C ABI of the GB300-native X-BACH difference-imaging path.
+ *
+ * This header is the drop-in boundary for X-BACH's stage API
+ * (include/bach.h:66-87 of D0V4HKIIN/Thesis-EMX-BACH): init, sss, cmv, cd,
+ * ksc, conv, sub, fin.  The reference passes a `ClData&` (OpenCL context,
+ * queue and cl::Buffer members, include/bach.h:25-64) plus a mutable
+ * `Arguments&` (include/argsUtil.h:7-57) from stage to stage; here an opaque
+ * `xb_ctx` owns the CUDA stream and every device buffer, and `xb_params`
+ * carries the Arguments fields that define the arithmetic.
+ *
+ * Conventions
+ *   - Every entry point returns an `int` status: XB_OK (0) or one of the
+ *     XB_ERR_* codes below.  Each reference `std::exit(1)` / sentinel path
+ *     has its own code (see the list).
+ *   - The caller owns host arrays; the context owns device memory.
+ *   - A context is not thread-safe; it issues all work on one CUDA stream.
+ *   - Image layout is row-major, x fastest: pixel (x, y) at index x + y*w,
+ *     the same layout as the FITS primary HDU read by the reference
+ *     (src/fitsUtil.cpp:8-37).
+ */
+#ifndef XBACH_H
+#define XBACH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define XB_OK 0
+#define XB_ERR_ARG 1             /* bad argument / parameter                    */
+#define XB_ERR_SIZE_MISMATCH 2   /* template/science differ: src/bach.cpp:20-24 */
+#define XB_ERR_STAMP_TOO_SMALL 3 /* stamp < 100 px: src/bachUtil.cpp:151-154    */
+#define XB_ERR_NO_SUBSTAMPS 4    /* no substamps at all: src/bach.cpp:166-169   */
+#define XB_ERR_CUDA 5            /* CUDA runtime error                          */
+#define XB_ERR_STATE 6           /* stage called out of order                   */
+#define XB_ERR_NOMEM 7           /* device allocation failed                    */
+#define XB_ERR_IO 8              /* FITS read/write failure                     */
+#define XB_ERR_SINGULAR 9        /* global LU saw an all-zero row; the
+                                    reference returns 1 and ignores it
+                                    (src/bachUtil.cpp:334-338); reported as a
+                                    warning flag, never as a failing status    */
+#define XB_ERR_UNSUPPORTED 10    /* parameter outside this build's limits       */
+#define XB_ERR_DEVICE_TIMEOUT 11 /* a bounded device-side wait ran out          */
+
+/* ---- mask bits (include/datatypeUtil.h:172-188, cl_kern/ini.cl:1-13) ---- */
+#define XB_MASK_BAD_PIX_VAL (1u << 0)
+#define XB_MASK_SAT_PIXEL (1u << 1)
+#define XB_MASK_LOW_PIXEL (1u << 2)
+#define XB_MASK_NAN_PIXEL (1u << 3)
+#define XB_MASK_BAD_CONV (1u << 4)
+#define XB_MASK_INPUT_MASK (1u << 5)
+#define XB_MASK_OK_CONV (1u << 6)
+#define XB_MASK_BAD_INPUT (1u << 7)
+#define XB_MASK_BAD_PIXEL_T (1u << 8)
+#define XB_MASK_SKIP_T (1u << 9)
+#define XB_MASK_BAD_PIXEL_S (1u << 10)
+#define XB_MASK_SKIP_S (1u << 11)
+#define XB_MASK_BAD_OUTPUT (1u << 12)
+#define XB_MASK_ALL ((1u << 13) - 1u)
+
+/* ---- precision modes --------------------------------------------------- */
+/* XB_MODE_PLAIN: the reference's precision choices (FP64 statistics, FP32
+ * Y-pass accumulation, FP64 W/Q/B, FP64 solves, FP64 convolution).  Every
+ * quantity that feeds a stamp / substamp / rejection decision is computed in
+ * the reference's operation order, so the decision sets are bit-identical to
+ * the CPU oracle.
+ * XB_MODE_MIXED: FP32 basis convolutions, 3xTF32 tensor-core Gram matrices,
+ * FP64 LU + one iterative-refinement step, FP32 full-frame convolution. */
+#define XB_MODE_PLAIN 0
+#define XB_MODE_MIXED 1
+
+#define XB_MAX_GAUSS 8
+
+/* Fields and defaults of include/argsUtil.h:7-57.  Defaults are produced by
+ * xb_params_default(). */
+typedef struct xb_params {
+  int stampsx;              /* -sx, default 10 */
+  int stampsy;              /* -sy, default 10 */
+  double threshLow;         /* 0.0 */
+  double threshHigh;        /* 25000.0 */
+  double threshKernFit;     /* 20.0 */
+  double sigKernFit;        /* 2.0 */
+  double sigClipAlpha;      /* 3.0 */
+  double iqRange;           /* 1.35 */
+  int maxKSStamps;          /* 3 */
+  int hSStampWidth;         /* 15 (substamp is 2*15+1 = 31 px) */
+  int hKernelWidth;         /* 10 (kernel is 2*10+1 = 21 px) */
+  double inSpreadMaskFactor;/* 1.0 */
+  int normalizeTemplate;    /* 1 */
+  int backgroundOrder;      /* 1 */
+  int kernelOrder;          /* 2 */
+  int nGauss;               /* 3 */
+  int dg[XB_MAX_GAUSS];     /* {6, 4, 2} polynomial degree per Gaussian */
+  float bg[XB_MAX_GAUSS];   /* 1/(2 sigma^2) stored as float, sigma 0.7/1.5/3.0 */
+  int mode;                 /* XB_MODE_PLAIN or XB_MODE_MIXED */
+  int verbose;              /* -v */
+} xb_params;
+
+/* Fill `p` with the reference defaults (include/argsUtil.h:7-57). */
+void xb_params_default(xb_params* p);
+
+/* Number of basis functions implied by nGauss/dg: sum (d+1)(d+2)/2, the
+ * counting rule of src/bach.cpp:181-188 (49 for the defaults). */
+int xb_params_npsf(const xb_params* p);
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct xb_ctx xb_ctx;
+
+/* Replaces main()'s OpenCL set-up (src/main.cpp:41-54): picks CUDA device
+ * `device` and creates the context's stream. */
+int xb_ctx_create(const xb_params* p, int device, xb_ctx** out);
+int xb_ctx_destroy(xb_ctx* ctx);
+/* Human-readable message for the last failing call on this context. */
+const char* xb_last_error(const xb_ctx* ctx);
+
+/* ---- stage API (include/bach.h:66-87) ------------------------------------ */
+
+/* init (src/bach.cpp:14-42): upload template T and science S (FP64 or FP32
+ * host arrays, w*h each) and build the input mask (maskInput + spreadMask).
+ * Returns XB_ERR_SIZE_MISMATCH if the sizes differ, as the reference exits. */
+int xb_init(xb_ctx* ctx, const double* T, int tw, int th, const double* S,
+            int sw, int sh);
+int xb_init_f32(xb_ctx* ctx, const float* T, int tw, int th, const float* S,
+                int sw, int sh);
+/* Same, with T and S already resident in device memory (FP32). */
+int xb_init_device_f32(xb_ctx* ctx, const float* dT, const float* dS, int w,
+                       int h);
+
+/* sss (src/bach.cpp:44-170): stamps, statistics, substamps, compaction,
+ * low-threshold retry. */
+int xb_sss(xb_ctx* ctx);
+/* cmv (src/bach.cpp:172-268): basis-convolved substamps W, Gram Q, B. */
+int xb_cmv(xb_ctx* ctx);
+/* cd (src/bach.cpp:270-313): test fits in both directions.  *convTemplate
+ * receives 1 when the template is the image to convolve. */
+int xb_cd(xb_ctx* ctx, int* convTemplate);
+/* ksc (src/bach.cpp:315-323): global kernel fit with substamp rejection. */
+int xb_ksc(xb_ctx* ctx);
+/* conv (src/bach.cpp:325-413): spatially varying convolution.  *kernSum
+ * receives the kernel sum at the image centre. */
+int xb_conv(xb_ctx* ctx, double* kernSum);
+/* sub (src/bach.cpp:415-440): difference image. */
+int xb_sub(xb_ctx* ctx);
+/* All of init..sub in order (fin = reading the images back). */
+int xb_run(xb_ctx* ctx, const float* T, const float* S, int w, int h,
+           float* convOut, float* diffOut);
+
+/* ---- results -------------------------------------------------------------- */
+#define XB_IMG_CONV 0 /* convolved image, the `-o` output (default diff.fits) */
+#define XB_IMG_DIFF 1 /* difference image, `sub.fits` */
+#define XB_IMG_MASK 2 /* 16-bit mask word per pixel (use xb_get_mask) */
+int xb_get_image(xb_ctx* ctx, int which, float* out);
+int xb_get_image_f64(xb_ctx* ctx, int which, double* out);
+int xb_get_mask(xb_ctx* ctx, uint16_t* out);
+/* Device pointers of the FP32 conv / diff images (valid until the next init
+ * or destroy); for callers that keep results on the GPU. */
+int xb_get_device_images(xb_ctx* ctx, const float** dConv, const float** dDiff);
+/* Kernel solution vector (nKernSolComp entries, 1-based like the reference;
+ * *n receives the length). */
+int xb_get_solution(xb_ctx* ctx, double* out, int cap, int* n);
+
+/* Generic introspection for parity checks: copies the named result array
+ * into `out` (at most `cap` bytes) and returns its size in bytes in *nbytes.
+ * Names are listed in the library's documentation (e.g. "sky0", "fwhm0",
+ * "ss_count0", "ss_xy0", "ss_val0", "cur", "merit", "kernel_sums0"). */
+int xb_get_array(xb_ctx* ctx, const char* name, void* out, size_t cap,
+                 size_t* nbytes);
+/* Scalar introspection ("convTemplate", "kernSum", "ksc_iterations",
+ * "stampsx", "stampsy", "fStampWidth", "sss_retry", "nstamps0", ...). */
+int xb_get_scalar(xb_ctx* ctx, const char* name, double* out);
+
+/* Number of this library's kernels launched since the context was created
+ * (for benchmark accounting). */
+long long xb_kernel_launches(const xb_ctx* ctx);
+
+/* ---- FITS I/O (src/fitsUtil.cpp:8-64 without CCfits) -------------------- */
+/* Reads the primary HDU (BITPIX -32 or -64) into a newly malloc'ed FP64
+ * array (free with xb_free).  Returns XB_ERR_IO / XB_ERR_UNSUPPORTED. */
+int xb_fits_read(const char* path, double** data, int* w, int* h);
+/* Writes a BITPIX -32 primary HDU (the reference writes FLOAT_IMG). */
+int xb_fits_write(const char* path, const double* data, int w, int h);
+void xb_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XBACH_H */
