@@ -116,6 +116,9 @@ int xb_ctx_create(const xb_params* p, int device, xb_ctx** out);
 int xb_ctx_destroy(xb_ctx* ctx);
 /* Human-readable message for the last failing call on this context. */
 const char* xb_last_error(const xb_ctx* ctx);
+/* Context options.  "trace" (0/1): keep host copies of the intermediate
+ * results of every stage for xb_get_array (parity checks; costs copies). */
+int xb_set_option(xb_ctx* ctx, const char* name, long long value);
 
 /* ---- stage API (include/bach.h:66-87) ------------------------------------ */
 

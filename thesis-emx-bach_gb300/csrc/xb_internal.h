@@ -1,0 +1,219 @@
+// xb_internal.h — context, geometry and helpers shared by the CUDA
+// translation units of the GB300 X-BACH library.
+//
+// Data layout in HBM (one context = one frame pair):
+//   img[2]      template / science, FP32 when the input was FP32 (exact
+//               promotion to FP64 on load), FP64 otherwise; row-major w*h.
+//   mask        uint16 per pixel (bit meanings of include/datatypeUtil.h:172).
+//   per stamp set (0 = stamps found on the template, 1 = on the science):
+//     count/cur/orig   int per kept stamp
+//     ssxy/ssval       maxSS substamp slots per kept stamp (int2 / double)
+//     W                [stamp][wRows][fSS*fSS]   FP64 (plain) or FP32 (mixed)
+//     Q                [stamp][qCount][qCount]   FP64
+//     B                [stamp][bCount]           FP64
+//   conv/diff   FP32 output images (plain mode also keeps FP64 copies).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "xbach.h"
+
+namespace xb {
+
+constexpr uint16_t BAD_PIX_VAL = 1u << 0, SAT_PIXEL = 1u << 1,
+                   LOW_PIXEL = 1u << 2, NAN_PIXEL = 1u << 3,
+                   BAD_CONV = 1u << 4, OK_CONV = 1u << 6,
+                   BAD_INPUT = 1u << 7, BAD_PIXEL_T = 1u << 8,
+                   SKIP_T = 1u << 9, BAD_PIXEL_S = 1u << 10,
+                   SKIP_S = 1u << 11, BAD_OUTPUT = 1u << 12,
+                   MASK_ALL = (1u << 13) - 1u;
+
+// Limits of this build (checked at context creation / sss).
+constexpr int MAX_NPSF = 128;       // basis functions
+constexpr int MAX_FK = 41;          // kernel width (hKernelWidth <= 20)
+constexpr int MAX_FSS = 63;         // substamp width (hSStampWidth <= 31)
+constexpr int MAX_SOL = 2048;       // solution length
+constexpr int MAX_MAXSS = 16;       // substamp slots per stamp
+
+struct Geo {
+  int fSS, hSS, fK, hK, nPSF, nComp1, nComp2, nComp, nBG, matSize, nSol;
+  int wRows, wCols, qCount, bCount, maxSS;
+};
+
+inline int triNum(int t) { return t * (t + 1) / 2; }
+
+Geo makeGeo(const xb_params& p);
+
+// Basis tables built once on the host (createKernelFilter/createKernelVector,
+// cl_kern/cmv.cl:1-68; the host Kernel struct of include/datatypeUtil.h).
+struct Basis {
+  std::vector<int> gauss, kx, ky;
+  std::vector<double> fX, fY, vec;  // nPSF*fK, nPSF*fK, nPSF*fK*fK
+  std::vector<int> bgX, bgY, kpX, kpY;
+  // unique Y filters: yGroupOf[n] = group; groups list their members
+  std::vector<int> yGroupStart, yGroupMembers;  // CSR
+};
+Basis buildBasis(const xb_params& p, const Geo& g);
+
+struct StampSetDev {
+  int n = 0;                 // kept stamps
+  int* orig = nullptr;       // original stamp index
+  int* count = nullptr;      // usable substamps (<= maxKSStamps)
+  int* cur = nullptr;        // current substamp index
+  int2* ssxy = nullptr;      // n * maxSS
+  double* ssval = nullptr;   // n * maxSS
+  void* W = nullptr;         // n * wRows * wCols (double or float)
+  double* Q = nullptr;       // n * qCount^2
+  double* B = nullptr;       // n * bCount
+  float* Wf = nullptr;       // mixed-mode FP32 W (alias of W)
+  float* Qf = nullptr;       // mixed-mode FP32 Gram [n][64][64]
+  std::vector<int> h_count, h_cur;
+};
+
+struct DevBuf {  // simple grow-only device allocation
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace xb
+
+struct xb_ctx {
+  xb_params p{};
+  xb::Geo g{};
+  xb::Basis basis;
+  int device = 0;
+  int smCount = 0;
+  cudaStream_t stream = nullptr;
+  int w = 0, h = 0;
+  int imgIsF64 = 0;
+  void* img[2] = {nullptr, nullptr};
+  uint16_t* mask = nullptr;
+  int stage = 0;  // 0 none, 1 init, 2 sss, 3 cmv, 4 cd, 5 ksc, 6 conv, 7 sub
+  // sss
+  int stampsx = 0, stampsy = 0, fStampWidth = 0, nAll = 0, sssRetry = 0;
+  int4* geomAll = nullptr;        // cx, cy, sx, sy for every grid stamp
+  double* skyAll[2] = {nullptr, nullptr};
+  double* fwhmAll[2] = {nullptr, nullptr};
+  int* cntAll[2] = {nullptr, nullptr};
+  int2* ssxyAll[2] = {nullptr, nullptr};
+  double* ssvalAll[2] = {nullptr, nullptr};
+  double* goodScratch = nullptr;  // nAll * fStampWidth^2 good pixels
+  uint8_t* clipScratch = nullptr; // nAll * fStampWidth^2 clip flags
+  xb::StampSetDev set[2];
+  // basis on device
+  double* dFX = nullptr;
+  double* dFY = nullptr;
+  double* dVec = nullptr;
+  int* dYGroupStart = nullptr;
+  int* dYGroupMembers = nullptr;
+  int* dKx = nullptr;
+  int* dKy = nullptr;
+  // cd / ksc
+  int convTemplate = 0, chosen = 0;
+  double merit[2] = {0, 0};
+  double* dSol = nullptr;          // nSol
+  std::vector<double> hSol;
+  double* dMat = nullptr;          // (matSize+1)^2
+  double* dMatLU = nullptr;        // factor workspace
+  int* dPiv = nullptr;
+  double* dWts = nullptr;          // nStamps * nComp2
+  double* dDots = nullptr;         // per-stamp dot products for the matrix
+  double* dSig = nullptr;          // per-stamp chi^2
+  double* dWork = nullptr;         // generic scratch (doubles)
+  int* dIWork = nullptr;           // generic scratch (ints)
+  size_t workDoubles = 0, workInts = 0;
+  int kscIterations = 0;
+  int singular = 0;
+  // conv / sub
+  double kernSum = 0.0;
+  float* convF = nullptr;
+  float* diffF = nullptr;
+  double* convD = nullptr;
+  double* diffD = nullptr;
+  // bookkeeping
+  long long launches = 0;
+  int trace = 0;
+  std::string lastError;
+  std::map<std::string, std::vector<uint8_t>> arrays;
+  std::map<std::string, double> scalars;
+  std::map<std::string, xb::DevBuf> pool;
+
+  template <class T>
+  void put(const std::string& k, const std::vector<T>& v) {
+    std::vector<uint8_t> b(v.size() * sizeof(T));
+    if(!v.empty()) memcpy(b.data(), v.data(), b.size());
+    arrays[k] = std::move(b);
+  }
+};
+
+namespace xb {
+
+// ---- error handling --------------------------------------------------------
+struct CudaError {
+  cudaError_t code;
+  const char* where;
+};
+#define XB_CUDA(call)                                          \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if(e_ != cudaSuccess) throw ::xb::CudaError{e_, #call};    \
+  } while(0)
+#define XB_LAUNCHED(ctx)                                             \
+  do {                                                               \
+    (ctx)->launches++;                                               \
+    cudaError_t e_ = cudaGetLastError();                             \
+    if(e_ != cudaSuccess) throw ::xb::CudaError{e_, "kernel launch"}; \
+  } while(0)
+
+struct XbError {
+  int code;
+  std::string msg;
+};
+
+// Named, grow-only device buffers: a repeated run on the same context
+// reuses its allocations, so steady-state runs allocate nothing.
+void* poolGet(xb_ctx* c, const char* name, size_t bytes);
+template <class T>
+T* buf(xb_ctx* c, const char* name, size_t n) {
+  return static_cast<T*>(poolGet(c, name, (n ? n : 1) * sizeof(T)));
+}
+template <class T>
+T* buf(xb_ctx* c, const std::string& name, size_t n) {
+  return buf<T>(c, name.c_str(), n);
+}
+
+template <class T>
+std::vector<T> toHost(xb_ctx* c, const T* d, size_t n) {
+  std::vector<T> h(n);
+  if(n) XB_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(T),
+                                cudaMemcpyDeviceToHost, c->stream));
+  XB_CUDA(cudaStreamSynchronize(c->stream));
+  return h;
+}
+template <class T>
+void toDevice(xb_ctx* c, T* d, const std::vector<T>& h) {
+  if(!h.empty())
+    XB_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T),
+                            cudaMemcpyHostToDevice, c->stream));
+}
+
+// ---- stage implementations (host orchestration in the .cu files) ---------
+void stageInitMask(xb_ctx* c);
+void stageSss(xb_ctx* c);
+void stageCmv(xb_ctx* c);
+void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
+void stageCd(xb_ctx* c);
+void stageKsc(xb_ctx* c);
+void stageConvSub(xb_ctx* c, bool doSub);
+
+// Kernel image at normalised position (xf, yf) and its sum into *dOut
+// (device): tree = 1 sums in 32-wide groups (cl_kern/cd.cl:419-442), tree = 0
+// sequentially (src/bachUtil.cpp:532-538).
+void kernelSumLaunch(xb_ctx* c, const double* dSol, double xf, double yf, int tree, double* dOut);
+
+}  // namespace xb

@@ -1,0 +1,777 @@
+// xb_sss.cu — the sss stage: stamp grid, per-stamp statistics, substamp
+// search, empty-stamp compaction and the low-threshold retry
+// (src/bach.cpp:44-170, src/sssUtil.cpp, src/bachUtil.cpp:130-280,
+// cl_kern/sss.cl).
+//
+// Every quantity that decides a stamp or substamp is computed in the
+// reference's operation order (no contraction: the library is built with
+// -fmad=false), so the stamp and substamp sets are bit-identical to the CPU
+// oracle.  Where the reference compacts with atomics (maskStamp,
+// sss.cl:157-188) the order is the ascending pixel index.
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+#include "xb_internal.h"
+
+namespace xb {
+
+namespace {
+
+constexpr int NSAMPLES = 100, PADDED = 128;
+constexpr int ST_THREADS = 256;
+
+__device__ __forceinline__ int satFloorToInt(double v) {
+  double f = floor(v);
+  if(f != f) return 0;
+  if(f >= 2147483647.0) return INT_MAX;
+  if(f <= -2147483648.0) return INT_MIN;
+  return (int)f;
+}
+
+// Numerical Recipes ran1 (cl_kern/sss.cl:108-146): three LCGs with a
+// 97-entry shuffle table; 64-bit integer state, exact.
+struct Ran1 {
+  long long ix1, ix2, ix3;
+  int idum, iff;
+  __device__ void init(int seed) {
+    idum = seed;
+    iff = 0;
+    ix1 = ix2 = ix3 = 0;
+  }
+  __device__ double next(double* r) {
+    const long long M1 = 259200, IA1 = 7141, IC1 = 54773;
+    const long long M2 = 134456, IA2 = 8121, IC2 = 28411;
+    const long long M3 = 243000, IA3 = 4561, IC3 = 51349;
+    const double RM1 = 1.0 / 259200, RM2 = 1.0 / 134456;
+    if(idum < 0 || iff == 0) {
+      iff = 1;
+      ix1 = (IC1 - idum) % M1;
+      ix1 = (IA1 * ix1 + IC1) % M1;
+      ix2 = ix1 % M2;
+      ix1 = (IA1 * ix1 + IC1) % M1;
+      ix3 = ix1 % M3;
+      for(int j = 1; j <= 97; j++) {
+        ix1 = (IA1 * ix1 + IC1) % M1;
+        ix2 = (IA2 * ix2 + IC2) % M2;
+        r[j] = ((double)ix1 + (double)ix2 * RM2) * RM1;
+      }
+      idum = 1;
+    }
+    ix1 = (IA1 * ix1 + IC1) % M1;
+    ix2 = (IA2 * ix2 + IC2) % M2;
+    ix3 = (IA3 * ix3 + IC3) % M3;
+    int j = 1 + (int)((97 * ix3) / M3);
+    double t = r[j];
+    r[j] = ((double)ix1 + (double)ix2 * RM2) * RM1;
+    return t;
+  }
+};
+
+// Block-wide exclusive scan of one int per thread (256 threads).
+__device__ __forceinline__ int blockExclusiveScan(int v, int* warpTot, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for(int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if(lane >= o) x += y;
+  }
+  if(lane == 31) warpTot[wid] = x;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    int s = 0;
+    for(int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      int t = warpTot[i];
+      warpTot[i] = s;
+      s += t;
+    }
+    *total = s;
+  }
+  __syncthreads();
+  int r = warpTot[wid] + x - v;
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------- stamp statistics --
+// One CTA per stamp: sampleStamp + pad + sortSamples (sss.cl:148-217),
+// maskStamp (:224-255), sigmaClip with maxIter 3 (bachUtil.cpp:255-266,
+// bach.cl:129-184) and createHistogram (sss.cl:257-391).
+template <class T>
+__global__ void __launch_bounds__(ST_THREADS)
+    k_stamp_stats(const T* __restrict__ img, uint16_t* __restrict__ mask,
+                  const int4* __restrict__ geom, int w, int h, int fSW,
+                  double* __restrict__ good, uint8_t* __restrict__ clip,
+                  double* __restrict__ chunkBuf, int maxChunks,
+                  double sigClipAlpha, double iqRange, double* __restrict__ skyOut,
+                  double* __restrict__ fwhmOut) {
+  const int s = blockIdx.x;
+  const int4 gm = geom[s];  // cx, cy, sx, sy
+  const int tid = threadIdx.x, lane = tid & 31;
+  __shared__ double samples[PADDED];
+  __shared__ double rtab[98];
+  __shared__ int cand[32];
+  __shared__ int sCount;
+  __shared__ int warpTot[ST_THREADS / 32];
+  __shared__ int sTotal;
+  __shared__ double sMean, sStd, sInv;
+  __shared__ int sPrev, sCurr, sClip, sDone;
+  __shared__ int bins[256];
+  __shared__ int okCount;
+  __shared__ double hLower, hUpper, hSky, hBinSize, hLowerBinVal;
+  __shared__ int hState;  // 0 continue, 1 stop (setFwhm), 2 stop (no fwhm)
+
+  // ---- phase A: random sampling (warp 0, RNG on lane 0) ----
+  if(tid < 32) {
+    Ran1 rng;
+    if(lane == 0) {
+      rng.init(-666);
+      sCount = 0;
+    }
+    const int numPix = gm.z * gm.w;
+    int cnt = 0, iter = 0;
+    while(cnt < NSAMPLES && iter < numPix) {
+      int b = min(32, numPix - iter);
+      if(lane == 0) {
+        for(int k = 0; k < b; k++) {
+          int rx = (int)floor(rng.next(rtab) * (int)gm.z);
+          int ry = (int)floor(rng.next(rtab) * (int)gm.w);
+          cand[k] = (rx + gm.x) + (ry + gm.y) * w;
+        }
+      }
+      __syncwarp();
+      bool ok = false;
+      double v = 0.0;
+      if(lane < b) {
+        int idx = cand[lane];
+        v = (double)img[idx];
+        ok = !(mask[idx] > 0 || fabs(v) <= 1e-10);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, ok);
+      int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+      if(ok && pos < NSAMPLES) samples[pos] = v;
+      cnt = min(NSAMPLES, cnt + __popc(bal));
+      iter += b;
+      __syncwarp();
+    }
+    if(lane == 0) sCount = cnt;
+    __syncwarp();
+    for(int i = lane; i < PADDED; i += 32)
+      if(i >= cnt) samples[i] = i < NSAMPLES ? 0.0 : INFINITY;
+    __syncwarp();
+    // bitonic network of the 28 host-launched sortSamples passes
+    for(int k = 2; k <= PADDED; k <<= 1)
+      for(int j = k >> 1; j > 0; j >>= 1) {
+        for(int i = lane; i < PADDED; i += 32) {
+          int ixj = i ^ j;
+          if(ixj > i) {
+            double a = samples[i], c = samples[ixj];
+            if((i & k) == 0 && a > c) {
+              samples[i] = c;
+              samples[ixj] = a;
+            } else if((i & k) != 0 && a < c) {
+              samples[i] = c;
+              samples[ixj] = a;
+            }
+          }
+        }
+        __syncwarp();
+      }
+  }
+  __syncthreads();
+
+  // ---- phase B: ordered compaction of good pixels (maskStamp) ----
+  double* gd = good + (size_t)s * fSW * fSW;
+  uint8_t* cl = clip + (size_t)s * fSW * fSW;
+  int nGood = 0;
+  for(int base = 0; base < fSW * fSW; base += ST_THREADS) {
+    int idxS = base + tid;
+    bool ok = false;
+    double pix = 0.0;
+    if(idxS < fSW * fSW) {
+      int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
+      if(xI < w && yI < h) {
+        size_t id = (size_t)xI + (size_t)yI * w;
+        pix = (double)img[id];
+        if(!(mask[id] > 0 || pix <= 1e-10)) {
+          if(isnan(pix)) mask[id] |= NAN_PIXEL | BAD_INPUT;
+          else ok = true;
+        }
+      }
+    }
+    int pos = blockExclusiveScan(ok ? 1 : 0, warpTot, &sTotal);
+    if(ok) {
+      gd[nGood + pos] = pix;
+      cl[nGood + pos] = 0;
+    }
+    nGood += sTotal;
+    __syncthreads();
+  }
+
+  // ---- phase C: sigma clip, maxIter 3 (bachUtil.cpp:34-128) ----
+  double* cS = chunkBuf + (size_t)s * 2 * maxChunks;
+  double* cS2 = cS + maxChunks;
+  if(tid == 0) {
+    sPrev = nGood;
+    sCurr = 0;
+    sDone = 0;
+    sMean = 0.0;
+    sStd = 1e10;
+    if(nGood == 0) sDone = 1;
+  }
+  __syncthreads();
+  const int nChunks = (nGood + 31) / 32;
+  for(int it = 0; it < 3; it++) {
+    if(sDone || sCurr == sPrev) break;
+    if(sPrev <= 1) {
+      if(tid == 0) {
+        sMean = 0.0;
+        sStd = 1e10;
+      }
+      break;
+    }
+    __syncthreads();
+    if(tid == 0) sCurr = sPrev;
+    for(int c = tid; c < nChunks; c += ST_THREADS) {
+      double a = 0.0, a2 = 0.0;
+      int lc = min(32, nGood - c * 32);
+      for(int l = 0; l < lc; l++) {
+        int k = c * 32 + l;
+        double d = cl[k] == 0 ? gd[k] : 0.0;
+        a += d;
+        a2 += d * d;
+      }
+      cS[c] = a;
+      cS2[c] = a2;
+    }
+    __syncthreads();
+    if(tid == 0) {
+      double sum = 0.0, sum2 = 0.0;
+      for(int c = 0; c < nChunks; c++) {
+        sum += cS[c];
+        sum2 += cS2[c];
+      }
+      double n = (double)sCurr;
+      double m = sum / n;
+      double sd = sqrt((sum2 - n * m * m) / (double)(sCurr - 1));
+      sMean = m;
+      sStd = sd;
+      sInv = 1.0 / sd;
+      sClip = 0;
+    }
+    __syncthreads();
+    int myClip = 0;
+    const double m = sMean, inv = sInv;
+    for(int k = tid; k < nGood; k += ST_THREADS)
+      if(cl[k] == 0 && fabs(gd[k] - m) * inv > sigClipAlpha) {
+        cl[k] = 1;
+        myClip++;
+      }
+    if(myClip) atomicAdd(&sClip, myClip);
+    __syncthreads();
+    if(tid == 0) sPrev = sCurr - sClip;
+    __syncthreads();
+  }
+  __syncthreads();
+  const double mean = sMean, invStd = 1.0 / sStd;
+
+  // ---- phase D: histogram sky / robust sigma (sss.cl:257-391) ----
+  if(tid == 0) {
+    int sc = sCount;
+    double upS = samples[(int)(0.9 * sc)];
+    double midS = samples[(int)(0.5 * sc)];
+    hBinSize = (upS - midS) / (double)NSAMPLES;
+    hLowerBinVal = midS - (128.0 * hBinSize);
+    hLower = hUpper = hSky = 0.0;
+    hState = 0;
+  }
+  __syncthreads();
+  for(int attempts = 0;; attempts++) {
+    if(attempts >= 5) {
+      if(tid == 0) hState = 2;
+      break;
+    }
+    for(int i = tid; i < 256; i += ST_THREADS) bins[i] = 0;
+    if(tid == 0) okCount = 0;
+    __syncthreads();
+    const double lbv = hLowerBinVal, bs = hBinSize;
+    int myOk = 0;
+    for(int i = tid; i < gm.z * gm.w; i += ST_THREADS) {
+      int x = i % gm.z, y = i / gm.z;
+      size_t id = (size_t)(gm.x + x) + (size_t)(gm.y + y) * w;
+      double v = (double)img[id];
+      if(mask[id] != 0 || v <= 1e-10) continue;
+      if(fabs(v - mean) * invStd > sigClipAlpha) continue;
+      int index = satFloorToInt((v - lbv) / bs);
+      index = index == INT_MAX ? INT_MAX : index + 1;
+      index = min(max(index, 0), 255);
+      atomicAdd(&bins[index], 1);
+      myOk++;
+    }
+    if(myOk) atomicAdd(&okCount, myOk);
+    __syncthreads();
+    if(tid == 0) {
+      const int ok = okCount;
+      double binSize = hBinSize, lowerBinVal = hLowerBinVal;
+      if(ok == 0 || binSize == 0.0) {
+        hState = 2;
+      } else {
+        double sumBins = 0.0, maxDens = 0.0;
+        int lowerIndex = 1, upperIndex = 1, maxIndex = -1;
+        while(upperIndex < 255) {
+          while(sumBins < ok / 10.0 && upperIndex < 255) sumBins += bins[upperIndex++];
+          if(sumBins / (upperIndex - lowerIndex) > maxDens) {
+            maxDens = sumBins / (upperIndex - lowerIndex);
+            maxIndex = lowerIndex;
+          }
+          sumBins -= bins[lowerIndex++];
+        }
+        if(maxIndex < 0 || maxIndex > 255) maxIndex = 0;
+        sumBins = 0.0;
+        double sumExpect = 0.0;
+        for(int i = maxIndex; sumBins < ok / 10.0 && i < 255; i++) {
+          sumBins += bins[i];
+          sumExpect += i * bins[i];
+        }
+        double modeBin = sumExpect / sumBins + 0.5;
+        double skyEst = lowerBinVal + binSize * (modeBin - 1.0);
+        double lower = ok * 0.25, upper = ok * 0.75;
+        sumBins = 0.0;
+        int i = 0;
+        while(sumBins < lower) sumBins += bins[i++];
+        lower = i - (sumBins - lower) / bins[i - 1];
+        while(sumBins < upper) sumBins += bins[i++];
+        upper = i - (sumBins - upper) / bins[i - 1];
+        hSky = skyEst;
+        hLower = lower;
+        hUpper = upper;
+        if(lower < 1.0 || upper > 255.0) {
+          hLowerBinVal = lowerBinVal - 128.0 * binSize;
+          hBinSize = binSize * 2;
+        } else if(upper - lower < 40.0) {
+          hBinSize = binSize / 3.0;
+          hLowerBinVal = skyEst - 128.0 * hBinSize;
+        } else {
+          hState = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if(hState != 0) break;
+  }
+  if(tid == 0) {
+    fwhmOut[s] = hState == 1 ? hBinSize * (hUpper - hLower) / iqRange : 0.0;
+    skyOut[s] = hSky;
+  }
+}
+
+// --------------------------------------------------------- substamp search --
+// One CTA per (stamp, image): findSubStamps (cl_kern/sss.cl:448-572).  The
+// raster scan is processed in chunks of 1024 pixels: the candidate test runs
+// in parallel, then candidates are visited in raster order with their mask
+// re-read (acceptances only add SKIP bits).  The reference's writes of the
+// bad-pixel bit for pixels above threshHigh (sss.cl:416-419, :484-487,
+// :512-515) are unreachable: such pixels carry BAD_INPUT from maskInput
+// (ini.cl:29), which every badMask contains, and that test comes first.
+constexpr int FS_THREADS = 256, FS_CHUNK = 1024, FS_FAILCACHE = 128;
+
+__device__ __forceinline__ uint16_t ldMask(const uint16_t* m, size_t i) {
+  return *((volatile const uint16_t*)m + i);
+}
+__device__ __forceinline__ void orMask(uint16_t* m, size_t i, uint16_t bits) {
+  uintptr_t a = (uintptr_t)(m + i);
+  unsigned* w32 = (unsigned*)(a & ~(uintptr_t)3);
+  unsigned sh = (a & 2) ? 16u : 0u;
+  atomicOr(w32, (unsigned)bits << sh);
+}
+
+template <class T>
+__global__ void __launch_bounds__(FS_THREADS)
+    k_find_substamps(const T* __restrict__ img0, const T* __restrict__ img1,
+                     uint16_t* __restrict__ mask, const int4* __restrict__ geom,
+                     const double* __restrict__ sky0, const double* __restrict__ fwhm0,
+                     const double* __restrict__ sky1, const double* __restrict__ fwhm1,
+                     int2* __restrict__ xy0, double* __restrict__ val0, int* __restrict__ cnt0,
+                     int2* __restrict__ xy1, double* __restrict__ val1, int* __restrict__ cnt1,
+                     int w, int fSW, int hSS, int maxSS, double tH, double tKF) {
+  const int s = blockIdx.x, im = blockIdx.y, tid = threadIdx.x;
+  const T* img = im == 0 ? img0 : img1;
+  const double sky = im == 0 ? sky0[s] : sky1[s];
+  const double fwhm = im == 0 ? fwhm0[s] : fwhm1[s];
+  int2* xyOut = (im == 0 ? xy0 : xy1) + (size_t)s * maxSS;
+  double* valOut = (im == 0 ? val0 : val1) + (size_t)s * maxSS;
+  const uint16_t badMask =
+      (uint16_t)((MASK_ALL & ~OK_CONV) & ~(im == 0 ? (BAD_PIXEL_S | SKIP_S) : (BAD_PIXEL_T | SKIP_T)));
+  const uint16_t skipMask = im == 0 ? SKIP_T : SKIP_S;
+  const int4 gm = geom[s];
+  const int cx = gm.x, cy = gm.y, sx = gm.z, sy = gm.w;
+  const double invFwhm = 1.0 / fwhm;
+
+  __shared__ int cand[FS_CHUNK];
+  __shared__ int warpTot[FS_THREADS / 32];
+  __shared__ int sTotal;
+  __shared__ int2 locXY[MAX_MAXSS];
+  __shared__ double locVal[MAX_MAXSS];
+  __shared__ int sCnt;
+  __shared__ double redV[FS_THREADS / 32];
+  __shared__ int redI[FS_THREADS / 32];
+  __shared__ int sMx, sMy, sBad, sSkip;
+  __shared__ double sSum;
+  __shared__ double win[MAX_FSS * MAX_FSS];
+  __shared__ int failX[FS_FAILCACHE], failY[FS_FAILCACHE];
+  __shared__ int nFail;
+  if(tid == 0) {
+    sCnt = 0;
+    nFail = 0;
+  }
+  __syncthreads();
+  const double floorV = sky + tKF * fwhm;
+  double dfrac = 0.9;
+  int passes = 0;
+  const int nPix = fSW * fSW;
+  while(sCnt < maxSS && passes < 256) {
+    passes++;
+    const double alt = sky + (tH - sky) * dfrac;
+    const double lim = floorV < alt ? alt : floorV;  // OpenCL max()
+    for(int base = 0; base < nPix && sCnt < maxSS; base += FS_CHUNK) {
+      // candidate flags for 4 consecutive raster positions per thread
+      int myN = 0;
+      int myIdx[4];
+#pragma unroll
+      for(int k = 0; k < 4; k++) {
+        int r = base + tid * 4 + k;
+        myIdx[k] = -1;
+        if(r < nPix) {
+          int absx = r % fSW + cx, absy = r / fSW + cy;
+          size_t a = (size_t)absx + (size_t)absy * w;
+          if(!(ldMask(mask, a) & badMask)) {
+            double v = (double)img[a];
+            if(!((v - sky) * invFwhm < tKF) && v > lim) myIdx[myN++] = r;
+          }
+        }
+      }
+      int pos = blockExclusiveScan(myN, warpTot, &sTotal);
+      for(int k = 0; k < myN; k++) cand[pos + k] = myIdx[k];
+      const int nCand = sTotal;
+      __syncthreads();
+      for(int ci = 0; ci < nCand; ci++) {
+        const int r = cand[ci];
+        const int absx = r % fSW + cx, absy = r / fSW + cy;
+        // the candidate's own pixel may have been skipped meanwhile
+        if(tid == 0) sSkip = (ldMask(mask, (size_t)absx + (size_t)absy * w) & badMask) ? 1 : 0;
+        __syncthreads();
+        if(sSkip) continue;
+        // local maximum within +-hSS clipped to the fStampWidth window
+        const int x0 = max(absx - hSS, cx), y0 = max(absy - hSS, cy);
+        const int x1 = min(absx + hSS, cx + fSW - 1), y1 = min(absy + hSS, cy + fSW - 1);
+        const int ww = x1 - x0 + 1, wn = ww * (y1 - y0 + 1);
+        double bv = 0.0;
+        int bi = INT_MAX;
+        for(int i = tid; i < wn; i += FS_THREADS) {
+          int kx = x0 + i % ww, ky = y0 + i / ww;
+          size_t ka = (size_t)kx + (size_t)ky * w;
+          if(ldMask(mask, ka) & badMask) continue;
+          double kv = (double)img[ka];
+          if((kv - sky) * invFwhm < tKF) continue;
+          if(kv > bv || (kv == bv && bi != INT_MAX && i < bi)) {
+            if(kv > bv) {
+              bv = kv;
+              bi = i;
+            } else if(i < bi) {
+              bi = i;
+            }
+          }
+        }
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1) {
+          double ov = __shfl_down_sync(0xffffffffu, bv, o);
+          int oi = __shfl_down_sync(0xffffffffu, bi, o);
+          if(ov > bv || (ov == bv && oi < bi)) {
+            bv = ov;
+            bi = oi;
+          }
+        }
+        if((tid & 31) == 0) {
+          redV[tid >> 5] = bv;
+          redI[tid >> 5] = bi;
+        }
+        __syncthreads();
+        if(tid == 0) {
+          double b = redV[0];
+          int i = redI[0];
+          for(int k = 1; k < FS_THREADS / 32; k++)
+            if(redV[k] > b || (redV[k] == b && redI[k] < i)) {
+              b = redV[k];
+              i = redI[k];
+            }
+          if(i == INT_MAX || !(b > 0.0)) {
+            sMx = absx;
+            sMy = absy;
+          } else {
+            sMx = x0 + i % ww;
+            sMy = y0 + i / ww;
+          }
+          // a window that failed once fails for the rest of the search:
+          // the mask only gains bits while substamps are being found
+          sBad = 0;
+          for(int k = 0; k < nFail; k++)
+            if(failX[k] == sMx && failY[k] == sMy) sBad = 1;
+        }
+        __syncthreads();
+        if(sBad) continue;
+        const int mx = sMx, my = sMy;
+        // checkSStamp (sss.cl:393-428), window clipped to the stamp size
+        const int u0 = max(mx - hSS, cx), v0 = max(my - hSS, cy);
+        const int u1 = min(mx + hSS, cx + sx - 1), v1 = min(my + hSS, cy + sy - 1);
+        const int uw = u1 - u0 + 1, un = uw * (v1 - v0 + 1);
+        int anyBad = 0;
+        for(int i = tid; i < un; i += FS_THREADS) {
+          int kx = u0 + i % uw, ky = v0 + i / uw;
+          size_t ka = (size_t)kx + (size_t)ky * w;
+          if(ldMask(mask, ka) & badMask) anyBad = 1;
+          double v = (double)img[ka];
+          win[i] = ((v - sky) / fwhm > tKF) ? v : NAN;  // NaN marks "not summed"
+        }
+        anyBad = __syncthreads_or(anyBad);
+        if(tid == 0) {
+          double ret = 0.0;
+          if(!anyBad) {
+            for(int i = 0; i < un; i++) {
+              double v = win[i];
+              if(v == v) ret += v;
+            }
+          }
+          sSum = ret;
+          if(ret == 0.0 && nFail < FS_FAILCACHE) {
+            failX[nFail] = mx;
+            failY[nFail] = my;
+            nFail++;
+          }
+        }
+        __syncthreads();
+        const double ret = sSum;
+        if(ret == 0.0) continue;
+        if(tid == 0) {
+          locXY[sCnt] = make_int2(mx, my);
+          locVal[sCnt] = ret;
+        }
+        const int u2 = max(mx - hSS, cx), v2 = max(my - hSS, cy);
+        const int u3 = min(mx + hSS, cx + sx - 1), v3 = min(my + hSS, cy + sy - 1);
+        const int sw = u3 - u2 + 1, sn = sw * (v3 - v2 + 1);
+        for(int i = tid; i < sn; i += FS_THREADS)
+          orMask(mask, (size_t)(u2 + i % sw) + (size_t)(v2 + i / sw) * w, skipMask);
+        __syncthreads();
+        if(tid == 0) sCnt = sCnt + 1;
+        __syncthreads();
+        if(sCnt >= maxSS) break;
+      }
+      __syncthreads();
+    }
+    if(lim == floorV) break;
+    dfrac -= 0.2;
+  }
+  __syncthreads();
+  if(tid == 0) {
+    const int cnt = sCnt;
+    // insertion sort, descending (sortSubStamps, sss.cl:430-446)
+    for(int i = 1; i < cnt; i++)
+      for(int j = i; j > 0 && locVal[j - 1] < locVal[j]; j--) {
+        int2 t = locXY[j - 1];
+        locXY[j - 1] = locXY[j];
+        locXY[j] = t;
+        double tv = locVal[j - 1];
+        locVal[j - 1] = locVal[j];
+        locVal[j] = tv;
+      }
+    for(int i = 0; i < maxSS; i++) {
+      xyOut[i] = i < cnt ? locXY[i] : make_int2(INT_MAX, INT_MAX);
+      valOut[i] = i < cnt ? locVal[i] : -INFINITY;
+    }
+    (im == 0 ? cnt0 : cnt1)[s] = min(cnt, maxSS / 2);
+  }
+}
+
+// removeEmptyStamps (src/sssUtil.cpp:106-197, sss.cl:574-638): keep stamps
+// with at least one substamp in ascending original order.  One CTA per image.
+__global__ void __launch_bounds__(256)
+    k_compact_stamps(const int* __restrict__ cntAll, const int2* __restrict__ xyAll,
+                     const double* __restrict__ valAll, int nAll, int maxSS,
+                     int* __restrict__ orig, int* __restrict__ count, int* __restrict__ cur,
+                     int2* __restrict__ xy, double* __restrict__ val, int* __restrict__ nOut) {
+  __shared__ int warpTot[8];
+  __shared__ int sTotal;
+  int done = 0;
+  for(int base = 0; base < nAll; base += 256) {
+    int s = base + threadIdx.x;
+    int keep = (s < nAll && cntAll[s] > 0) ? 1 : 0;
+    int pos = blockExclusiveScan(keep, warpTot, &sTotal) + done;
+    if(keep) {
+      orig[pos] = s;
+      count[pos] = cntAll[s];
+      cur[pos] = 0;
+      for(int k = 0; k < maxSS; k++) {
+        bool live = k < cntAll[s];
+        xy[(size_t)pos * maxSS + k] = live ? xyAll[(size_t)s * maxSS + k] : make_int2(INT_MAX, INT_MAX);
+        val[(size_t)pos * maxSS + k] = live ? valAll[(size_t)s * maxSS + k] : -INFINITY;
+      }
+    }
+    done += sTotal;
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) *nOut = done;
+}
+
+__global__ void k_reset_skip(uint16_t* mask, long long n) {
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    mask[i] &= (uint16_t)~(SKIP_S | SKIP_T);
+}
+
+}  // namespace
+
+static void sssPass(xb_ctx* c, int* nKept) {
+  const Geo& g = c->g;
+  const int fSW = c->fStampWidth, nAll = c->nAll;
+  const int maxChunks = (fSW * fSW + 31) / 32;
+  double* chunkBuf = c->dWork;  // sized by stageSss
+  for(int im = 0; im < 2; im++) {
+    if(c->imgIsF64)
+      k_stamp_stats<double><<<nAll, ST_THREADS, 0, c->stream>>>(
+          (const double*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
+          c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
+          c->p.iqRange, c->skyAll[im], c->fwhmAll[im]);
+    else
+      k_stamp_stats<float><<<nAll, ST_THREADS, 0, c->stream>>>(
+          (const float*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
+          c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
+          c->p.iqRange, c->skyAll[im], c->fwhmAll[im]);
+    XB_LAUNCHED(c);
+  }
+  dim3 grid(nAll, 2);
+  if(c->imgIsF64)
+    k_find_substamps<double><<<grid, FS_THREADS, 0, c->stream>>>(
+        (const double*)c->img[0], (const double*)c->img[1], c->mask, c->geomAll,
+        c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0],
+        c->ssvalAll[0], c->cntAll[0], c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w,
+        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit);
+  else
+    k_find_substamps<float><<<grid, FS_THREADS, 0, c->stream>>>(
+        (const float*)c->img[0], (const float*)c->img[1], c->mask, c->geomAll,
+        c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0],
+        c->ssvalAll[0], c->cntAll[0], c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w,
+        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit);
+  XB_LAUNCHED(c);
+  for(int im = 0; im < 2; im++) {
+    StampSetDev& S = c->set[im];
+    k_compact_stamps<<<1, 256, 0, c->stream>>>(c->cntAll[im], c->ssxyAll[im], c->ssvalAll[im],
+                                               nAll, g.maxSS, S.orig, S.count, S.cur, S.ssxy,
+                                               S.ssval, c->dIWork + im);
+    XB_LAUNCHED(c);
+  }
+  std::vector<int> n = toHost(c, c->dIWork, 2);
+  nKept[0] = n[0];
+  nKept[1] = n[1];
+}
+
+void stageSss(xb_ctx* c) {
+  const Geo& g = c->g;
+  const int w = c->w, h = c->h;
+  // stamp width rule of src/bach.cpp:51-66
+  c->stampsx = c->p.stampsx;
+  c->stampsy = c->p.stampsy;
+  int fSW = std::min(w / c->stampsx, h / c->stampsy);
+  fSW -= g.fK;
+  fSW -= fSW % 2 == 0 ? 1 : 0;
+  if(fSW < g.fSS) {
+    fSW = g.fSS + g.fK;
+    fSW -= fSW % 2 == 0 ? 1 : 0;
+    c->stampsx = w / fSW;
+    c->stampsy = h / fSW;
+  }
+  c->fStampWidth = fSW;
+  if(c->stampsx <= 0 || c->stampsy <= 0) throw XbError{XB_ERR_ARG, "image too small for one stamp"};
+  if(fSW > 2048) throw XbError{XB_ERR_UNSUPPORTED, "stamp width above 2048"};
+  if(g.maxSS > MAX_MAXSS || g.fSS > MAX_FSS)
+    throw XbError{XB_ERR_UNSUPPORTED, "substamp parameters above this build's limits"};
+  const int nAll = c->stampsx * c->stampsy;
+  c->nAll = nAll;
+  // createStampBounds (sss.cl:86-105)
+  std::vector<int4> geom(nAll);
+  for(int id = 0; id < nAll; id++) {
+    int sxI = id % c->stampsx, syI = id / c->stampsx;
+    int startX = sxI * w / c->stampsx, startY = syI * h / c->stampsy;
+    int stopX = std::min(startX + fSW, w), stopY = std::min(startY + fSW, h);
+    geom[id] = make_int4(startX, startY, stopX - startX, stopY - startY);
+    if((stopX - startX) * (stopY - startY) < NSAMPLES)  // bachUtil.cpp:145-155
+      throw XbError{XB_ERR_STAMP_TOO_SMALL, "Not enough pixels in a stamp"};
+  }
+  // buffers for this grid
+  c->geomAll = buf<int4>(c, "geomAll", nAll);
+  for(int im = 0; im < 2; im++) {
+    const std::string sfx = std::to_string(im);
+    c->skyAll[im] = buf<double>(c, "skyAll" + sfx, nAll);
+    c->fwhmAll[im] = buf<double>(c, "fwhmAll" + sfx, nAll);
+    c->cntAll[im] = buf<int>(c, "cntAll" + sfx, nAll);
+    c->ssxyAll[im] = buf<int2>(c, "ssxyAll" + sfx, (size_t)nAll * g.maxSS);
+    c->ssvalAll[im] = buf<double>(c, "ssvalAll" + sfx, (size_t)nAll * g.maxSS);
+    StampSetDev& S = c->set[im];
+    S.orig = buf<int>(c, "orig" + sfx, nAll);
+    S.count = buf<int>(c, "count" + sfx, nAll);
+    S.cur = buf<int>(c, "cur" + sfx, nAll);
+    S.ssxy = buf<int2>(c, "ssxy" + sfx, (size_t)nAll * g.maxSS);
+    S.ssval = buf<double>(c, "ssval" + sfx, (size_t)nAll * g.maxSS);
+  }
+  c->goodScratch = buf<double>(c, "goodScratch", (size_t)nAll * fSW * fSW);
+  c->clipScratch = buf<uint8_t>(c, "clipScratch", (size_t)nAll * fSW * fSW);
+  const size_t chunkDoubles = (size_t)nAll * 2 * ((fSW * fSW + 31) / 32);
+  c->dWork = buf<double>(c, "chunkScratch", chunkDoubles);
+  c->dIWork = buf<int>(c, "iwork", 64);
+  toDevice(c, c->geomAll, geom);
+  int nKept[2];
+  sssPass(c, nKept);
+  const int oldCount = nAll;
+  const double fT = (double)nKept[0] / oldCount, fS = (double)nKept[1] / oldCount;
+  c->sssRetry = 0;
+  if(fT < 0.1 || fS < 0.1) {
+    // bach.cpp:142-161: halve threshLow (unused by sss), clear the SKIP bits,
+    // recompute everything with the current mask
+    c->sssRetry = 1;
+    const long long n = (long long)w * h;
+    k_reset_skip<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(c->mask, n);
+    XB_LAUNCHED(c);
+    sssPass(c, nKept);
+  }
+  c->set[0].n = nKept[0];
+  c->set[1].n = nKept[1];
+  if(nKept[0] == 0 && nKept[1] == 0) throw XbError{XB_ERR_NO_SUBSTAMPS, "No substamps found"};
+  for(int im = 0; im < 2; im++) {
+    StampSetDev& S = c->set[im];
+    S.h_count = toHost(c, S.count, S.n);
+    S.h_cur.assign(S.n, 0);
+  }
+  if(c->trace) {
+    for(int im = 0; im < 2; im++) {
+      const std::string sfx = std::to_string(im);
+      c->put("sky" + sfx, toHost(c, c->skyAll[im], nAll));
+      c->put("fwhm" + sfx, toHost(c, c->fwhmAll[im], nAll));
+      c->put("ss_count_all" + sfx, toHost(c, c->cntAll[im], nAll));
+      c->put("ss_xy_all" + sfx, toHost(c, c->ssxyAll[im], (size_t)nAll * g.maxSS));
+      c->put("ss_val_all" + sfx, toHost(c, c->ssvalAll[im], (size_t)nAll * g.maxSS));
+      const StampSetDev& S = c->set[im];
+      c->put("stamp_index" + sfx, toHost(c, S.orig, S.n));
+      c->put("ss_count" + sfx, toHost(c, S.count, S.n));
+      c->put("ss_xy" + sfx, toHost(c, S.ssxy, (size_t)S.n * g.maxSS));
+      c->put("ss_val" + sfx, toHost(c, S.ssval, (size_t)S.n * g.maxSS));
+      c->scalars["nstamps" + sfx] = S.n;
+    }
+    c->put("mask_sss", toHost(c, c->mask, (size_t)w * h));
+  }
+  c->scalars["stampsx"] = c->stampsx;
+  c->scalars["stampsy"] = c->stampsy;
+  c->scalars["fStampWidth"] = c->fStampWidth;
+  c->scalars["sss_retry"] = c->sssRetry;
+}
+
+}  // namespace xb

@@ -1,0 +1,238 @@
+"""ctypes binding of libxbach_gb300.so, the C ABI of include/xbach.h.
+
+The stage methods mirror X-BACH's stage API (include/bach.h:66-87): init,
+sss, cmv, cd, ksc, conv, sub.  There is no CPU fallback: loading fails
+loudly when the native library is missing.
+"""
+import ctypes
+import pathlib
+
+import numpy as np
+
+PKG = pathlib.Path(__file__).resolve().parent.parent
+LIB_PATH = PKG / "lib" / "libxbach_gb300.so"
+
+XB_MAX_GAUSS = 8
+XB_MODE_PLAIN = 0
+XB_MODE_MIXED = 1
+XB_IMG_CONV = 0
+XB_IMG_DIFF = 1
+
+STATUS = {
+    0: "XB_OK", 1: "XB_ERR_ARG", 2: "XB_ERR_SIZE_MISMATCH",
+    3: "XB_ERR_STAMP_TOO_SMALL", 4: "XB_ERR_NO_SUBSTAMPS", 5: "XB_ERR_CUDA",
+    6: "XB_ERR_STATE", 7: "XB_ERR_NOMEM", 8: "XB_ERR_IO", 9: "XB_ERR_SINGULAR",
+    10: "XB_ERR_UNSUPPORTED", 11: "XB_ERR_DEVICE_TIMEOUT",
+}
+
+
+class XbParams(ctypes.Structure):
+    """Mirror of `xb_params` (include/xbach.h)."""
+    _fields_ = [
+        ("stampsx", ctypes.c_int), ("stampsy", ctypes.c_int),
+        ("threshLow", ctypes.c_double), ("threshHigh", ctypes.c_double),
+        ("threshKernFit", ctypes.c_double), ("sigKernFit", ctypes.c_double),
+        ("sigClipAlpha", ctypes.c_double), ("iqRange", ctypes.c_double),
+        ("maxKSStamps", ctypes.c_int), ("hSStampWidth", ctypes.c_int),
+        ("hKernelWidth", ctypes.c_int), ("inSpreadMaskFactor", ctypes.c_double),
+        ("normalizeTemplate", ctypes.c_int), ("backgroundOrder", ctypes.c_int),
+        ("kernelOrder", ctypes.c_int), ("nGauss", ctypes.c_int),
+        ("dg", ctypes.c_int * XB_MAX_GAUSS), ("bg", ctypes.c_float * XB_MAX_GAUSS),
+        ("mode", ctypes.c_int), ("verbose", ctypes.c_int),
+    ]
+
+
+class XbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+EXPORTS = [
+    "xb_params_default", "xb_params_npsf", "xb_ctx_create", "xb_ctx_destroy",
+    "xb_last_error", "xb_set_option", "xb_init", "xb_init_f32",
+    "xb_init_device_f32", "xb_sss", "xb_cmv", "xb_cd", "xb_ksc", "xb_conv",
+    "xb_sub", "xb_run", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
+    "xb_get_device_images", "xb_get_solution", "xb_get_array",
+    "xb_get_scalar", "xb_kernel_launches", "xb_fits_read", "xb_fits_write",
+    "xb_free",
+]
+
+
+def lib():
+    """Loads the native library once (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"native library missing: {LIB_PATH} (run build())")
+    L = ctypes.CDLL(str(LIB_PATH))
+    P = ctypes.POINTER
+    vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.xb_params_default.argtypes = [P(XbParams)]
+    L.xb_params_npsf.argtypes = [P(XbParams)]
+    L.xb_ctx_create.argtypes = [P(XbParams), i, P(vp)]
+    L.xb_ctx_destroy.argtypes = [vp]
+    L.xb_last_error.argtypes = [vp]
+    L.xb_last_error.restype = ctypes.c_char_p
+    L.xb_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
+    L.xb_init.argtypes = [vp, vp, i, i, vp, i, i]
+    L.xb_init_f32.argtypes = [vp, vp, i, i, vp, i, i]
+    L.xb_init_device_f32.argtypes = [vp, vp, vp, i, i]
+    for f in ("xb_sss", "xb_cmv", "xb_ksc", "xb_sub"):
+        getattr(L, f).argtypes = [vp]
+    L.xb_cd.argtypes = [vp, P(i)]
+    L.xb_conv.argtypes = [vp, P(d)]
+    L.xb_run.argtypes = [vp, vp, vp, i, i, vp, vp]
+    L.xb_get_image.argtypes = [vp, i, vp]
+    L.xb_get_image_f64.argtypes = [vp, i, vp]
+    L.xb_get_mask.argtypes = [vp, vp]
+    L.xb_get_device_images.argtypes = [vp, P(vp), P(vp)]
+    L.xb_get_solution.argtypes = [vp, vp, i, P(i)]
+    L.xb_get_array.argtypes = [vp, ctypes.c_char_p, vp, ctypes.c_size_t,
+                               P(ctypes.c_size_t)]
+    L.xb_get_scalar.argtypes = [vp, ctypes.c_char_p, P(d)]
+    L.xb_kernel_launches.argtypes = [vp]
+    L.xb_kernel_launches.restype = ctypes.c_longlong
+    L.xb_fits_read.argtypes = [ctypes.c_char_p, P(vp), P(i), P(i)]
+    L.xb_fits_write.argtypes = [ctypes.c_char_p, vp, i, i]
+    L.xb_free.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def default_params(**kw):
+    p = XbParams()
+    lib().xb_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        if k in ("dg", "bg"):
+            arr = getattr(p, k)
+            for j, x in enumerate(v):
+                arr[j] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class Context:
+    """One frame pair on one GPU (an `xb_ctx`)."""
+
+    def __init__(self, params=None, device=0, trace=False):
+        self.L = lib()
+        self.params = params if params is not None else default_params()
+        h = ctypes.c_void_p()
+        rc = self.L.xb_ctx_create(ctypes.byref(self.params), device, ctypes.byref(h))
+        if rc != 0:
+            raise XbError(rc, "xb_ctx_create failed")
+        self.h = h
+        if trace:
+            self._check(self.L.xb_set_option(self.h, b"trace", 1))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.xb_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc != 0:
+            raise XbError(rc, self.L.xb_last_error(self.h).decode())
+        return rc
+
+    # ---- stage API ----
+    def init(self, T, S):
+        T = np.ascontiguousarray(T)
+        S = np.ascontiguousarray(S)
+        h, w = T.shape
+        sh, sw = S.shape
+        if T.dtype == np.float32 and S.dtype == np.float32:
+            return self._check(self.L.xb_init_f32(self.h, T.ctypes.data, w, h,
+                                                  S.ctypes.data, sw, sh))
+        T = T.astype(np.float64)
+        S = S.astype(np.float64)
+        return self._check(self.L.xb_init(self.h, T.ctypes.data, w, h,
+                                          S.ctypes.data, sw, sh))
+
+    def init_device(self, dT, dS, w, h):
+        """dT/dS: device pointers (ints) of FP32 images kept alive by the caller."""
+        return self._check(self.L.xb_init_device_f32(self.h, ctypes.c_void_p(dT),
+                                                     ctypes.c_void_p(dS), w, h))
+
+    def sss(self):
+        return self._check(self.L.xb_sss(self.h))
+
+    def cmv(self):
+        return self._check(self.L.xb_cmv(self.h))
+
+    def cd(self):
+        ct = ctypes.c_int(-1)
+        self._check(self.L.xb_cd(self.h, ctypes.byref(ct)))
+        return ct.value
+
+    def ksc(self):
+        return self._check(self.L.xb_ksc(self.h))
+
+    def conv(self):
+        ks = ctypes.c_double()
+        self._check(self.L.xb_conv(self.h, ctypes.byref(ks)))
+        return ks.value
+
+    def sub(self):
+        return self._check(self.L.xb_sub(self.h))
+
+    def run_all(self, T, S):
+        self.init(T, S)
+        self.sss()
+        self.cmv()
+        self.cd()
+        self.ksc()
+        self.conv()
+        self.sub()
+
+    # ---- results ----
+    def image(self, which, f64=True):
+        n = self.w * self.h
+        out = np.empty(n, np.float64 if f64 else np.float32)
+        fn = self.L.xb_get_image_f64 if f64 else self.L.xb_get_image
+        self._check(fn(self.h, which, out.ctypes.data))
+        return out.reshape(self.hgt, self.w)
+
+    def mask(self):
+        out = np.empty(self.w * self.hgt, np.uint16)
+        self._check(self.L.xb_get_mask(self.h, out.ctypes.data))
+        return out.reshape(self.hgt, self.w)
+
+    def solution(self):
+        n = ctypes.c_int()
+        self._check(self.L.xb_get_solution(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float64)
+        self._check(self.L.xb_get_solution(self.h, out.ctypes.data, n.value, None))
+        return out
+
+    def array(self, name, dtype):
+        n = ctypes.c_size_t()
+        if self.L.xb_get_array(self.h, name.encode(), None, 0, ctypes.byref(n)):
+            raise KeyError(name)
+        out = np.empty(n.value // np.dtype(dtype).itemsize, dtype)
+        self.L.xb_get_array(self.h, name.encode(), out.ctypes.data, n.value, None)
+        return out
+
+    def scalar(self, name):
+        v = ctypes.c_double()
+        if self.L.xb_get_scalar(self.h, name.encode(), ctypes.byref(v)):
+            raise KeyError(name)
+        return v.value
+
+    def launches(self):
+        return self.L.xb_kernel_launches(self.h)
+
+    @property
+    def w(self):
+        return int(self.scalar("w"))
+
+    @property
+    def hgt(self):
+        return int(self.scalar("h"))

@@ -1,0 +1,100 @@
+"""Seeded synthetic template/science frame pairs.
+
+Stand-ins for the survey frames the reference measures on (they are not
+available): point sources with pixel-integrated Gaussian PSFs on a Poisson
+sky with Gaussian read noise.  The science frame is the template scene scaled
+by `scale`, seen through a broader PSF, plus a linear background, with a few
+variable sources.  Optional cosmic-ray hits and clipped saturated stars.
+Counter-based RNG (Philox) seeded per configuration, so a (config, frame)
+pair is reproducible on any machine with the same numpy.
+"""
+import numpy as np
+from scipy.special import erf
+
+CONFIGS = {
+    # 512x512, 1500 sources, FWHM 2.5 (template) / 3.5 (science)
+    1: dict(size=512, n_src=1500, fwhm_t=(2.5, 2.5), fwhm_s=(3.5, 3.5),
+            flux=(1e3, 1e6), cr_frac=0.0, n_sat=0, stamps=10,
+            saturation=None),
+    # 2048x2048, 20k sources, FWHM varying across the field, 1% cosmic-ray
+    # pixels, 40 saturated stars; the detector saturates at 6e4 (every pixel
+    # is clipped there and threshHigh sits at that level), 16x16 stamps
+    2: dict(size=2048, n_src=20000, fwhm_t=(2.2, 3.2), fwhm_s=(3.0, 4.2),
+            flux=(1e3, 1e6), cr_frac=0.01, n_sat=40, stamps=16,
+            saturation=6e4),
+}
+
+
+def _render(img, xs, ys, fluxes, sigmas):
+    """Adds pixel-integrated Gaussians (one sigma per source) into img."""
+    h, w = img.shape
+    r = int(np.ceil(4.0 * sigmas.max())) + 1
+    off = np.arange(-r, r + 1)
+    cx = np.floor(xs).astype(np.int64)
+    cy = np.floor(ys).astype(np.int64)
+    px = cx[:, None] + off[None, :]                      # (n, k)
+    py = cy[:, None] + off[None, :]
+    s2 = (sigmas * np.sqrt(2.0))[:, None]
+    gx = 0.5 * (erf((px + 0.5 - xs[:, None]) / s2) - erf((px - 0.5 - xs[:, None]) / s2))
+    gy = 0.5 * (erf((py + 0.5 - ys[:, None]) / s2) - erf((py - 0.5 - ys[:, None]) / s2))
+    vals = fluxes[:, None, None] * gy[:, :, None] * gx[:, None, :]   # (n, ky, kx)
+    X = np.broadcast_to(px[:, None, :], vals.shape)
+    Y = np.broadcast_to(py[:, :, None], vals.shape)
+    ok = (X >= 0) & (X < w) & (Y >= 0) & (Y < h)
+    idx = (Y[ok] * w + X[ok]).astype(np.int64)
+    img += np.bincount(idx, weights=vals[ok], minlength=h * w).reshape(h, w)
+
+
+def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over):
+    """Returns (template, science, info) for BASELINE configuration `config`.
+
+    frame: index of the pair within a batch (changes the seed).
+    """
+    cfg = dict(CONFIGS[config])
+    if size is not None:
+        cfg["size"] = size
+    if n_src is not None:
+        cfg["n_src"] = n_src
+    cfg.update(over)
+    rng = np.random.Generator(np.random.Philox(key=config * 1000003 + frame))
+    n = cfg["size"]
+    sky, rn, scale = 1000.0, 5.0, 1.1
+    ns = cfg["n_src"]
+    xs = rng.uniform(0, n - 1, ns)
+    ys = rng.uniform(0, n - 1, ns)
+    lf = np.log10(cfg["flux"])
+    flux = 10.0 ** rng.uniform(lf[0], lf[1], ns)
+    sat = np.zeros(ns, bool)
+    if cfg["n_sat"]:
+        k = rng.choice(ns, cfg["n_sat"], replace=False)
+        flux[k] = 10.0 ** rng.uniform(6.5, 7.5, cfg["n_sat"])
+        sat[k] = True
+    var = rng.choice(ns, min(15, ns), replace=False)
+    flux_s = flux * scale
+    flux_s[var] *= 1.0 + rng.uniform(-0.2, 0.2, len(var))
+
+    def fwhm_at(rng_fwhm):
+        a, b = rng_fwhm
+        return a + (b - a) * xs / max(n - 1, 1)
+
+    c = 1.0 / (2.0 * np.sqrt(2.0 * np.log(2.0)))
+    sig_t = fwhm_at(cfg["fwhm_t"]) * c
+    sig_s = fwhm_at(cfg["fwhm_s"]) * c
+    T = np.zeros((n, n))
+    S = np.zeros((n, n))
+    _render(T, xs, ys, flux, sig_t)
+    _render(S, xs, ys, flux_s, sig_s)
+    xx = np.arange(n)[None, :].repeat(n, 0)
+    S += 50.0 + 0.01 * xx
+    T = rng.poisson(T + sky).astype(np.float64) + rng.normal(0.0, rn, T.shape)
+    S = rng.poisson(S + sky).astype(np.float64) + rng.normal(0.0, rn, S.shape)
+    if cfg["cr_frac"] > 0:
+        for img in (T, S):
+            m = rng.random(img.shape) < cfg["cr_frac"]
+            img[m] += rng.uniform(5e3, 5e4, int(m.sum()))
+    if cfg["saturation"]:
+        np.minimum(T, cfg["saturation"], out=T)
+        np.minimum(S, cfg["saturation"], out=S)
+    info = dict(config=config, frame=frame, stamps=cfg["stamps"], size=n, n_src=ns,
+                threshHigh=cfg["saturation"] or 25000.0)
+    return T.astype(dtype), S.astype(dtype), info
