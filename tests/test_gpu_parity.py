@@ -1,8 +1,10 @@
 """GPU parity: the plain CUDA path against the CPU oracle on the same inputs.
 
-Integer / index results (masks, stamp and substamp sets, rejection sets) and
-every FP64 quantity that decides one of them must be bit-identical; the
-output images are compared within the FP tolerances stated per test.
+Integer / index results (masks, stamp and substamp sets, test-stamp and
+rejection sets) and every FP64 quantity that decides one of them must be
+bit-identical.  The convolved and difference images use fused multiply-adds
+on the GPU and plain products in the oracle; they are compared within
+1e-11 of the frame's pixel scale.
 """
 import numpy as np
 import pytest
@@ -21,25 +23,25 @@ def bit_equal(a, b):
 CASES = ["test01", "config1", "config2"]
 
 
+def case_inputs(name, test01):
+    from xbach.synth import make_pair
+    if name == "test01":
+        return test01["T"].astype(np.float32), test01["S"].astype(np.float32), {}
+    cfg = int(name[-1])
+    T, S, info = make_pair(cfg)
+    return T, S, dict(stampsx=info["stamps"], stampsy=info["stamps"],
+                      threshHigh=info["threshHigh"])
+
+
 @pytest.fixture(scope="module", params=CASES)
 def pair(request, oracle, test01):
     import xbach
-    from xbach.synth import make_pair
-    if request.param == "test01":
-        T, S = test01["T"].astype(np.float32), test01["S"].astype(np.float32)
-        kw = {}
-    else:
-        cfg = int(request.param[-1])
-        T, S, info = make_pair(cfg)
-        kw = dict(stampsx=info["stamps"], stampsy=info["stamps"],
-                  threshHigh=info["threshHigh"])
+    T, S, kw = case_inputs(request.param, test01)
     ref = oracle.run(oracle.default_params(**kw), T.astype(np.float64),
                      S.astype(np.float64), keep_w=True)
     assert ref.status == 0
     ctx = xbach.Context(xbach.default_params(**kw), trace=True)
-    ctx.init(T, S)
-    ctx.sss()
-    ctx.cmv()
+    ctx.run_all(T, S)
     return request.param, ref, ctx
 
 
@@ -78,5 +80,73 @@ def test_sss_mask(pair):
 def test_cmv_bit_exact(pair, name):
     _, ref, ctx = pair
     a, b = ctx.array(name, np.float64), ref.array(name, np.float64)
-    assert a.shape == b.shape
     assert bit_equal(a, b), (name, np.abs(a - b).max())
+
+
+@pytest.mark.parametrize("name", ["kernel_sums0", "kernel_sums1", "cd_matrix0",
+                                  "cd_matrix1", "cd_solution0", "cd_solution1",
+                                  "cd_sig0", "cd_sig1"])
+def test_cd_bit_exact(pair, name):
+    _, ref, ctx = pair
+    try:
+        b = ref.array(name, np.float64)
+    except KeyError:
+        pytest.skip(f"{name}: direction had no test stamps")
+    a = ctx.array(name, np.float64)
+    assert bit_equal(a, b), (name, np.nanmax(np.abs(a - b)))
+
+
+def test_cd_decision(pair):
+    _, ref, ctx = pair
+    for k in ("cd_test0", "cd_test1"):
+        try:
+            b = ref.array(k, np.int32)
+        except KeyError:
+            continue
+        assert np.array_equal(ctx.array(k, np.int32), b), k
+    for k in ("merit0", "merit1"):
+        assert bit_equal(np.array([ctx.scalar(k)]), np.array([ref.scalar(k)])), k
+    assert ctx.scalar("convTemplate") == ref.scalar("convTemplate")
+
+
+def test_ksc_rejection_sets_identical(pair):
+    _, ref, ctx = pair
+    assert ctx.scalar("ksc_iterations") == ref.scalar("ksc_iterations")
+    assert np.array_equal(ctx.array("ksc_rejects", np.int32), ref.array("ksc_rejects", np.int32))
+    assert np.array_equal(ctx.array("cur", np.int32), ref.array("cur", np.int32))
+
+
+@pytest.mark.parametrize("name", ["ksc_matrix0", "solution", "ksc_sig_last"])
+def test_ksc_bit_exact(pair, name):
+    _, ref, ctx = pair
+    a, b = ctx.array(name, np.float64), ref.array(name, np.float64)
+    assert bit_equal(a, b), (name, np.nanmax(np.abs(a - b)))
+
+
+def test_kernel_sum_bit_exact(pair):
+    _, ref, ctx = pair
+    assert bit_equal(np.array([ctx.scalar("kernSum")]), np.array([ref.scalar("kernSum")]))
+
+
+def test_final_mask_identical(pair):
+    _, ref, ctx = pair
+    assert np.array_equal(ctx.array("mask", np.uint16), ref.array("mask", np.uint16))
+
+
+@pytest.mark.parametrize("name", ["conv", "diff"])
+def test_images_within_tolerance(pair, name):
+    _, ref, ctx = pair
+    a, b = ctx.array(name, np.float64), ref.array(name, np.float64)
+    scale = np.abs(ref.array("conv", np.float64)).max()
+    # FMA (GPU) against separate multiply/add (oracle): 441-term sums
+    assert np.abs(a - b).max() <= 1e-11 * scale
+    # masked and border pixels carry the same 1e-30 marker
+    assert np.array_equal(a == 1e-30, b == 1e-30)
+
+
+def test_float_images_match_fp64(pair):
+    import xbach
+    _, ref, ctx = pair
+    f = ctx.image(xbach.XB_IMG_DIFF, f64=False)
+    d = ctx.image(xbach.XB_IMG_DIFF, f64=True)
+    assert np.array_equal(f, d.astype(np.float32))

@@ -194,7 +194,7 @@ class Context:
 
     # ---- results ----
     def image(self, which, f64=True):
-        n = self.w * self.h
+        n = self.w * self.hgt
         out = np.empty(n, np.float64 if f64 else np.float32)
         fn = self.L.xb_get_image_f64 if f64 else self.L.xb_get_image
         self._check(fn(self.h, which, out.ctypes.data))
