@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 X-BACH difference-imaging path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--mode plain|mixed]
+
+Workload: BASELINE configuration 2 - a 2048x2048 FP32 template/science pair
+(seeded synthetic field: 20k sources, FWHM varying across the field, 1 %
+cosmic-ray pixels, 40 saturated stars, detector saturation 6e4), 16x16 stamps,
+49 basis functions, spatial kernel order 2, background order 1.  One step is
+one difference image: init (mask) -> sss -> cmv -> cd -> ksc -> conv -> sub.
+
+value: difference images per second with T and S already resident in HBM,
+timed with CUDA events on the library's stream, L2 flushed (256 MB write)
+before every step, max over ranks.  e2e: the same through xb_run() with the
+host->device copy of both FP32 inputs from pinned memory and the
+device->host read of the conv and diff images inside the timed region.
+
+N > 1 (torchrun): replicas - every rank runs its own frame pairs on its own
+GPU; the only cross-rank traffic is the barrier and the max of the timings.
+
+--impl reference: the reference's CPU path.  The reference cannot be built
+here (OpenCL and CCfits are absent), so this arm times the repository's FP64
+C++ restatement of it (oracle/, OpenMP over all host threads) on the same
+frame pair; rank 0 only.
+"""
+import argparse
+import ctypes
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = pathlib.Path(__file__).resolve().parent
+PKG = REPO / "thesis-emx-bach_gb300"
+sys.path.insert(0, str(PKG))
+sys.path.insert(0, str(REPO / "tests"))
+
+METRIC = "difference-images/s at 2048², chosen vs plain GPU at ≤1e-3σ; % HBM/TC peak"
+UNIT = "difference-images/s"
+WORKLOAD = ("config 2: 2048x2048 FP32 template/science pair, 20k sources, FWHM 2.2-3.2/3.0-4.2 px, "
+            "1% cosmic-ray pixels, 40 saturated stars, saturation 6e4 (threshHigh), 16x16 stamps, "
+            "49 basis functions (3 Gaussians, degrees 6/4/2), kernel order 2, background order 1")
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def frame_params(xbach_or_oracle, info, mode=None):
+    kw = dict(stampsx=info["stamps"], stampsy=info["stamps"], threshHigh=info["threshHigh"])
+    if mode is not None:
+        kw["mode"] = mode
+    return xbach_or_oracle.default_params(**kw)
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in pathlib.Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_frames_per_s(T, S, info, runs):
+    import build_native
+    build_native.build_oracle()
+    from xbach_testlib import Oracle
+    o = Oracle()
+    p = frame_params(o, info)
+    T64, S64 = T.astype("float64"), S.astype("float64")
+    threads = os.cpu_count() or 1
+    times = []
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        r = o.run(p, T64, S64, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        assert r.status == 0, r.status
+        del r
+    return runs / sum(times), threads, times
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from xbach.synth import make_pair
+    T, S, info = make_pair(2)
+    if args.warmup > 0:
+        cpu_frames_per_s(T, S, info, args.warmup)
+    fps, threads, times = cpu_frames_per_s(T, S, info, args.steps)
+    total = sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded config-2 field)",
+        "config": {"workload": WORKLOAD, "implementation": "FP64 C++ restatement of the reference "
+                   "CPU path (the reference needs OpenCL + CCfits, absent here)"},
+        "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full config-2 frame pairs, one per step"},
+        "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- roofline --
+def roofline_for(name, ms_per_launch, n_pix, mode, hbm_peak):
+    """Algorithmic bytes of one launch of the dominant kernel (per-pixel byte
+    counts are derived in the design doc) and the achieved bandwidth."""
+    if name == "conv_sub":
+        # reads I, O (FP32), writes mask (2 B), conv and diff (FP32; plain
+        # mode also the FP64 copies)
+        per_px = 4 + 4 + 2 + 4 + 4 + (16 if mode == "plain" else 0)
+        traffic_bytes = per_px * n_pix
+    else:
+        return None
+    achieved = traffic_bytes / (ms_per_launch * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None, "kernel": name,
+            "algorithmic_bytes_per_launch": traffic_bytes, "ms_per_launch": ms_per_launch}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--cpu-runs", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local = dist_env()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+        __graft_entry__._paths()
+    import xbach
+    from xbach.synth import make_pair
+
+    T, S, info = make_pair(2, frame=rank)
+    h, w = T.shape
+    n_pix = w * h
+    mode = xbach.XB_MODE_PLAIN if args.mode == "plain" else xbach.XB_MODE_MIXED
+    ctx = xbach.Context(frame_params(xbach, info, mode), device=local)
+    dT = torch.from_numpy(T).cuda()
+    dS = torch.from_numpy(S).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def pipeline():
+        ctx.init_device(dT.data_ptr(), dS.data_ptr(), w, h)
+        ctx.sss()
+        ctx.cmv()
+        ctx.cd()
+        ctx.ksc()
+        ctx.conv()
+        ctx.sub()
+
+    for _ in range(args.warmup):
+        pipeline()
+    torch.cuda.synchronize()
+    ctx.set_option("time_kernels", 1)
+    launches0 = ctx.launches()
+    total_ms = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if world > 1:
+                dist.barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            pipeline()
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+        torch.cuda.synchronize()
+    launches = ctx.launches() - launches0
+    kernels = {}
+    for name in ("mask_input", "spread_mask", "stamp_stats", "find_substamps", "compact_stamps",
+                 "fill_w", "fill_finish", "gram_qb", "stamp_test_fit", "cd_select", "weights",
+                 "stamp_dots", "build_matrix", "build_rhs", "global_lu", "global_lubksb",
+                 "kernel_sum", "sigs", "cd_merit", "ksc_check", "conv_sub"):
+        ms, n = ctx.kernel_time(name)
+        if n:
+            kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}
+    ctx.set_option("time_kernels", 0)
+    clocks = clk.summary()
+    t_max = total_ms
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * args.steps / (t_max / 1000.0)
+
+    # ---- end to end through xb_run with pinned host buffers ----
+    hT = torch.from_numpy(T).pin_memory()
+    hS = torch.from_numpy(S).pin_memory()
+    hC = torch.empty((h, w), dtype=torch.float32).pin_memory()
+    hD = torch.empty((h, w), dtype=torch.float32).pin_memory()
+    L = xbach.lib()
+
+    def run_e2e():
+        rc = L.xb_run(ctx.h, ctypes.c_void_p(hT.data_ptr()), ctypes.c_void_p(hS.data_ptr()), w, h,
+                      ctypes.c_void_p(hC.data_ptr()), ctypes.c_void_p(hD.data_ptr()))
+        if rc:
+            raise RuntimeError(L.xb_last_error(ctx.h).decode())
+
+    run_e2e()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run_e2e()
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+           "h2d_bytes_per_step": 2 * 4 * n_pix, "d2h_bytes_per_step": 2 * 4 * n_pix}
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+    hbm_peak, _, peak_src = measured_peaks()
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_total"]) if kernels else None
+    roof = None
+    if "conv_sub" in kernels:
+        cs = kernels["conv_sub"]
+        roof = roofline_for("conv_sub", cs["ms_total"] / cs["launches"], n_pix, args.mode, hbm_peak)
+    if roof is not None:
+        roof["peak_source"] = peak_src
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.mode == "plain" else "f32",
+        "data": "synthetic (seeded config-2 field)",
+        "config": {"workload": WORKLOAD, "mode": args.mode, "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every step (256 MB write)",
+                   "inputs": "device-resident FP32 T,S"},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+        "dominant_kernel": dominant, "kernels": kernels,
+    }
+    if world == 1 and args.cpu_runs > 0:
+        fps, threads, _ = cpu_frames_per_s(T, S, info, args.cpu_runs)
+        line["cpu_baseline"] = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{args.cpu_runs} full config-2 frame pairs"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -117,7 +117,10 @@ int xb_ctx_destroy(xb_ctx* ctx);
 /* Human-readable message for the last failing call on this context. */
 const char* xb_last_error(const xb_ctx* ctx);
 /* Context options.  "trace" (0/1): keep host copies of the intermediate
- * results of every stage for xb_get_array (parity checks; costs copies). */
+ * results of every stage for xb_get_array (parity checks; costs copies).
+ * "time_kernels" (0/1): time the main kernels with CUDA events on the
+ * context stream; xb_get_scalar("kt:<kernel>:ms" / "kt:<kernel>:n") returns
+ * the accumulated milliseconds / launch count (setting it resets them). */
 int xb_set_option(xb_ctx* ctx, const char* name, long long value);
 
 /* ---- stage API (include/bach.h:66-87) ------------------------------------ */
@@ -179,6 +182,9 @@ int xb_get_scalar(xb_ctx* ctx, const char* name, double* out);
 /* Number of this library's kernels launched since the context was created
  * (for benchmark accounting). */
 long long xb_kernel_launches(const xb_ctx* ctx);
+/* The CUDA stream (cudaStream_t) all of the context's work runs on, for
+ * callers that record events or order their own work against it. */
+int xb_get_stream(xb_ctx* ctx, void** stream);
 
 /* ---- FITS I/O (src/fitsUtil.cpp:8-64 without CCfits) -------------------- */
 /* Reads the primary HDU (BITPIX -32 or -64) into a newly malloc'ed FP64

@@ -172,8 +172,14 @@ const char* xb_last_error(const xb_ctx* c) { return c ? c->lastError.c_str() : "
 int xb_set_option(xb_ctx* c, const char* name, long long value) {
   if(!c || !name) return XB_ERR_ARG;
   std::string n(name);
-  if(n == "trace") c->trace = value != 0;
-  else return XB_ERR_ARG;
+  if(n == "trace") {
+    c->trace = value != 0;
+  } else if(n == "time_kernels") {
+    c->timeKernels = value != 0;
+    c->kt.total.clear();
+  } else {
+    return XB_ERR_ARG;
+  }
   return XB_OK;
 }
 
@@ -341,6 +347,16 @@ int xb_get_array(xb_ctx* c, const char* name, void* out, size_t cap, size_t* nby
 
 int xb_get_scalar(xb_ctx* c, const char* name, double* out) {
   if(!c || !name || !out) return XB_ERR_ARG;
+  const std::string nm(name);
+  if(nm.rfind("kt:", 0) == 0) {  // kt:<kernel>:ms | kt:<kernel>:n
+    int rc = guarded(c, [&] { ktCollect(c); });
+    if(rc != XB_OK) return rc;
+    const size_t colon = nm.rfind(':');
+    auto kt = c->kt.total.find(nm.substr(3, colon - 3));
+    if(kt == c->kt.total.end() || colon <= 3) return XB_ERR_ARG;
+    *out = nm.substr(colon + 1) == "n" ? (double)kt->second.second : kt->second.first;
+    return XB_OK;
+  }
   auto it = c->scalars.find(name);
   if(it == c->scalars.end()) return XB_ERR_ARG;
   *out = it->second;
@@ -348,5 +364,11 @@ int xb_get_scalar(xb_ctx* c, const char* name, double* out) {
 }
 
 long long xb_kernel_launches(const xb_ctx* c) { return c ? c->launches : 0; }
+
+int xb_get_stream(xb_ctx* c, void** stream) {
+  if(!c || !stream) return XB_ERR_ARG;
+  *stream = (void*)c->stream;
+  return XB_OK;
+}
 
 }  // extern "C"

@@ -225,6 +225,7 @@ void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
   size_t smemFill = (size_t)(tw * tw + th * tw + 2) * sizeof(float) + 2 * g.fK * sizeof(double);
   dim3 grid(nList, nGroups);
   double* W = (double*)S.W;
+  { KT_SCOPE(c, "fill_w");
   if(c->imgIsF64)
     k_fill_w<double><<<grid, FILL_THREADS, smemFill, c->stream>>>(
         (const double*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, c->dFX,
@@ -234,13 +235,17 @@ void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
         (const float*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, c->dFX,
         c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, W);
   XB_LAUNCHED(c);
+  }
   int2* bgXY = buf<int2>(c, "bgXY", g.nBG);
+  { KT_SCOPE(c, "fill_finish");
   k_fill_finish<<<nList, FILL_THREADS, 0, c->stream>>>(dList, S.count, S.cur, S.ssxy, g.maxSS,
                                                        c->dKx, c->dKy, g.nPSF, bgXY, g.nBG,
                                                        g.hSS, c->w, c->h, g.wRows, W);
   XB_LAUNCHED(c);
+  }
   size_t smemGram = ((size_t)(g.qCount - 1) * (GQ_KT + 1) + (size_t)g.wCols) * sizeof(double);
   const int other = 1 - imgConv;
+  { KT_SCOPE(c, "gram_qb");
   if(c->imgIsF64)
     k_gram_qb<double><<<nList, FILL_THREADS, smemGram, c->stream>>>(
         (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
@@ -250,6 +255,7 @@ void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
         (const float*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
         g.wRows, g.qCount, W, S.Q, S.B);
   XB_LAUNCHED(c);
+  }
 }
 
 void stageCmv(xb_ctx* c) {

@@ -226,18 +226,22 @@ void stageConvSub(xb_ctx* c, bool doSub) {
   const int I = c->chosen, O = 1 - c->chosen;
   dim3 grid(a.xSteps, ySteps);
   if(c->imgIsF64) {
+    { KT_SCOPE(c, "conv_sub");
     k_conv_sub_f64<double><<<grid, CONV_THREADS, smem, c->stream>>>(
         (const double*)c->img[I], (const double*)c->img[O], c->dSol, c->dVec, ks, a, c->mask,
         c->convD, c->convF, c->diffD, c->diffF);
     XB_LAUNCHED(c);
+    }
     k_border<double><<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
         (const double*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convD, c->convF,
         c->diffD, c->diffF);
   } else {
+    { KT_SCOPE(c, "conv_sub");
     k_conv_sub_f64<float><<<grid, CONV_THREADS, smem, c->stream>>>(
         (const float*)c->img[I], (const float*)c->img[O], c->dSol, c->dVec, ks, a, c->mask,
         c->convD, c->convF, c->diffD, c->diffF);
     XB_LAUNCHED(c);
+    }
     k_border<float><<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
         (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convD, c->convF,
         c->diffD, c->diffF);

@@ -140,6 +140,32 @@ void* poolGet(xb_ctx* c, const char* name, size_t bytes) {
   return p;
 }
 
+cudaEvent_t ktEvent(xb_ctx* c) {
+  if(!c->kt.pool.empty()) {
+    cudaEvent_t e = c->kt.pool.back();
+    c->kt.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  XB_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void ktCollect(xb_ctx* c) {
+  if(c->kt.pending.empty()) return;
+  XB_CUDA(cudaStreamSynchronize(c->stream));
+  for(auto& o : c->kt.pending) {
+    float ms = 0.f;
+    XB_CUDA(cudaEventElapsedTime(&ms, o.a, o.b));
+    auto& t = c->kt.total[o.name];
+    t.first += ms;
+    t.second += 1;
+    c->kt.pool.push_back(o.a);
+    c->kt.pool.push_back(o.b);
+  }
+  c->kt.pending.clear();
+}
+
 // ---------------------------------------------------------------- kernels --
 
 // maskInput (cl_kern/ini.cl:15-35).  Four pixels per thread.
@@ -212,6 +238,7 @@ void stageInitMask(xb_ctx* c) {
   const int border = c->p.hSStampWidth + c->p.hKernelWidth;
   const long long n = (long long)c->w * c->h;
   int blocks = (int)std::min<long long>((n + 1023) / 1024, (long long)c->smCount * 16);
+  { KT_SCOPE(c, "mask_input");
   if(c->imgIsF64)
     k_mask_input<double><<<blocks, 256, 0, c->stream>>>(
         (const double*)c->img[0], (const double*)c->img[1], c->mask, c->w, c->h,
@@ -221,13 +248,16 @@ void stageInitMask(xb_ctx* c) {
         (const float*)c->img[0], (const float*)c->img[1], c->mask, c->w, c->h,
         border, c->p.threshHigh, c->p.threshLow);
   XB_LAUNCHED(c);
+  }
   const int spreadWidth = (int)(c->p.hKernelWidth * c->p.inSpreadMaskFactor);
   const int r = spreadWidth / 2;
   if(r > 0) {
     dim3 grid((c->w + SP_TX - 1) / SP_TX, (c->h + SP_TY - 1) / SP_TY);
     size_t smem = (size_t)(SP_TX + 2 * r) * (SP_TY + 2 * r) + (size_t)(SP_TY + 2 * r) * SP_TX;
+    { KT_SCOPE(c, "spread_mask");
     k_spread_mask<<<grid, SP_TX * 4, smem, c->stream>>>(c->mask, c->w, c->h, r);
     XB_LAUNCHED(c);
+    }
   }
 }
 

@@ -877,11 +877,14 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   StampSetDev& S = c->set[si];
   const int2* kp = kernelPowers(c);
   const int nW = nList * g.nComp2;
+  { KT_SCOPE(c, "weights");
   k_weights<<<(nW + 255) / 256, 256, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.ssxy, g.maxSS,
                                                     kp, g.nComp2, c->w, c->h, f.wts);
   XB_LAUNCHED(c);
+  }
   if(nList > 0) {
     const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + g.wCols) * sizeof(double);
+    { KT_SCOPE(c, "stamp_dots");
     if(c->imgIsF64)
       k_stamp_dots<double><<<nList, DOT_THREADS, smem, c->stream>>>(
           f.list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
@@ -891,17 +894,22 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
           f.list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
           g.nBG, (const float*)c->img[other], c->w, c->h, f.dots, f.stride);
     XB_LAUNCHED(c);
+    }
   }
   const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
+  { KT_SCOPE(c, "build_matrix");
   k_build_matrix<<<(int)std::min<long long>((nTri + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
       f.list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, f.dots, f.stride, g.nComp1, g.nComp2,
       g.nBG, g.matSize, f.M);
   XB_LAUNCHED(c);
+  }
   const int bgBase = g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + (cpuRhs ? g.nBG : 0);
+  { KT_SCOPE(c, "build_rhs");
   k_build_rhs<<<(g.nSol + 127) / 128, 128, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.B,
                                                           g.qCount, f.wts, f.dots, f.stride, bgBase,
                                                           g.nComp1, g.nComp2, g.nBG, g.nSol, dSol);
   XB_LAUNCHED(c);
+  }
   if(c->trace) {
     const int ld = g.matSize + 1;
     std::string key = cpuRhs ? "ksc_matrix" : ("cd_matrix" + std::to_string(si));
@@ -928,11 +936,15 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  { KT_SCOPE(c, "global_lu");
   XB_CUDA(cudaLaunchKernelEx(&cfg, k_global_lu<CL>, f.M, n, f.piv, f.singular));
   XB_LAUNCHED(c);
+  }
   const size_t smemS = (size_t)(2 * (n + 1)) * sizeof(double) + (size_t)(n + 1) * sizeof(int);
+  { KT_SCOPE(c, "global_lubksb");
   k_global_lubksb<<<1, 256, smemS, c->stream>>>(f.M, n, f.piv, dSol);
   XB_LAUNCHED(c);
+  }
 }
 
 static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const double* dSol,
@@ -943,6 +955,7 @@ static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const do
   const int pix = g.wCols, rc = (pix + 31) / 32;
   const size_t smem = ((size_t)g.nPSF + rc * 32 + rc) * sizeof(double) + (size_t)(rc * 32 + rc) * sizeof(int);
   const int other = 1 - convImg;
+  { KT_SCOPE(c, "sigs");
   if(c->imgIsF64)
     k_sigs<double><<<nList, SIG_THREADS, smem, c->stream>>>(
         dList, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
@@ -954,12 +967,15 @@ static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const do
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const float*)c->img[convImg],
         (const float*)c->img[other], c->mask, c->w, c->h, dSig);
   XB_LAUNCHED(c);
+  }
 }
 
 void kernelSumLaunch(xb_ctx* c, const double* dSol, double xf, double yf, int tree, double* dOut) {
+  { KT_SCOPE(c, "kernel_sum");
   k_kernel_sum<<<1, 256, 0, c->stream>>>(dSol, c->dVec, c->g.nPSF, c->p.kernelOrder, c->g.fK, xf, yf,
                                          tree, dOut);
   XB_LAUNCHED(c);
+  }
 }
 
 void stageCd(xb_ctx* c) {
@@ -978,13 +994,17 @@ void stageCd(xb_ctx* c) {
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
     if(S.n > 0) {
+      { KT_SCOPE(c, "stamp_test_fit");
       k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, ks[si]);
       XB_LAUNCHED(c);
+      }
     }
+    { KT_SCOPE(c, "cd_select");
     k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, c->p.sigClipAlpha, c->p.sigKernFit,
                                           f.flags, f.cs, f.cs2, testIdx[si], nTest + si,
                                           stats + 2 * si);
     XB_LAUNCHED(c);
+    }
   }
   std::vector<int> hT = toHost(c, nTest, 2);
   const int solStride = std::max(g.nSol, g.matSize + 1);
@@ -1001,9 +1021,11 @@ void stageCd(xb_ctx* c) {
     kernelSumLaunch(c, sol, (0 - 0.5 * c->w) / (0.5 * c->w), (0 - 0.5 * c->h) / (0.5 * c->h), 1,
                     kMean + si);
     computeSigs(c, si, f.list, hT[si], sol, si, f.sig);
+    { KT_SCOPE(c, "cd_merit");
     k_cd_merit<<<1, 256, 0, c->stream>>>(f.sig, hT[si], kMean + si, c->p.sigClipAlpha,
                                          f.scratchD, f.flags, f.cs, f.cs2, merit + si);
     XB_LAUNCHED(c);
+    }
     std::vector<double> m = toHost(c, merit + si, 1);
     c->merit[si] = m[0];
     if(c->trace) {
@@ -1046,10 +1068,12 @@ void stageKsc(xb_ctx* c) {
     computeSigs(c, si, allList, n, c->dSol, si, f.sig);
     k_zero_ints<<<1, 32, 0, c->stream>>>(outs, 4);
     XB_LAUNCHED(c);
+    { KT_SCOPE(c, "ksc_check");
     k_ksc_check<<<1, 256, 0, c->stream>>>(f.sig, n, S.count, S.cur, c->p.sigClipAlpha,
                                           c->p.sigKernFit, chi2, f.flags, f.cs, f.cs2, refill,
                                           outs, passOf);
     XB_LAUNCHED(c);
+    }
     std::vector<int> o = toHost(c, outs, 3);
     const int nRefill = o[0];
     check = nRefill > 0;

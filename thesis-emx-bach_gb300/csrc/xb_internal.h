@@ -75,6 +75,19 @@ struct StampSetDev {
   std::vector<int> h_count, h_cur;
 };
 
+// Optional per-kernel CUDA-event timing (option "time_kernels"): launches
+// wrapped in KT_SCOPE record events on the context stream; totals are
+// collected on request.
+struct KTimers {
+  std::vector<cudaEvent_t> pool;
+  struct Open {
+    std::string name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Open> pending;
+  std::map<std::string, std::pair<double, long long>> total;  // ms, launches
+};
+
 struct DevBuf {  // simple grow-only device allocation
   void* p = nullptr;
   size_t bytes = 0;
@@ -138,6 +151,8 @@ struct xb_ctx {
   // bookkeeping
   long long launches = 0;
   int trace = 0;
+  int timeKernels = 0;
+  xb::KTimers kt;
   std::string lastError;
   std::map<std::string, std::vector<uint8_t>> arrays;
   std::map<std::string, double> scalars;
@@ -201,6 +216,31 @@ void toDevice(xb_ctx* c, T* d, const std::vector<T>& h) {
     XB_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T),
                             cudaMemcpyHostToDevice, c->stream));
 }
+
+// ---- kernel timers --------------------------------------------------------
+cudaEvent_t ktEvent(xb_ctx* c);
+void ktCollect(xb_ctx* c);
+struct KtScope {
+  xb_ctx* c;
+  const char* name;
+  cudaEvent_t a = nullptr;
+  KtScope(xb_ctx* ctx, const char* n) : c(ctx), name(n) {
+    if(c->timeKernels) {
+      a = ktEvent(c);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~KtScope() {
+    if(a) {
+      cudaEvent_t b = ktEvent(c);
+      cudaEventRecord(b, c->stream);
+      c->kt.pending.push_back({name, a, b});
+    }
+  }
+};
+#define XB_CAT2(a, b) a##b
+#define XB_CAT(a, b) XB_CAT2(a, b)
+#define KT_SCOPE(ctx, name) ::xb::KtScope XB_CAT(kt_scope_, __LINE__)((ctx), (name))
 
 // ---- stage implementations (host orchestration in the .cu files) ---------
 void stageInitMask(xb_ctx* c);

@@ -637,6 +637,7 @@ static void sssPass(xb_ctx* c, int* nKept) {
   const int maxChunks = (fSW * fSW + 31) / 32;
   double* chunkBuf = c->dWork;  // sized by stageSss
   for(int im = 0; im < 2; im++) {
+    { KT_SCOPE(c, "stamp_stats");
     if(c->imgIsF64)
       k_stamp_stats<double><<<nAll, ST_THREADS, 0, c->stream>>>(
           (const double*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
@@ -648,8 +649,10 @@ static void sssPass(xb_ctx* c, int* nKept) {
           c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
           c->p.iqRange, c->skyAll[im], c->fwhmAll[im]);
     XB_LAUNCHED(c);
+    }
   }
   dim3 grid(nAll, 2);
+  { KT_SCOPE(c, "find_substamps");
   if(c->imgIsF64)
     k_find_substamps<double><<<grid, FS_THREADS, 0, c->stream>>>(
         (const double*)c->img[0], (const double*)c->img[1], c->mask, c->geomAll,
@@ -663,12 +666,15 @@ static void sssPass(xb_ctx* c, int* nKept) {
         c->ssvalAll[0], c->cntAll[0], c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w,
         fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit);
   XB_LAUNCHED(c);
+  }
   for(int im = 0; im < 2; im++) {
     StampSetDev& S = c->set[im];
+    { KT_SCOPE(c, "compact_stamps");
     k_compact_stamps<<<1, 256, 0, c->stream>>>(c->cntAll[im], c->ssxyAll[im], c->ssvalAll[im],
                                                nAll, g.maxSS, S.orig, S.count, S.cur, S.ssxy,
                                                S.ssval, c->dIWork + im);
     XB_LAUNCHED(c);
+    }
   }
   std::vector<int> n = toHost(c, c->dIWork, 2);
   nKept[0] = n[0];

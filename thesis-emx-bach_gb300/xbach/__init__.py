@@ -56,8 +56,8 @@ EXPORTS = [
     "xb_init_device_f32", "xb_sss", "xb_cmv", "xb_cd", "xb_ksc", "xb_conv",
     "xb_sub", "xb_run", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
-    "xb_get_scalar", "xb_kernel_launches", "xb_fits_read", "xb_fits_write",
-    "xb_free",
+    "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
+    "xb_fits_write", "xb_free",
 ]
 
 
@@ -96,6 +96,7 @@ def lib():
     L.xb_get_scalar.argtypes = [vp, ctypes.c_char_p, P(d)]
     L.xb_kernel_launches.argtypes = [vp]
     L.xb_kernel_launches.restype = ctypes.c_longlong
+    L.xb_get_stream.argtypes = [vp, P(vp)]
     L.xb_fits_read.argtypes = [ctypes.c_char_p, P(vp), P(i), P(i)]
     L.xb_fits_write.argtypes = [ctypes.c_char_p, vp, i, i]
     L.xb_free.argtypes = [vp]
@@ -228,6 +229,22 @@ class Context:
 
     def launches(self):
         return self.L.xb_kernel_launches(self.h)
+
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        s = ctypes.c_void_p()
+        self._check(self.L.xb_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def set_option(self, name, value):
+        return self._check(self.L.xb_set_option(self.h, name.encode(), int(value)))
+
+    def kernel_time(self, name):
+        """(total ms, launches) of a timed kernel (option time_kernels)."""
+        try:
+            return self.scalar(f"kt:{name}:ms"), int(self.scalar(f"kt:{name}:n"))
+        except KeyError:
+            return 0.0, 0
 
     @property
     def w(self):
