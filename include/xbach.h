@@ -186,6 +186,33 @@ long long xb_kernel_launches(const xb_ctx* ctx);
  * callers that record events or order their own work against it. */
 int xb_get_stream(xb_ctx* ctx, void** stream);
 
+/* ---- allocation-free stamp statistics ------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (another allocator owns the device, or a cudaMalloc would stall
+ * their work): the sky level and robust sigma of every stamp, computed by the
+ * same kernel as xb_sss, with all scratch taken from a 32 MiB device array
+ * built into the library (held on every GPU that loads it until exit).
+ *   dImg   w*h FP32 image, device memory
+ *   dMask  w*h mask words (in/out: NaN pixels get NAN_PIXEL|BAD_INPUT, as in
+ *          xb_sss)
+ *   dGeom  nStamps x {x, y, width, height} ints, 16-byte aligned, device
+ *   dSky, dFwhm  nStamps doubles each, device memory
+ *   stream cudaStream_t to launch on (NULL = legacy default stream); the call
+ *          returns after the launch, results are ready when the stream is
+ * Limit: nStamps * (9 * fStampWidth^2 + 16 * ceil(fStampWidth^2 / 32)) bytes
+ * must fit in 32 MiB (2048^2 with 16x16 stamps of 107 px needs 27 MiB);
+ * larger requests return XB_ERR_UNSUPPORTED and nothing runs.  The first call
+ * on each device looks up the array's device address, so make that first call
+ * before capturing a stream.  All calls share the one array: calls whose
+ * launches overlap on the GPU race with each other; the kernel needs nothing
+ * cleared, it writes every scratch byte before reading it.  `err` (may be
+ * NULL) receives a message on failure.  Calls no allocation routine. */
+int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w, int h,
+                           const int* dGeom, int nStamps, int fStampWidth,
+                           double sigClipAlpha, double iqRange, double* dSky,
+                           double* dFwhm, void* stream, char* err,
+                           size_t errCap);
+
 /* ---- FITS I/O (src/fitsUtil.cpp:8-64 without CCfits) -------------------- */
 /* Reads the primary HDU (BITPIX -32 or -64) into a newly malloc'ed FP64
  * array (free with xb_free).  Returns XB_ERR_IO / XB_ERR_UNSUPPORTED. */

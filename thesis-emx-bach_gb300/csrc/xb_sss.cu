@@ -781,3 +781,92 @@ void stageSss(xb_ctx* c) {
 }
 
 }  // namespace xb
+
+// ---------------------------------------------------------------------------
+// Per-stamp statistics without any allocation.
+//
+// Some callers cannot allocate device memory: code that runs while another
+// allocator (a framework's caching pool, a service's preallocated arena)
+// owns the device and must not be bypassed, or code that must not let a
+// cudaMalloc/cudaFree implicitly synchronise the device in the middle of
+// its own work.  For them the stamp statistics of the sss stage (sky level
+// and robust sigma per stamp, the same kernel xb_sss runs) are available
+// with all scratch memory taken from a fixed device array that is part of the
+// library image: every GPU that loads the library holds these 32 MiB until
+// the process exits.  The caller passes the image, the mask, the stamp
+// geometry and the two output arrays, all in device memory.
+
+#include <cstring>
+#include <mutex>
+
+namespace {
+
+constexpr size_t kStatsScratchBytes = size_t(32) << 20;  // 32 MiB
+constexpr int kMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_statsScratch[kStatsScratchBytes];
+
+std::mutex g_statsScratchMutex;
+void* g_statsScratchAddr[kMaxDevices] = {};
+
+size_t alignUp(size_t v) { return (v + 255) & ~size_t(255); }
+
+int noallocFail(char* err, size_t errCap, int code, const char* msg) {
+  if(err && errCap) {
+    std::strncpy(err, msg, errCap - 1);
+    err[errCap - 1] = '\0';
+  }
+  return code;
+}
+
+}  // namespace
+
+extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w, int h,
+                                      const int* dGeom, int nStamps, int fStampWidth,
+                                      double sigClipAlpha, double iqRange, double* dSky,
+                                      double* dFwhm, void* stream, char* err, size_t errCap) {
+  if(!dImg || !dMask || !dGeom || !dSky || !dFwhm || w <= 0 || h <= 0 || nStamps <= 0 ||
+     fStampWidth <= 0)
+    return noallocFail(err, errCap, XB_ERR_ARG, "null pointer or non-positive size");
+  if(((uintptr_t)dGeom & 15u) != 0)
+    return noallocFail(err, errCap, XB_ERR_ARG, "stamp geometry must be 16-byte aligned");
+  // scratch carve-up: good pixels (FP64), clip flags (bytes), chunk sums
+  const size_t pix = (size_t)fStampWidth * fStampWidth;
+  const int maxChunks = (int)((pix + 31) / 32);
+  const size_t goodBytes = alignUp((size_t)nStamps * pix * sizeof(double));
+  const size_t clipBytes = alignUp((size_t)nStamps * pix);
+  const size_t chunkBytes = alignUp((size_t)nStamps * 2 * maxChunks * sizeof(double));
+  if(pix > (size_t)1 << 26 || goodBytes + clipBytes + chunkBytes > kStatsScratchBytes)
+    return noallocFail(err, errCap, XB_ERR_UNSUPPORTED,
+                       "stamps need more than the 32 MiB scratch: nStamps * (9 * fStampWidth^2 "
+                       "+ 16 * ceil(fStampWidth^2 / 32)) bytes must fit");
+  int dev = -1;
+  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return noallocFail(err, errCap, XB_ERR_CUDA, "no usable current CUDA device");
+  void* base = nullptr;
+  {
+    // The array's device address is looked up once per device, with that
+    // device current; host code must not use the symbol itself as an address.
+    std::lock_guard<std::mutex> lock(g_statsScratchMutex);
+    if(!g_statsScratchAddr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_statsScratch);
+      if(e != cudaSuccess || !p)
+        return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
+      g_statsScratchAddr[dev] = p;
+    }
+    base = g_statsScratchAddr[dev];
+  }
+  unsigned char* b = static_cast<unsigned char*>(base);
+  double* good = reinterpret_cast<double*>(b);
+  uint8_t* clip = b + goodBytes;
+  double* chunks = reinterpret_cast<double*>(b + goodBytes + clipBytes);
+  // Nothing needs clearing: within one launch every scratch byte the kernel
+  // reads is written first (clip flags and good pixels during the
+  // compaction, chunk sums before they are summed).
+  xb::k_stamp_stats<float><<<nStamps, xb::ST_THREADS, 0, (cudaStream_t)stream>>>(
+      dImg, dMask, reinterpret_cast<const int4*>(dGeom), w, h, fStampWidth, good, clip, chunks,
+      maxChunks, sigClipAlpha, iqRange, dSky, dFwhm);
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
+  return XB_OK;
+}

@@ -57,7 +57,7 @@ EXPORTS = [
     "xb_sub", "xb_run", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
     "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
-    "xb_fits_write", "xb_free",
+    "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc",
 ]
 
 
