@@ -1,0 +1,77 @@
+"""The mixed-precision (chosen) path against the plain path and the oracle.
+
+Acceptance (BASELINE metric): the chosen difference image is within 1e-3 of
+the per-pixel noise sigma of the plain GPU result,
+sigma_pix = sqrt(|S| + |conv| + 2 sigma_rn^2) with the frames' read noise
+sigma_rn = 5 ADU (gain 1), over pixels both paths leave unmasked.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIGMA_RN = 5.0
+
+
+def run(mode, T, S, kw, trace=True):
+    import xbach
+    ctx = xbach.Context(xbach.default_params(mode=mode, **kw), trace=trace)
+    ctx.run_all(T, S)
+    return ctx
+
+
+def case(name, test01):
+    from xbach.synth import make_pair
+    if name == "test01":
+        return test01["T"].astype(np.float32), test01["S"].astype(np.float32), {}
+    T, S, info = make_pair(int(name[-1]))
+    return T, S, dict(stampsx=info["stamps"], stampsy=info["stamps"],
+                      threshHigh=info["threshHigh"])
+
+
+@pytest.fixture(scope="module", params=["test01", "config1", "config2"])
+def both(request, test01):
+    import xbach
+    T, S, kw = case(request.param, test01)
+    plain = run(xbach.XB_MODE_PLAIN, T, S, kw)
+    mixed = run(xbach.XB_MODE_MIXED, T, S, kw)
+    return request.param, T, S, plain, mixed
+
+
+def test_same_stamp_sets_and_direction(both):
+    _, _, _, plain, mixed = both
+    for k in ("ss_xy0", "ss_xy1", "ss_count0", "ss_count1"):
+        assert np.array_equal(plain.array(k, np.int32), mixed.array(k, np.int32)), k
+    assert plain.scalar("convTemplate") == mixed.scalar("convTemplate")
+
+
+# test01 (the reference's 330x330 golden case) has a global system with
+# cond ~6e13 and a negative kernel sum; there even rounding the plain path's
+# own FP64 W to FP32 moves the difference image by 1.2e-3 sigma, so FP32
+# storage of W cannot meet 1e-3 sigma on it.  The BASELINE workloads
+# (configs 1 and 2) are held to the metric's 1e-3 sigma.
+SIGMA_BAR = {"test01": 1e-2, "config1": 1e-3, "config2": 1e-3}
+KSUM_BAR = {"test01": 1e-4, "config1": 1e-5, "config2": 1e-5}
+
+
+def test_kernel_sum_close(both):
+    name, _, _, plain, mixed = both
+    assert abs(mixed.scalar("kernSum") / plain.scalar("kernSum") - 1) < KSUM_BAR[name]
+
+
+def test_diff_within_1e3_sigma_of_plain(both):
+    import xbach
+    name, T, S, plain, mixed = both
+    dp = plain.image(xbach.XB_IMG_DIFF)
+    dm = mixed.image(xbach.XB_IMG_DIFF)
+    cp = plain.image(xbach.XB_IMG_CONV)
+    ct = plain.scalar("convTemplate")
+    target = S if ct else T   # the image subtracted from the convolved one
+    ok = (dp != 1e-30) & (dm != 1e-30)
+    assert ok.mean() > 0.5
+    sigma = np.sqrt(np.abs(target) + np.abs(cp) + 2 * SIGMA_RN ** 2)
+    err = np.abs(dm - dp)[ok] / sigma[ok]
+    assert err.max() <= SIGMA_BAR[name], (name, err.max())
+    # masks agree except where the FP32 good-fraction test sits on 0.99
+    mp, mm = plain.array("mask", np.uint16), mixed.array("mask", np.uint16)
+    assert np.mean(mp != mm) < 1e-4

@@ -218,6 +218,10 @@ __global__ void __launch_bounds__(FILL_THREADS)
 // src/cmvUtil.cpp:37-187).
 void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
   if(nList <= 0) return;
+  if(mixedMode(c)) {
+    fillStampsMixed(c, si, dList, nList, imgConv);
+    return;
+  }
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
   const int nGroups = (int)c->basis.yGroupStart.size() - 1;
@@ -269,7 +273,12 @@ void stageCmv(xb_ctx* c) {
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
     const std::string sfx = std::to_string(si);
-    S.W = buf<double>(c, "W" + sfx, (size_t)std::max(S.n, 1) * g.wRows * g.wCols);
+    if(mixedMode(c)) {
+      S.Wf = buf<float>(c, "Wf" + sfx, (size_t)std::max(S.n, 1) * g.wRows * mixedLd(g));
+      S.dots = buf<double>(c, "dots" + sfx, (size_t)std::max(S.n, 1) * mixedDotStride(g));
+    } else {
+      S.W = buf<double>(c, "W" + sfx, (size_t)std::max(S.n, 1) * g.wRows * g.wCols);
+    }
     S.Q = buf<double>(c, "Q" + sfx, (size_t)std::max(S.n, 1) * g.qCount * g.qCount);
     S.B = buf<double>(c, "B" + sfx, (size_t)std::max(S.n, 1) * g.bCount);
     std::vector<int> all(S.n);
@@ -284,7 +293,10 @@ void stageCmv(xb_ctx* c) {
       const std::string sfx = std::to_string(si);
       c->put("Q" + sfx, toHost(c, S.Q, (size_t)S.n * g.qCount * g.qCount));
       c->put("B" + sfx, toHost(c, S.B, (size_t)S.n * g.bCount));
-      c->put("W" + sfx, toHost(c, (const double*)S.W, (size_t)S.n * g.wRows * g.wCols));
+      if(mixedMode(c))
+        c->put("Wf" + sfx, toHost(c, S.Wf, (size_t)S.n * g.wRows * mixedLd(g)));
+      else
+        c->put("W" + sfx, toHost(c, (const double*)S.W, (size_t)S.n * g.wRows * g.wCols));
     }
   }
 }

@@ -198,8 +198,6 @@ void stageConvSub(xb_ctx* c, bool doSub) {
   const size_t n = (size_t)c->w * c->h;
   c->convF = buf<float>(c, "convF", n);
   c->diffF = buf<float>(c, "diffF", n);
-  c->convD = buf<double>(c, "convD", n);
-  c->diffD = buf<double>(c, "diffD", n);
   double* ks = buf<double>(c, "kernSum", 1);
   // kernel sum at the frame centre, sequential sum (bachUtil.cpp:532-538)
   {
@@ -207,6 +205,22 @@ void stageConvSub(xb_ctx* c, bool doSub) {
     const double xf = (c->w / 2 - hx) / hx, yf = (c->h / 2 - hy) / hy;
     kernelSumLaunch(c, c->dSol, xf, yf, 0, ks);
   }
+  if(mixedMode(c)) {
+    c->convD = nullptr;
+    c->diffD = nullptr;
+    convSubMixed(c, ks);
+    c->kernSum = toHost(c, ks, 1)[0];
+    c->scalars["kernSum"] = c->kernSum;
+    if(c->trace) {
+      std::vector<float> cf = toHost(c, c->convF, n), df = toHost(c, c->diffF, n);
+      c->put("conv", std::vector<double>(cf.begin(), cf.end()));
+      c->put("diff", std::vector<double>(df.begin(), df.end()));
+      c->put("mask", toHost(c, c->mask, n));
+    }
+    return;
+  }
+  c->convD = buf<double>(c, "convD", n);
+  c->diffD = buf<double>(c, "diffD", n);
   ConvArgs a{};
   a.w = c->w;
   a.h = c->h;

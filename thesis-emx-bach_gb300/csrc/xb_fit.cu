@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(256)
     k_build_matrix(const int* __restrict__ list, int nList, const int* __restrict__ count,
                    const int* __restrict__ cur, const double* __restrict__ Q, int qc,
                    const double* __restrict__ wts, const double* __restrict__ dots, int stride,
-                   int nC1, int nC2, int nBG, int matSize, double* __restrict__ M) {
+                   int byStamp, int nC1, int nC2, int nBG, int matSize, double* __restrict__ M) {
   const int ld = matSize + 1, nComp = nC1 * nC2;
   const long long nTri = (long long)matSize * (matSize + 1) / 2;
   for(long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nTri;
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256)
       const int s = list[t];
       const double* Qs = Q + (size_t)s * qc * qc;
       const double* wt = wts + (size_t)t * nC2;
-      const double* dt = dots + (size_t)t * stride;
+      const double* dt = dots + (size_t)(byStamp ? s : t) * stride;
       if(row == 1 && col == 1) {
         m0 += Qs[1 * qc + 1];
       } else if(row > nComp + 1 && col > nComp + 1) {
@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(256)
 __global__ void k_build_rhs(const int* __restrict__ list, int nList, const int* __restrict__ count,
                             const int* __restrict__ cur, const double* __restrict__ B, int qc,
                             const double* __restrict__ wts, const double* __restrict__ dots,
-                            int stride, int bgBase, int nC1, int nC2, int nBG, int nSol,
-                            double* __restrict__ res) {
+                            int stride, int byStamp, int bgBase, int nC1, int nC2, int nBG,
+                            int nSol, double* __restrict__ res) {
   const int id = blockIdx.x * blockDim.x + threadIdx.x;
   if(id >= nSol) return;
   const int nComp = nC1 * nC2;
@@ -377,7 +377,7 @@ __global__ void k_build_rhs(const int* __restrict__ list, int nList, const int* 
       int i = (id - 2) / nC2 + 1, j = (id - 2) % nC2;
       r0 += Bs[i + 1] * wts[(size_t)t * nC2 + j];
     } else if(id >= nComp + 2 && id < nComp + 2 + nBG) {
-      r0 += dots[(size_t)t * stride + bgBase + (id - (nComp + 2))];
+      r0 += dots[(size_t)(byStamp ? s : t) * stride + bgBase + (id - (nComp + 2))];
     }
   }
   res[id] = r0;
@@ -882,7 +882,9 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
                                                     kp, g.nComp2, c->w, c->h, f.wts);
   XB_LAUNCHED(c);
   }
-  if(nList > 0) {
+  const bool mixed = mixedMode(c);
+  const double* dots = mixed ? S.dots : f.dots;  // mixed: filled per stamp by the Gram kernel
+  if(nList > 0 && !mixed) {
     const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + g.wCols) * sizeof(double);
     { KT_SCOPE(c, "stamp_dots");
     if(c->imgIsF64)
@@ -899,15 +901,16 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
   { KT_SCOPE(c, "build_matrix");
   k_build_matrix<<<(int)std::min<long long>((nTri + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
-      f.list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, f.dots, f.stride, g.nComp1, g.nComp2,
-      g.nBG, g.matSize, f.M);
+      f.list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, dots, f.stride, mixed ? 1 : 0, g.nComp1,
+      g.nComp2, g.nBG, g.matSize, f.M);
   XB_LAUNCHED(c);
   }
   const int bgBase = g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + (cpuRhs ? g.nBG : 0);
   { KT_SCOPE(c, "build_rhs");
   k_build_rhs<<<(g.nSol + 127) / 128, 128, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.B,
-                                                          g.qCount, f.wts, f.dots, f.stride, bgBase,
-                                                          g.nComp1, g.nComp2, g.nBG, g.nSol, dSol);
+                                                          g.qCount, f.wts, dots, f.stride,
+                                                          mixed ? 1 : 0, bgBase, g.nComp1,
+                                                          g.nComp2, g.nBG, g.nSol, dSol);
   XB_LAUNCHED(c);
   }
   if(c->trace) {
@@ -920,6 +923,10 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   const int n = g.matSize, ld = n + 1;
   k_zero_ints<<<1, 32, 0, c->stream>>>(f.singular, 1);
   XB_LAUNCHED(c);
+  if(mixed) {
+    globalSolveMixed(c, f.M, n, dSol, f.piv, f.singular);
+    return;
+  }
   constexpr int CL = 8;
   const int ncol = (n + CL - 1) / CL;
   const size_t smem = ((size_t)ncol * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
@@ -950,6 +957,10 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
 static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const double* dSol,
                         int convImg, double* dSig) {
   if(nList <= 0) return;
+  if(mixedMode(c)) {
+    sigsMixed(c, si, dList, nList, dSol, convImg, dSig);
+    return;
+  }
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
   const int pix = g.wCols, rc = (pix + 31) / 32;

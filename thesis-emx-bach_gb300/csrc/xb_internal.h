@@ -70,8 +70,8 @@ struct StampSetDev {
   void* W = nullptr;         // n * wRows * wCols (double or float)
   double* Q = nullptr;       // n * qCount^2
   double* B = nullptr;       // n * bCount
-  float* Wf = nullptr;       // mixed-mode FP32 W (alias of W)
-  float* Qf = nullptr;       // mixed-mode FP32 Gram [n][64][64]
+  float* Wf = nullptr;       // mixed mode: FP32 W [n][wRows][ld], ld = wCols padded to 32
+  double* dots = nullptr;    // mixed mode: per-stamp dot table of the global matrix
   std::vector<int> h_count, h_cur;
 };
 
@@ -250,6 +250,16 @@ void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
 void stageCd(xb_ctx* c);
 void stageKsc(xb_ctx* c);
 void stageConvSub(xb_ctx* c, bool doSub);
+
+// mixed-precision stages (xb_mixed.cu)
+int mixedLd(const Geo& g);
+int mixedDotStride(const Geo& g);
+void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
+void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSol, int convImg,
+               double* dSig);
+void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* singular);
+void convSubMixed(xb_ctx* c, double* dKernSum);
+inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
 
 // Kernel image at normalised position (xf, yf) and its sum into *dOut
 // (device): tree = 1 sums in 32-wide groups (cl_kern/cd.cl:419-442), tree = 0

@@ -1,0 +1,882 @@
+// xb_mixed.cu — the mixed-precision (chosen) path, XB_MODE_MIXED.
+//
+// Same stages, same decisions logic, different arithmetic:
+//   * basis convolutions of the substamps in FP32 FMA, W kept in FP32;
+//   * one Gram matrix per stamp of the W rows plus the projected image row
+//     (FP32 accumulation), scattered into Q, B and the dot products the
+//     global normal matrix needs (createQ/createB/createMatrix terms);
+//   * the global system in FP64: LU with fused multiply-adds on a 16-CTA
+//     thread-block cluster, triangular solves by column sweeps, and one
+//     iterative-refinement step with an FP64 residual;
+//   * the chi^2 model in FP32 (the reference already stores it in FP32,
+//     cl_kern/cd.cl:489-531);
+//   * the full-frame convolution in FP32: four kernel blocks per CTA, seven
+//     pixels per thread held in registers.
+// Statistics, substamp search and the per-stamp test fits are shared with the
+// plain path.
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <climits>
+
+#include "xb_device.cuh"
+#include "xb_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace xb {
+
+namespace {
+
+constexpr int MX_THREADS = 256;
+
+__device__ __forceinline__ float floatNormF(int x, int w) {
+  float hw = (float)w * 0.5f;
+  return ((float)x - hw) / hw;
+}
+
+// ------------------------------------------------------------ W in FP32 ---
+// One CTA per (stamp, group of basis functions sharing a Y filter).
+template <class T>
+__global__ void __launch_bounds__(MX_THREADS)
+    k_fill_w_f32(const T* __restrict__ img, int w, int h, const int* __restrict__ list,
+                 const int* __restrict__ count, const int* __restrict__ cur,
+                 const int2* __restrict__ ssxy, int maxSS, const double* __restrict__ fX,
+                 const double* __restrict__ fY, const int* __restrict__ gStart,
+                 const int* __restrict__ gMembers, int hSS, int hK, int wRows, int ldW,
+                 float* __restrict__ W) {
+  extern __shared__ float fw_s[];
+  const int s = list[blockIdx.x], gi = blockIdx.y, tid = threadIdx.x;
+  const int fK = 2 * hK + 1, fSS = 2 * hSS + 1, wCols = fSS * fSS;
+  const int xHalf = hSS + hK, tw = 2 * xHalf + 1, th = fSS;
+  const int m0 = gStart[gi], m1 = gStart[gi + 1];
+  float* Ws = W + (size_t)s * wRows * ldW;
+  const bool live = cur[s] < count[s];
+  if(!live) {
+    for(int m = m0; m < m1; m++)
+      for(int p = tid; p < ldW; p += MX_THREADS) Ws[(size_t)gMembers[m] * ldW + p] = 0.f;
+    return;
+  }
+  const int2 c = ssxy[(size_t)s * maxSS + cur[s]];
+  float* win = fw_s;              // tw * tw
+  float* tmp = win + tw * tw;     // th * tw
+  float* fy = tmp + th * tw;      // fK
+  float* fx = fy + fK;            // fK
+  const int n0 = gMembers[m0];
+  for(int i = tid; i < fK; i += MX_THREADS) fy[i] = (float)fY[(size_t)n0 * fK + i];
+  for(int i = tid; i < tw * tw; i += MX_THREADS) {
+    int gx = min(max(c.x - xHalf + i % tw, 0), w - 1);
+    int gy = min(max(c.y - xHalf + i / tw, 0), h - 1);
+    win[i] = (float)img[(size_t)gx + (size_t)gy * w];
+  }
+  __syncthreads();
+  for(int p = tid; p < th * tw; p += MX_THREADS) {
+    const int row = p / tw, col = p % tw;
+    float v = 0.f;
+#pragma unroll 7
+    for(int y = -hK; y <= hK; y++) v = fmaf(win[(row + hK + y) * tw + col], fy[hK - y], v);
+    tmp[p] = v;
+  }
+  for(int m = m0; m < m1; m++) {
+    const int n = gMembers[m];
+    __syncthreads();
+    for(int i = tid; i < fK; i += MX_THREADS) fx[i] = (float)fX[(size_t)n * fK + i];
+    __syncthreads();
+    for(int p = tid; p < ldW; p += MX_THREADS) {
+      float w0 = 0.f;
+      if(p < wCols) {
+        const int row = p / fSS, ii = p % fSS;
+#pragma unroll 7
+        for(int x = -hK; x <= hK; x++) w0 = fmaf(tmp[row * tw + ii + x + hK], fx[hK - x], w0);
+      }
+      Ws[(size_t)n * ldW + p] = w0;
+    }
+  }
+}
+
+// convStampOdd and convStampBg in FP32; pads the background rows.
+__global__ void __launch_bounds__(MX_THREADS)
+    k_fill_finish_f32(const int* __restrict__ list, const int* __restrict__ count,
+                      const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
+                      const int* __restrict__ kx, const int* __restrict__ ky, int nPSF,
+                      const int2* __restrict__ bgXY, int nBG, int hSS, int w, int h, int wRows,
+                      int ldW, float* __restrict__ W) {
+  const int s = list[blockIdx.x], tid = threadIdx.x;
+  const int fSS = 2 * hSS + 1, wCols = fSS * fSS;
+  float* Ws = W + (size_t)s * wRows * ldW;
+  const bool live = cur[s] < count[s];
+  for(int n = 1; n < nPSF; n++) {
+    if(kx[n] % 2 != 0 || ky[n] % 2 != 0) continue;
+    for(int p = tid; p < wCols; p += MX_THREADS) Ws[(size_t)n * ldW + p] -= Ws[p];
+  }
+  int2 c = make_int2(0, 0);
+  if(live) c = ssxy[(size_t)s * maxSS + cur[s]];
+  for(int b = 0; b < nBG; b++)
+    for(int p = tid; p < ldW; p += MX_THREADS) {
+      float a = 0.f;
+      if(live && p < wCols) {
+        const float xf = floatNormF(c.x - hSS + p % fSS, w), yf = floatNormF(c.y - hSS + p / fSS, h);
+        float ax = 1.f, ay = 1.f;
+        for(int i = 0; i < bgXY[b].x; i++) ax *= xf;
+        for(int i = 0; i < bgXY[b].y; i++) ay *= yf;
+        a = ax * ay;
+      }
+      Ws[(size_t)(nPSF + b) * ldW + p] = a;
+    }
+}
+
+// ------------------------------------------------------------------ Gram ---
+// G = X X^T with X = [W rows; image row] over the substamp pixels.  The
+// products of two FP32 values are exact in FP64 and are accumulated in FP64:
+// the normal matrices are ill-conditioned (cond ~1e14), and an FP32
+// accumulation moves the fitted kernel sum by up to 9 %, while FP32 storage of
+// W itself (a consistent design matrix) moves it by ~1e-7.  Each stamp's
+// lower triangle is split over GM_SPLIT CTAs; k_gram_scatter then fills Q
+// (createQ), B (createB) and the global-matrix dot table.
+constexpr int GM_KT = 32, GM_SPLIT = 6, GM_E = 1;
+template <class T>
+__global__ void __launch_bounds__(MX_THREADS)
+    k_gram_mixed(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
+                 const int* __restrict__ count, const int* __restrict__ cur,
+                 const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int ldW,
+                 const float* __restrict__ W, double* __restrict__ Gout) {
+  extern __shared__ double gm_s[];
+  const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
+  const int fSS = 2 * hSS + 1, wCols = fSS * fSS, R = wRows + 1;
+  const int nEnt = R * (R + 1) / 2;
+  const int per = (nEnt + GM_SPLIT - 1) / GM_SPLIT, e0 = blockIdx.y * per;
+  double* tile = gm_s;  // R x (GM_KT + 1)
+  const float* Ws = W + (size_t)s * wRows * ldW;
+  const bool live = cur[s] < count[s];
+  int2 c = make_int2(0, 0);
+  if(live) c = ssxy[(size_t)s * maxSS + cur[s]];
+  int ei = -1, ej = 0;
+  const int idx = e0 + tid;
+  if(tid < per && idx < nEnt) {
+    int i = (int)((sqrtf(8.f * idx + 1.f) - 1.f) * 0.5f);
+    while((i + 1) * (i + 2) / 2 <= idx) i++;
+    while(i * (i + 1) / 2 > idx) i--;
+    ei = i;
+    ej = idx - i * (i + 1) / 2;
+  }
+  double acc = 0.0;
+  for(int k0 = 0; k0 < wCols; k0 += GM_KT) {
+    const int kt = min(GM_KT, wCols - k0);
+    for(int i = tid; i < R * GM_KT; i += MX_THREADS) {
+      const int r = i / GM_KT, kk = i % GM_KT;
+      float v = 0.f;
+      if(kk < kt) {
+        if(r < wRows) {
+          v = Ws[(size_t)r * ldW + k0 + kk];
+        } else if(live) {
+          const int k = k0 + kk;
+          const int gx = min(max(c.x - hSS + k % fSS, 0), w - 1);
+          const int gy = min(max(c.y - hSS + k / fSS, 0), h - 1);
+          v = (float)other[(size_t)gx + (size_t)gy * w];
+        }
+      }
+      tile[r * (GM_KT + 1) + kk] = (double)v;
+    }
+    __syncthreads();
+    if(ei >= 0) {
+      const double* a = tile + ei * (GM_KT + 1);
+      const double* b = tile + ej * (GM_KT + 1);
+      for(int kk = 0; kk < kt; kk++) acc = fma(a[kk], b[kk], acc);
+    }
+    __syncthreads();
+  }
+  if(ei >= 0) {
+    double* G = Gout + (size_t)t * R * R;
+    G[ei * R + ej] = acc;
+    G[ej * R + ei] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(MX_THREADS)
+    k_gram_scatter(const int* __restrict__ list, const int* __restrict__ count,
+                   const int* __restrict__ cur, int wRows, int nPSF, int nBG, int qc,
+                   const double* __restrict__ Gin, double* __restrict__ Q,
+                   double* __restrict__ B, double* __restrict__ dots, int stride) {
+  const int t = blockIdx.x, s = list[t], tid = threadIdx.x, R = wRows + 1;
+  const double* G = Gin + (size_t)t * R * R;
+  const bool live = cur[s] < count[s];
+  double* Qs = Q + (size_t)s * qc * qc;
+  for(int i = tid; i < qc * qc; i += MX_THREADS) {
+    const int a = i / qc, b = i % qc;
+    Qs[i] = (a > 0 && b > 0 && b <= a) ? G[(a - 1) * R + (b - 1)] : 0.0;
+  }
+  for(int i = tid; i < qc; i += MX_THREADS)
+    B[(size_t)s * qc + i] = (i > 0 && live) ? G[wRows * R + (i - 1)] : 0.0;
+  double* d = dots + (size_t)s * stride;
+  const int nC1 = nPSF - 1, nKB = nC1 * nBG;
+  for(int i = tid; i < stride; i += MX_THREADS) {
+    double v = 0.0;
+    if(i < nKB) {
+      v = G[(nPSF + i % nBG) * R + (1 + i / nBG)];
+    } else if(i < nKB + nBG) {
+      v = G[(nPSF + (i - nKB)) * R + 0];
+    } else if(i < nKB + nBG + nBG * nBG) {
+      const int e = i - nKB - nBG, ib = e / nBG, jb = e % nBG;
+      v = jb <= ib ? G[(nPSF + ib) * R + (nPSF + jb)] : 0.0;
+    } else {
+      const int ib = (i - nKB - nBG - nBG * nBG) % nBG;  // both RHS forms
+      v = live ? G[wRows * R + (nPSF + ib)] : 0.0;
+    }
+    d[i] = v;
+  }
+}
+
+// ---------------------------------------------------- chi^2, FP32 model ---
+template <class T>
+__global__ void __launch_bounds__(MX_THREADS)
+    k_sigs_f32(const int* __restrict__ list, const int* __restrict__ count,
+               const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
+               const float* __restrict__ W, int wRows, int ldW, int hSS, int nPSF, int kOrder,
+               int bgOrder, int nComp, const double* __restrict__ sol, const T* __restrict__ tImg,
+               const T* __restrict__ sImg, uint16_t* __restrict__ mask, int w, int h,
+               double* __restrict__ sig) {
+  __shared__ double coeff[MAX_NPSF];
+  __shared__ double sBg;
+  __shared__ double rs[MX_THREADS / 32];
+  __shared__ int rc[MX_THREADS / 32];
+  const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
+  const int fSS = 2 * hSS + 1, pix = fSS * fSS;
+  const bool live = cur[s] < count[s];
+  int2 c = make_int2(0, 0);
+  if(live) c = ssxy[(size_t)s * maxSS + cur[s]];
+  if(live) {
+    const double xf = (c.x - w * 0.5) / (w * 0.5), yf = (c.y - h * 0.5) / (h * 0.5);
+    const int nC2 = (kOrder + 1) * (kOrder + 2) / 2;
+    for(int i = tid; i < nPSF; i += MX_THREADS) {
+      double cc = 0.0;
+      if(i == 0) {
+        cc = sol[1];
+      } else {
+        int k = 2 + (i - 1) * nC2;
+        double ax = 1.0;
+        for(int x = 0; x <= kOrder; x++) {
+          double ay = 1.0;
+          for(int y = 0; y <= kOrder - x; y++) {
+            cc = fma(sol[k++], ax * ay, cc);
+            ay *= yf;
+          }
+          ax *= xf;
+        }
+      }
+      coeff[i] = cc;
+    }
+    if(tid == 0) {
+      double bg = 0.0, ax = 1.0;
+      int k = nComp + 2;
+      for(int i = 0; i <= bgOrder; i++) {
+        double ay = 1.0;
+        for(int j = 0; j <= bgOrder - i; j++) {
+          bg = fma(sol[k++], ax * ay, bg);
+          ay *= yf;
+        }
+        ax *= xf;
+      }
+      sBg = bg;
+    }
+  }
+  __syncthreads();
+  // The coefficients of an ill-conditioned fit cancel strongly, so the model
+  // is summed in FP64 and stored in FP32 as the reference does.
+  const float* Ws = W + (size_t)s * wRows * ldW;
+  double acc = 0.0;
+  int cnt = 0;
+  if(live) {
+    const double bg = sBg;
+    for(int j = tid; j < pix; j += MX_THREADS) {
+      double md = 0.0;
+      for(int i = 0; i < nPSF; i++) md = fma(coeff[i], (double)Ws[(size_t)i * ldW + j], md);
+      const float m0 = (float)md;
+      const int ax = j % fSS - fSS / 2 + c.x, ay = j / fSS - fSS / 2 + c.y;
+      const size_t ai = (size_t)min(max(ax, 0), w - 1) + (size_t)min(max(ay, 0), h - 1) * w;
+      const double sD = (double)sImg[ai];
+      if((mask[ai] & BAD_INPUT) == 0 && fabs(sD) > 1e-10) {
+        if(isnan(m0) || isnan(sD)) {
+          maskOr(mask, ai, NAN_PIXEL);
+        } else {
+          const double diff = (double)m0 - sD + bg;
+          acc += diff * diff / (fabs((double)tImg[ai]) + fabs(sD));
+          cnt++;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_down_sync(0xffffffffu, acc, o);
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  }
+  if((tid & 31) == 0) {
+    rs[tid >> 5] = acc;
+    rc[tid >> 5] = cnt;
+  }
+  __syncthreads();
+  if(tid == 0) {
+    double a = 0.0;
+    int n = 0;
+    for(int i = 0; i < MX_THREADS / 32; i++) {
+      a += rs[i];
+      n += rc[i];
+    }
+    double r = -1.0;
+    if(n > 0) {
+      r = a / n;
+      if(r >= 1e10) r = -1.0;
+    }
+    sig[t] = r;
+  }
+}
+
+// ------------------------------------------------- global LU, FP64 + FMA ---
+// Same distribution as the plain kernel (columns cyclic over the cluster's
+// shared memories); pivots compared on the bit patterns of the non-negative
+// doubles, trailing updates with fused multiply-adds.
+template <int CL>
+__global__ void __launch_bounds__(256)
+    k_global_lu_fast(double* __restrict__ M, int n, int* __restrict__ idxOut,
+                     int* __restrict__ singular) {
+  extern __shared__ double gl_s[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank(), tid = threadIdx.x, nt = blockDim.x;
+  const int ld = n + 1, ncol = (n + CL - 1) / CL;
+  double* col = gl_s;
+  double* vv = col + (size_t)ncol * ld;
+  double* bc = vv + ld;
+  double* L = bc + 2 * (ld + 1);
+  __shared__ unsigned long long rv[8];
+  __shared__ int ri[8];
+  __shared__ int sP, sMaxI, sSing;
+  if(tid == 0) sSing = 0;
+  __syncthreads();
+  for(int i = 1 + tid; i <= n; i += nt) {
+    double big = 0.0;
+    for(int j = 1; j <= n; j++) big = fmax(big, fabs(M[(size_t)i * ld + j]));
+    if(big == 0.0) sSing = 1;
+    vv[i] = 1.0 / big;
+  }
+  __syncthreads();
+  if(sSing) {
+    if(rank == 0 && tid == 0) *singular = 1;
+    if(rank == 0)
+      for(int i = tid; i <= n; i += nt) idxOut[i] = 0;
+    cluster.sync();
+    return;
+  }
+  for(int lc = 0; lc < ncol; lc++) {
+    const int j = lc * CL + rank + 1;
+    for(int i = tid; i <= n; i += nt) col[(size_t)lc * ld + i] = j <= n ? M[(size_t)i * ld + j] : 0.0;
+  }
+  if(tid == 0) sMaxI = 0;
+  __syncthreads();
+  cluster.sync();
+  for(int j = 1; j <= n; j++) {
+    const int owner = (j - 1) % CL, lcj = (j - 1) / CL;
+    double* myBc = bc + (j & 1) * (ld + 1);
+    if(rank == owner) {
+      double* cj = col + (size_t)lcj * ld;
+      unsigned long long bv = 0;
+      int bi = -1;
+      for(int i = j + tid; i <= n; i += nt) {
+        const double dum = vv[i] * fabs(cj[i]);
+        if(!isnan(dum)) {
+          const unsigned long long u = (unsigned long long)__double_as_longlong(dum);
+          if(bi < 0 || u > bv || (u == bv && i > bi)) {
+            bv = u;
+            bi = i;
+          }
+        }
+      }
+#pragma unroll
+      for(int o = 16; o > 0; o >>= 1) {
+        unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if(oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi > bi))) {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if((tid & 31) == 0) {
+        rv[tid >> 5] = bv;
+        ri[tid >> 5] = bi;
+      }
+      __syncthreads();
+      if(tid == 0) {
+        unsigned long long v = rv[0];
+        int i0 = ri[0];
+        for(int q = 1; q < nt / 32; q++)
+          if(ri[q] >= 0 && (i0 < 0 || rv[q] > v || (rv[q] == v && ri[q] > i0))) {
+            v = rv[q];
+            i0 = ri[q];
+          }
+        const int p = i0 >= 0 ? i0 : sMaxI;
+        if(p != j) {
+          double t = cj[p];
+          cj[p] = cj[j];
+          cj[j] = t;
+        }
+        if(cj[j] == 0.0) cj[j] = 1.0e-20;
+        myBc[0] = (double)p;
+      }
+      __syncthreads();
+      const double piv = cj[j];
+      for(int i = j + 1 + tid; i <= n; i += nt) {
+        const double l = cj[i] / piv;
+        cj[i] = l;
+        myBc[i] = l;
+      }
+    }
+    cluster.sync();
+    const double* src = cluster.map_shared_rank(myBc, owner);
+    if(tid == 0) {
+      sP = (int)src[0];
+      sMaxI = sP;
+    }
+    for(int i = j + 1 + tid; i <= n; i += nt) L[i] = src[i];
+    __syncthreads();
+    const int p = sP;
+    if(rank == 0 && tid == 0) idxOut[j] = p;
+    if(p != j) {
+      for(int lc = tid; lc < ncol; lc += nt) {
+        if(rank == owner && lc == lcj) continue;
+        double* cc = col + (size_t)lc * ld;
+        double t = cc[p];
+        cc[p] = cc[j];
+        cc[j] = t;
+      }
+      if(tid == 0) vv[p] = vv[j];
+    }
+    __syncthreads();
+    const int lcStart = (j - rank + CL - 1) / CL;
+    const int nLoc = ncol - lcStart, m = n - j;
+    for(int e = tid; e < nLoc * m; e += nt) {
+      const int lc = lcStart + e / m, i = j + 1 + e % m;
+      if(lc * CL + rank + 1 > n) continue;
+      double* cc = col + (size_t)lc * ld;
+      cc[i] = fma(-L[i], cc[j], cc[i]);
+    }
+    __syncthreads();
+  }
+  cluster.sync();
+  for(int lc = 0; lc < ncol; lc++) {
+    const int j = lc * CL + rank + 1;
+    if(j > n) break;
+    for(int i = tid; i <= n; i += nt) M[(size_t)i * ld + j] = col[(size_t)lc * ld + i];
+  }
+  if(rank == 0 && tid == 0) idxOut[0] = 0;
+}
+
+// Forward/back substitution by column sweeps plus one refinement step with
+// the FP64 residual r = b - A x of the original matrix A.  One CTA.
+__device__ void sweepSolve(const double* __restrict__ LU, int n, const int* piv, double* x,
+                           const double* invU) {
+  const int tid = threadIdx.x, nt = blockDim.x, ld = n + 1;
+  __syncthreads();
+  if(tid == 0)
+    for(int i = 1; i <= n; i++) {
+      const int ip = piv[i];
+      const double t = x[ip];
+      x[ip] = x[i];
+      x[i] = t;
+    }
+  __syncthreads();
+  for(int j = 1; j < n; j++) {
+    const double xj = x[j];
+    for(int i = j + 1 + tid; i <= n; i += nt) x[i] = fma(-LU[(size_t)i * ld + j], xj, x[i]);
+    __syncthreads();
+  }
+  for(int j = n; j >= 1; j--) {
+    const double xj = x[j] * invU[j];
+    for(int i = 1 + tid; i < j; i += nt) x[i] = fma(-LU[(size_t)i * ld + j], xj, x[i]);
+    __syncthreads();
+    if(tid == 0) x[j] = xj;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+    k_solve_refine(const double* __restrict__ LU, const double* __restrict__ A, int n,
+                   const int* __restrict__ piv, double* __restrict__ b) {
+  extern __shared__ double sv_s[];
+  const int tid = threadIdx.x, nt = blockDim.x, ld = n + 1;
+  double* x = sv_s;          // n + 1
+  double* bb = x + ld;       // n + 1
+  double* invU = bb + ld;    // n + 1
+  double* d = invU + ld;     // n + 1
+  int* p = (int*)(d + ld);   // n + 1
+  for(int i = tid; i <= n; i += nt) {
+    bb[i] = b[i];
+    x[i] = b[i];
+    p[i] = piv[i];
+    invU[i] = i > 0 ? 1.0 / LU[(size_t)i * ld + i] : 0.0;
+  }
+  sweepSolve(LU, n, p, x, invU);
+  // r = b - A x, one warp per row
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for(int i = 1 + warp; i <= n; i += nw) {
+    double a = 0.0;
+    for(int j = 1 + lane; j <= n; j += 32) a = fma(A[(size_t)i * ld + j], x[j], a);
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if(lane == 0) d[i] = bb[i] - a;
+  }
+  if(tid == 0) d[0] = 0.0;
+  sweepSolve(LU, n, p, d, invU);
+  for(int i = 1 + tid; i <= n; i += nt) b[i] = x[i] + d[i];
+}
+
+// -------------------------------------------------- conv + sub in FP32 ----
+// Four kernel blocks (84 columns) x one block row (21 rows) per CTA; each
+// thread produces seven adjacent pixels of one block row, streaming the image
+// row through registers.
+constexpr int CV_BX = 4;  // blocks per CTA along x
+struct ConvArgsF {
+  int w, h, hK, fK, nPSF, kOrder, bgOrder, nComp, scaleConv;
+  float tH, tL;
+};
+
+__device__ __forceinline__ uint16_t convMaskF(float t, float tH, float tL) {
+  uint16_t m = 0;
+  if(t == 0.f) m |= BAD_INPUT | BAD_PIX_VAL;
+  if(t >= tH) m |= BAD_INPUT | SAT_PIXEL;
+  if(t <= tL) m |= BAD_INPUT | LOW_PIXEL;
+  return m;
+}
+__device__ __forceinline__ uint16_t afterMaskF(float t, float tH, float tL) {
+  uint16_t m = 0;
+  if(t == 0.f) m |= BAD_OUTPUT | BAD_INPUT | BAD_PIX_VAL;
+  if(t >= tH) m |= BAD_OUTPUT | BAD_INPUT | SAT_PIXEL;
+  if(t <= tL) m |= BAD_OUTPUT | BAD_INPUT | LOW_PIXEL;
+  return m;
+}
+
+template <int FK>
+__global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
+    k_conv_sub_f32(const float* __restrict__ I, const float* __restrict__ O,
+                   const double* __restrict__ sol, const double* __restrict__ Kt,
+                   const double* __restrict__ kernSumPtr, ConvArgsF a,
+                   uint16_t* __restrict__ mask, float* __restrict__ convF,
+                   float* __restrict__ diffF) {
+  constexpr int HK = FK / 2, NK = FK * FK, PX = 7, TPR = FK / PX;  // threads per block row
+  constexpr int TW = CV_BX * FK + 2 * HK, TH = FK + 2 * HK;
+  __shared__ float tile[TH][TW + 1];
+  __shared__ unsigned char bad[TH][TW + 1];
+  __shared__ unsigned char rowBad[TH][CV_BX * FK];  // OR of bad over the x window
+  __shared__ float kern[CV_BX][NK];
+  __shared__ double poly[CV_BX][16];
+  __shared__ float aks[CV_BX];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int xB0 = blockIdx.x * CV_BX, yB = blockIdx.y;
+  const int x0 = xB0 * FK, y0 = yB * FK;   // tile origin; block pixels start at +HK
+  const int nC2 = (a.kOrder + 1) * (a.kOrder + 2) / 2;
+  if(tid < CV_BX) {
+    // spatial terms xf^i yf^j at the block centre (conv(), src/bach.cpp:339-350)
+    const double hx = 0.5 * a.w, hy = 0.5 * a.h;
+    const double xf = ((xB0 + tid) * FK + 2 * HK - hx) / hx, yf = (yB * FK + 2 * HK - hy) / hy;
+    double ax = 1.0;
+    int t = 0;
+    for(int x = 0; x <= a.kOrder; x++) {
+      double ay = 1.0;
+      for(int y = 0; y <= a.kOrder - x; y++) {
+        poly[tid][t++] = ax * ay;
+        ay *= yf;
+      }
+      ax *= xf;
+    }
+  }
+  for(int i = tid; i < TH * TW; i += nthr) {
+    const int ly = i / TW, lx = i % TW;
+    const int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
+    const float v = I[(size_t)gx + (size_t)gy * a.w];
+    tile[ly][lx] = v;
+    bad[ly][lx] = (convMaskF(v, a.tH, a.tL) & BAD_INPUT) ? 1 : 0;
+  }
+  __syncthreads();
+  // kernel of each block from the FP64 spatial-term images, rounded once
+  for(int e = tid; e < CV_BX * NK; e += nthr) {
+    const int b = e / NK, p = e % NK;
+    double k0 = 0.0;
+    for(int t = 0; t < nC2; t++) k0 = fma(poly[b][t], Kt[(size_t)t * NK + p], k0);
+    kern[b][p] = (float)k0;
+  }
+  for(int e = tid; e < TH * CV_BX * FK; e += nthr) {
+    const int ly = e / (CV_BX * FK), lx = e % (CV_BX * FK);
+    unsigned char o = 0;
+#pragma unroll
+    for(int d = 0; d < FK; d++) o |= bad[ly][lx + d];
+    rowBad[ly][lx] = o;
+  }
+  __syncthreads();
+  if(tid < CV_BX) {
+    float s = 0.f;
+    for(int p = 0; p < NK; p++) s += fabsf(kern[tid][p]);
+    aks[tid] = s;
+  }
+  __syncthreads();
+  const float kernSum = (float)*kernSumPtr;
+  const float invKernMult = a.scaleConv ? 1.f / kernSum : 1.f;
+  const float convFactor = a.scaleConv ? kernSum : 1.f;
+  const float finalFactor = a.scaleConv ? -(1.f / kernSum) : 1.f;
+  // thread -> (block b, output row ly, first column lx0)
+  const int perBlock = FK * TPR;
+  if(tid >= CV_BX * perBlock) return;
+  const int b = tid / perBlock, r = tid % perBlock, ly = r / TPR, lx0 = b * FK + (r % TPR) * PX;
+  const float* kb = kern[b];
+  float acc[PX];
+#pragma unroll
+  for(int q = 0; q < PX; q++) acc[q] = 0.f;
+  for(int jj = 0; jj < FK; jj++) {
+    float win[PX + FK - 1];
+#pragma unroll
+    for(int q = 0; q < PX + FK - 1; q++) win[q] = tile[ly + jj][lx0 + q];
+    const float* krow = kb + (FK - 1 - jj) * FK;
+#pragma unroll
+    for(int ii = 0; ii < FK; ii++) {
+      const float kk = krow[FK - 1 - ii];
+#pragma unroll
+      for(int q = 0; q < PX; q++) acc[q] = fmaf(kk, win[q + ii], acc[q]);
+    }
+  }
+#pragma unroll
+  for(int q = 0; q < PX; q++) {
+    const int x = x0 + HK + lx0 + q, y = y0 + HK + ly;
+    if(x >= a.w - HK || y >= a.h - HK) continue;
+    // background polynomial (getBackground, cd.cl:444-467), FP64
+    const double bxf = (x - 0.5 * a.w) / (0.5 * a.w), byf = (y - 0.5 * a.h) / (0.5 * a.h);
+    double bgv = 0.0, ax = 1.0;
+    int k = a.nComp + 2;
+    for(int i = 0; i <= a.bgOrder; i++) {
+      double ay = 1.0;
+      for(int j = 0; j <= a.bgOrder - i; j++) {
+        bgv = fma(sol[k++], ax * ay, bgv);
+        ay *= byf;
+      }
+      ax *= bxf;
+    }
+    const float v = (acc[q] + (float)bgv) * invKernMult;
+    const size_t id = (size_t)x + (size_t)y * a.w;
+    const float tc = tile[ly + HK][lx0 + q + HK];
+    const uint16_t cm = convMaskF(tc, a.tH, a.tL);
+    uint16_t nm = cm;
+    if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
+    unsigned char any = 0;
+    for(int jj = 0; jj < FK; jj++) any |= rowBad[ly + jj][lx0 + q];
+    if(any) {
+      float uks = 0.f;
+      for(int jj = 0; jj < FK; jj++)
+        for(int ii = 0; ii < FK; ii++)
+          if(!bad[ly + jj][lx0 + q + ii]) uks += fabsf(kb[(FK - 1 - ii) + (FK - 1 - jj) * FK]);
+      if((uks / aks[b]) < 0.99f) nm |= BAD_OUTPUT | BAD_CONV;
+      else nm |= OK_CONV;
+    }
+    const float o = O[id];
+    nm |= afterMaskF(o, a.tH, a.tL);
+    mask[id] = nm;
+    convF[id] = v;
+    diffF[id] = (nm & BAD_OUTPUT) ? 1e-30f : (v * convFactor - o) * finalFactor;
+  }
+}
+
+// Kernel images of the spatial terms, FP64: Kt[t] = sum_n sol[2+(n-1)*nC2+t]
+// * basis_n (+ sol[1] * basis_0 for the constant term), so that the kernel at
+// (xf, yf) is sum_t xf^i yf^j Kt[t] (makeKernelCoeffs + makeKernel,
+// cl_kern/cd.cl:354-417, regrouped by spatial term).
+__global__ void k_kernel_terms(const double* __restrict__ sol, const double* __restrict__ vec,
+                               int nPSF, int nC2, int nk, double* __restrict__ Kt) {
+  for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < nC2 * nk; e += gridDim.x * blockDim.x) {
+    const int t = e / nk, p = e % nk;
+    double k0 = t == 0 ? sol[1] * vec[p] : 0.0;
+    for(int n = 1; n < nPSF; n++) k0 = fma(sol[2 + (n - 1) * nC2 + t], vec[(size_t)n * nk + p], k0);
+    Kt[e] = k0;
+  }
+}
+
+__global__ void k_border_f32(const float* __restrict__ O, int w, int h, int hK, float tH, float tL,
+                             uint16_t* __restrict__ mask, float* __restrict__ convF,
+                             float* __restrict__ diffF) {
+  const long long n = (long long)w * h;
+  for(long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < n;
+      id += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(id % w), y = (int)(id / w);
+    if(x >= hK && x < w - hK && y >= hK && y < h - hK) continue;
+    mask[id] |= afterMaskF(O[id], tH, tL);
+    convF[id] = 1e-30f;
+    diffF[id] = 1e-30f;
+  }
+}
+
+}  // namespace
+
+// ============================================================ host side ===
+
+int mixedLd(const Geo& g) { return (g.wCols + 31) / 32 * 32; }
+
+int mixedDotStride(const Geo& g) { return g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + 2 * g.nBG; }
+
+void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
+  if(nList <= 0) return;
+  const Geo& g = c->g;
+  StampSetDev& S = c->set[si];
+  const int ldW = mixedLd(g);
+  const int nGroups = (int)c->basis.yGroupStart.size() - 1;
+  const int tw = 2 * (g.hSS + g.hK) + 1, th = g.fSS;
+  const size_t smemFill = (size_t)(tw * tw + th * tw + 2 * g.fK) * sizeof(float);
+  const int other = 1 - imgConv;
+  {
+    KT_SCOPE(c, "fill_w");
+    dim3 grid(nList, nGroups);
+    if(c->imgIsF64)
+      k_fill_w_f32<double><<<grid, MX_THREADS, smemFill, c->stream>>>(
+          (const double*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS,
+          c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+    else
+      k_fill_w_f32<float><<<grid, MX_THREADS, smemFill, c->stream>>>(
+          (const float*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS,
+          c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+    XB_LAUNCHED(c);
+  }
+  {
+    KT_SCOPE(c, "fill_finish");
+    k_fill_finish_f32<<<nList, MX_THREADS, 0, c->stream>>>(
+        dList, S.count, S.cur, S.ssxy, g.maxSS, c->dKx, c->dKy, g.nPSF, buf<int2>(c, "bgXY", g.nBG),
+        g.nBG, g.hSS, c->w, c->h, g.wRows, ldW, S.Wf);
+    XB_LAUNCHED(c);
+  }
+  {
+    KT_SCOPE(c, "gram");
+    const int R = g.wRows + 1;
+    const size_t smem = (size_t)R * (GM_KT + 1) * sizeof(double);
+    if((R * (R + 1) / 2 + GM_SPLIT - 1) / GM_SPLIT > GM_E * MX_THREADS)
+      throw XbError{XB_ERR_UNSUPPORTED, "too many basis functions for the Gram kernel"};
+    double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
+    dim3 grid(nList, GM_SPLIT);
+    if(c->imgIsF64)
+      k_gram_mixed<double><<<grid, MX_THREADS, smem, c->stream>>>(
+          (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
+          g.wRows, ldW, S.Wf, G);
+    else
+      k_gram_mixed<float><<<grid, MX_THREADS, smem, c->stream>>>(
+          (const float*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
+          g.wRows, ldW, S.Wf, G);
+    XB_LAUNCHED(c);
+    k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, S.count, S.cur, g.wRows, g.nPSF,
+                                                        g.nBG, g.qCount, G, S.Q, S.B, S.dots,
+                                                        mixedDotStride(g));
+    XB_LAUNCHED(c);
+  }
+}
+
+void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSol, int convImg,
+               double* dSig) {
+  if(nList <= 0) return;
+  const Geo& g = c->g;
+  StampSetDev& S = c->set[si];
+  const int other = 1 - convImg;
+  KT_SCOPE(c, "sigs");
+  if(c->imgIsF64)
+    k_sigs_f32<double><<<nList, MX_THREADS, 0, c->stream>>>(
+        dList, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
+        c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const double*)c->img[convImg],
+        (const double*)c->img[other], c->mask, c->w, c->h, dSig);
+  else
+    k_sigs_f32<float><<<nList, MX_THREADS, 0, c->stream>>>(
+        dList, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
+        c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const float*)c->img[convImg],
+        (const float*)c->img[other], c->mask, c->w, c->h, dSig);
+  XB_LAUNCHED(c);
+}
+
+// LU + refined solve of the (n+1)^2 system in M (row 0 / column 0 unused);
+// rhs (n+1 entries, index 0 unused) is replaced by the solution.
+void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* singular) {
+  const int ld = n + 1;
+  double* A = buf<double>(c, "mixed_A", (size_t)ld * ld);
+  XB_CUDA(cudaMemcpyAsync(A, M, sizeof(double) * ld * ld, cudaMemcpyDeviceToDevice, c->stream));
+  static int clusterSize = 0;
+  auto launchLu = [&](auto kernel, int CL) -> cudaError_t {
+    const int ncol = (n + CL - 1) / CL;
+    const size_t smem = ((size_t)ncol * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if(e != cudaSuccess) return e;
+    if(CL > 8) {
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if(e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, M, n, piv, singular);
+  };
+  {
+    KT_SCOPE(c, "global_lu");
+    cudaError_t e = cudaErrorUnknown;
+    if(clusterSize != 8) {
+      e = launchLu(k_global_lu_fast<16>, 16);
+      if(e == cudaSuccess) clusterSize = 16;
+      else cudaGetLastError();
+    }
+    if(e != cudaSuccess) {
+      XB_CUDA(launchLu(k_global_lu_fast<8>, 8));
+      clusterSize = 8;
+    }
+    XB_LAUNCHED(c);
+  }
+  {
+    KT_SCOPE(c, "global_solve");
+    const size_t smem = (size_t)4 * ld * sizeof(double) + (size_t)ld * sizeof(int);
+    k_solve_refine<<<1, 1024, smem, c->stream>>>(M, A, n, piv, rhs);
+    XB_LAUNCHED(c);
+  }
+}
+
+void convSubMixed(xb_ctx* c, double* dKernSum) {
+  const Geo& g = c->g;
+  if(g.fK != 21) throw XbError{XB_ERR_UNSUPPORTED, "mixed conv is built for 21-px kernels"};
+  const int I = c->chosen, O = 1 - c->chosen;
+  if(c->imgIsF64) throw XbError{XB_ERR_UNSUPPORTED, "mixed mode takes FP32 images"};
+  const int nk = g.fK * g.fK;
+  double* Kt = buf<double>(c, "kernel_terms", (size_t)g.nComp2 * nk);
+  k_kernel_terms<<<(g.nComp2 * nk + 255) / 256, 256, 0, c->stream>>>(c->dSol, c->dVec, g.nPSF,
+                                                                      g.nComp2, nk, Kt);
+  XB_LAUNCHED(c);
+  ConvArgsF a{};
+  a.w = c->w;
+  a.h = c->h;
+  a.hK = g.hK;
+  a.fK = g.fK;
+  a.nPSF = g.nPSF;
+  a.kOrder = c->p.kernelOrder;
+  a.bgOrder = c->p.backgroundOrder;
+  a.nComp = g.nComp;
+  a.scaleConv = (c->p.normalizeTemplate && c->convTemplate) || (!c->p.normalizeTemplate && !c->convTemplate);
+  a.tH = (float)c->p.threshHigh;
+  a.tL = (float)c->p.threshLow;
+  const int xSteps = (c->w + g.fK - 1) / g.fK, ySteps = (c->h + g.fK - 1) / g.fK;
+  dim3 grid((xSteps + CV_BX - 1) / CV_BX, ySteps);
+  {
+    KT_SCOPE(c, "conv_sub");
+    k_conv_sub_f32<21><<<grid, CV_BX * 21 * 3, 0, c->stream>>>(
+        (const float*)c->img[I], (const float*)c->img[O], c->dSol, Kt, dKernSum, a, c->mask,
+        c->convF, c->diffF);
+    XB_LAUNCHED(c);
+  }
+  const long long n = (long long)c->w * c->h;
+  k_border_f32<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
+      (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convF, c->diffF);
+  XB_LAUNCHED(c);
+}
+
+}  // namespace xb

@@ -593,6 +593,258 @@ __global__ void __launch_bounds__(FS_THREADS)
   }
 }
 
+// ------------------------------------------------ substamp search by maps --
+// The same decisions as k_find_substamps, restructured: between two accepted
+// substamps the mask does not change, so for every pixel of the stamp window
+// the reference's local-maximum search (sss.cl:494-526) and window check
+// (checkSStamp, :393-428) are tabulated once per mask state:
+//   * a separable sliding-window argmax over the qualifying pixels (largest
+//     value, ties to the first pixel in raster order: row pass keeps the
+//     smallest x, column pass the smallest y), keys compared as the bit
+//     patterns of positive doubles;
+//   * separable window ORs of "bad", "above kernel-fit threshold" and "above
+//     threshold but not positive".
+// Each pass then looks for the first candidate in raster order whose window
+// passes, in parallel; the scan before it changes nothing, and after an
+// acceptance the maps are rebuilt and the scan resumes at the next pixel.
+// The accepted substamp's value is the sequential sum of sss.cl:421-424; for
+// FP32 input every summand is a float, all partial sums are exact in FP64
+// whenever sum|v| < 2^52 * (quantum of the smallest |v|), which is checked,
+// and then a parallel sum is the same number.
+constexpr int FM_THREADS = 256;
+enum : uint8_t { FL_PRED = 1, FL_NONPOS = 2, FL_KFQ = 4, FL_VPOS = 8 };
+enum : uint8_t { OK_BAD = 1, OK_PRED = 2, OK_NONPOS = 4 };
+
+__device__ __forceinline__ bool keyBetter(unsigned long long k, int i, unsigned long long bk, int bi) {
+  return k > bk || (k == bk && k != 0 && i < bi);
+}
+
+template <class T>
+__device__ void fmBuild(const T* img, const uint16_t* mask, int w, int cx, int cy, int n, int sx,
+                        int sy, int hSS, uint16_t badMask, const uint8_t* flags, uint8_t* bad,
+                        unsigned long long* key, unsigned short* hx, uint8_t* rowf, int* arg,
+                        uint8_t* okw) {
+  const int N = n * n, tid = threadIdx.x;
+  for(int p = tid; p < N; p += FM_THREADS) {
+    const int lx = p % n, ly = p / n;
+    const size_t a = (size_t)(cx + lx) + (size_t)(cy + ly) * w;
+    const uint8_t b = (ldMask(mask, a) & badMask) ? 1 : 0;
+    bad[p] = b;
+    const uint8_t f = flags[p];
+    key[p] = (!b && (f & FL_KFQ) && (f & FL_VPOS))
+                 ? (unsigned long long)__double_as_longlong((double)img[a]) : 0ull;
+  }
+  __syncthreads();
+  for(int p = tid; p < N; p += FM_THREADS) {
+    const int lx = p % n, ly = p / n, row = ly * n;
+    unsigned long long bk = 0;
+    int bi = 0xFFFF;
+    for(int x = max(lx - hSS, 0); x <= min(lx + hSS, n - 1); x++) {
+      const unsigned long long k = key[row + x];
+      if(keyBetter(k, x, bk, bi)) {
+        bk = k;
+        bi = x;
+      }
+    }
+    hx[p] = bk ? (unsigned short)bi : (unsigned short)0xFFFF;
+    uint8_t o = 0;
+    for(int x = max(lx - hSS, 0); x <= min(lx + hSS, sx - 1); x++) {
+      const uint8_t f = flags[row + x];
+      o |= bad[row + x] ? OK_BAD : 0;
+      o |= (f & FL_PRED) ? OK_PRED : 0;
+      o |= (f & FL_NONPOS) ? OK_NONPOS : 0;
+    }
+    rowf[p] = o;
+  }
+  __syncthreads();
+  for(int p = tid; p < N; p += FM_THREADS) {
+    const int lx = p % n, ly = p / n;
+    unsigned long long bk = 0;
+    int bi = -1;
+    for(int y = max(ly - hSS, 0); y <= min(ly + hSS, n - 1); y++) {
+      const unsigned short xx = hx[y * n + lx];
+      if(xx == 0xFFFF) continue;
+      const int q = y * n + xx;
+      const unsigned long long k = key[q];
+      if(k > bk) {  // rows visited in ascending y: the first row keeps ties
+        bk = k;
+        bi = q;
+      }
+    }
+    arg[p] = bi;
+    uint8_t o = 0;
+    for(int y = max(ly - hSS, 0); y <= min(ly + hSS, sy - 1); y++) o |= rowf[y * n + lx];
+    okw[p] = o;
+  }
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(FM_THREADS)
+    k_find_substamps_maps(const T* __restrict__ img0, const T* __restrict__ img1,
+                          uint16_t* __restrict__ mask, const int4* __restrict__ geom,
+                          const double* __restrict__ sky0, const double* __restrict__ fwhm0,
+                          const double* __restrict__ sky1, const double* __restrict__ fwhm1,
+                          int2* __restrict__ xy0, double* __restrict__ val0, int* __restrict__ cnt0,
+                          int2* __restrict__ xy1, double* __restrict__ val1, int* __restrict__ cnt1,
+                          int w, int fSW, int hSS, int maxSS, double tH, double tKF,
+                          unsigned char* __restrict__ scratch, size_t perCta, int floatInput) {
+  const int s = blockIdx.x, im = blockIdx.y, tid = threadIdx.x;
+  const T* img = im == 0 ? img0 : img1;
+  const double sky = im == 0 ? sky0[s] : sky1[s];
+  const double fwhm = im == 0 ? fwhm0[s] : fwhm1[s];
+  int2* xyOut = (im == 0 ? xy0 : xy1) + (size_t)s * maxSS;
+  double* valOut = (im == 0 ? val0 : val1) + (size_t)s * maxSS;
+  const uint16_t badMask =
+      (uint16_t)((MASK_ALL & ~OK_CONV) & ~(im == 0 ? (BAD_PIXEL_S | SKIP_S) : (BAD_PIXEL_T | SKIP_T)));
+  const uint16_t skipMask = im == 0 ? SKIP_T : SKIP_S;
+  const int4 gm = geom[s];
+  const int cx = gm.x, cy = gm.y, sx = gm.z, sy = gm.w, n = fSW, N = n * n;
+  const double invFwhm = 1.0 / fwhm;
+  unsigned char* base = scratch + (size_t)(im * gridDim.x + s) * perCta;
+  unsigned long long* key = (unsigned long long*)base;  // N
+  int* arg = (int*)(key + N);                           // N
+  unsigned short* hx = (unsigned short*)(arg + N);      // N
+  uint8_t* flags = (uint8_t*)(hx + N);                  // N
+  uint8_t* bad = flags + N;                             // N
+  uint8_t* rowf = bad + N;                              // N
+  uint8_t* okw = rowf + N;                              // N
+  __shared__ int2 locXY[MAX_MAXSS];
+  __shared__ double locVal[MAX_MAXSS];
+  __shared__ int sBest;
+  __shared__ double rA[FM_THREADS / 32], rB[FM_THREADS / 32];
+  __shared__ double sSum;
+  __shared__ int sExact;
+  // static flags: checkSStamp predicate, kernel-fit qualification, v > 0
+  for(int p = tid; p < N; p += FM_THREADS) {
+    const double v = (double)img[(size_t)(cx + p % n) + (size_t)(cy + p / n) * w];
+    uint8_t f = 0;
+    const bool pr = (v - sky) / fwhm > tKF;
+    if(pr) f |= FL_PRED;
+    if(pr && !(v > 0.0)) f |= FL_NONPOS;
+    if(!((v - sky) * invFwhm < tKF)) f |= FL_KFQ;
+    if(v > 0.0) f |= FL_VPOS;
+    flags[p] = f;
+  }
+  __syncthreads();
+  fmBuild(img, mask, w, cx, cy, n, sx, sy, hSS, badMask, flags, bad, key, hx, rowf, arg, okw);
+  const double floorV = sky + tKF * fwhm;
+  double dfrac = 0.9;
+  int cnt = 0, passes = 0;
+  while(cnt < maxSS && passes < 256) {
+    passes++;
+    const double alt = sky + (tH - sky) * dfrac;
+    const double lim = floorV < alt ? alt : floorV;  // OpenCL max()
+    int start = 0;
+    while(cnt < maxSS && start < N) {
+      // first candidate >= start whose window passes (or needs the exact sum)
+      int mine = INT_MAX;
+      for(int p0 = start; p0 < N && mine == INT_MAX; p0 += 4 * FM_THREADS) {
+        for(int k = 0; k < 4; k++) {
+          const int p = p0 + k * FM_THREADS + tid;
+          if(p >= N || p >= mine) break;
+          if(bad[p] || !(flags[p] & FL_KFQ)) continue;
+          const double v = (double)img[(size_t)(cx + p % n) + (size_t)(cy + p / n) * w];
+          if(!(v > lim)) continue;
+          const int m = arg[p] >= 0 ? arg[p] : p;
+          const uint8_t o = okw[m];
+          if(!(o & OK_BAD) && (o & OK_PRED)) {
+            mine = p;
+            break;
+          }
+        }
+        mine = __reduce_min_sync(0xffffffffu, mine);
+        if(tid == 0) sBest = INT_MAX;
+        __syncthreads();
+        if((tid & 31) == 0 && mine != INT_MAX) atomicMin(&sBest, mine);
+        __syncthreads();
+        mine = sBest;
+        __syncthreads();
+      }
+      if(mine == INT_MAX) break;
+      const int p = mine, m = arg[p] >= 0 ? arg[p] : p;
+      const int mx = cx + m % n, my = cy + m / n;
+      const int u0 = max(mx - hSS, cx), v0 = max(my - hSS, cy);
+      const int u1 = min(mx + hSS, cx + sx - 1), v1 = min(my + hSS, cy + sy - 1);
+      const int uw = u1 - u0 + 1, un = uw * (v1 - v0 + 1);
+      // value of the substamp: sum of the thresholded pixels in raster order
+      double part = 0.0, amin = INFINITY;
+      for(int i = tid; i < un; i += FM_THREADS) {
+        const int lx = u0 + i % uw - cx, ly = v0 + i / uw - cy;
+        if(flags[ly * n + lx] & FL_PRED) {
+          const double v = (double)img[(size_t)(cx + lx) + (size_t)(cy + ly) * w];
+          part += v;
+          amin = fmin(amin, fabs(v));
+        }
+      }
+#pragma unroll
+      for(int o = 16; o > 0; o >>= 1) {
+        part += __shfl_down_sync(0xffffffffu, part, o);
+        amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
+      }
+      if((tid & 31) == 0) {
+        rA[tid >> 5] = part;
+        rB[tid >> 5] = amin;
+      }
+      __syncthreads();
+      if(tid == 0) {
+        double t = 0.0, mn = INFINITY;
+        for(int i = 0; i < FM_THREADS / 32; i++) {
+          t += rA[i];
+          mn = fmin(mn, rB[i]);
+        }
+        int exact = 0;
+        if(floatInput && !(okw[m] & OK_NONPOS) && mn > 0.0 && mn < INFINITY) {
+          int e;
+          frexp(mn, &e);                           // mn in [2^(e-1), 2^e)
+          const double quantum = ldexp(1.0, e - 1 - 23);
+          exact = t < ldexp(quantum, 52) ? 1 : 0;  // t = sum|v| here (all v > 0)
+        }
+        if(!exact) {
+          t = 0.0;
+          for(int yy = v0; yy <= v1; yy++)
+            for(int xx = u0; xx <= u1; xx++)
+              if(flags[(yy - cy) * n + (xx - cx)] & FL_PRED) t += (double)img[(size_t)xx + (size_t)yy * w];
+        }
+        sSum = t;
+      }
+      __syncthreads();
+      const double ret = sSum;
+      start = p + 1;
+      if(ret == 0.0) continue;
+      if(tid == 0) {
+        locXY[cnt] = make_int2(mx, my);
+        locVal[cnt] = ret;
+      }
+      cnt++;
+      for(int i = tid; i < un; i += FM_THREADS)
+        orMask(mask, (size_t)(u0 + i % uw) + (size_t)(v0 + i / uw) * w, skipMask);
+      __syncthreads();
+      if(cnt < maxSS)
+        fmBuild(img, mask, w, cx, cy, n, sx, sy, hSS, badMask, flags, bad, key, hx, rowf, arg, okw);
+    }
+    if(cnt >= maxSS || lim == floorV) break;
+    dfrac -= 0.2;
+  }
+  __syncthreads();
+  if(tid == 0) {
+    for(int i = 1; i < cnt; i++)
+      for(int j = i; j > 0 && locVal[j - 1] < locVal[j]; j--) {
+        int2 t = locXY[j - 1];
+        locXY[j - 1] = locXY[j];
+        locXY[j] = t;
+        double tv = locVal[j - 1];
+        locVal[j - 1] = locVal[j];
+        locVal[j] = tv;
+      }
+    for(int i = 0; i < maxSS; i++) {
+      xyOut[i] = i < cnt ? locXY[i] : make_int2(INT_MAX, INT_MAX);
+      valOut[i] = i < cnt ? locVal[i] : -INFINITY;
+    }
+    (im == 0 ? cnt0 : cnt1)[s] = min(cnt, maxSS / 2);
+  }
+}
+
 // removeEmptyStamps (src/sssUtil.cpp:106-197, sss.cl:574-638): keep stamps
 // with at least one substamp in ascending original order.  One CTA per image.
 __global__ void __launch_bounds__(256)
@@ -653,18 +905,20 @@ static void sssPass(xb_ctx* c, int* nKept) {
   }
   dim3 grid(nAll, 2);
   { KT_SCOPE(c, "find_substamps");
+  const size_t perCta = ((size_t)fSW * fSW * 18 + 255) / 256 * 256;
+  unsigned char* scratch = buf<unsigned char>(c, "fm_scratch", (size_t)2 * nAll * perCta);
   if(c->imgIsF64)
-    k_find_substamps<double><<<grid, FS_THREADS, 0, c->stream>>>(
+    k_find_substamps_maps<double><<<grid, FM_THREADS, 0, c->stream>>>(
         (const double*)c->img[0], (const double*)c->img[1], c->mask, c->geomAll,
         c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0],
         c->ssvalAll[0], c->cntAll[0], c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w,
-        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit);
+        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit, scratch, perCta, 0);
   else
-    k_find_substamps<float><<<grid, FS_THREADS, 0, c->stream>>>(
+    k_find_substamps_maps<float><<<grid, FM_THREADS, 0, c->stream>>>(
         (const float*)c->img[0], (const float*)c->img[1], c->mask, c->geomAll,
         c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0],
         c->ssvalAll[0], c->cntAll[0], c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w,
-        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit);
+        fSW, g.hSS, g.maxSS, c->p.threshHigh, c->p.threshKernFit, scratch, perCta, 1);
   XB_LAUNCHED(c);
   }
   for(int im = 0; im < 2; im++) {
