@@ -367,16 +367,9 @@ __global__ void __launch_bounds__(ST_THREADS)
   }
 }
 
-// --------------------------------------------------------- substamp search --
-// One CTA per (stamp, image): findSubStamps (cl_kern/sss.cl:448-572).  The
-// raster scan is processed in chunks of 1024 pixels: the candidate test runs
-// in parallel, then candidates are visited in raster order with their mask
-// re-read (acceptances only add SKIP bits).  The reference's writes of the
-// bad-pixel bit for pixels above threshHigh (sss.cl:416-419, :484-487,
-// :512-515) are unreachable: such pixels carry BAD_INPUT from maskInput
-// (ini.cl:29), which every badMask contains, and that test comes first.
-constexpr int FS_THREADS = 256, FS_CHUNK = 1024, FS_FAILCACHE = 128;
-
+// Mask access shared by the substamp search: volatile 16-bit loads (other
+// CTAs of the same launch may set SKIP bits nearby) and a 16-bit OR done as a
+// 32-bit atomic on the containing word (the mask buffer has 2 spare entries).
 __device__ __forceinline__ uint16_t ldMask(const uint16_t* m, size_t i) {
   return *((volatile const uint16_t*)m + i);
 }
@@ -387,215 +380,10 @@ __device__ __forceinline__ void orMask(uint16_t* m, size_t i, uint16_t bits) {
   atomicOr(w32, (unsigned)bits << sh);
 }
 
-template <class T>
-__global__ void __launch_bounds__(FS_THREADS)
-    k_find_substamps(const T* __restrict__ img0, const T* __restrict__ img1,
-                     uint16_t* __restrict__ mask, const int4* __restrict__ geom,
-                     const double* __restrict__ sky0, const double* __restrict__ fwhm0,
-                     const double* __restrict__ sky1, const double* __restrict__ fwhm1,
-                     int2* __restrict__ xy0, double* __restrict__ val0, int* __restrict__ cnt0,
-                     int2* __restrict__ xy1, double* __restrict__ val1, int* __restrict__ cnt1,
-                     int w, int fSW, int hSS, int maxSS, double tH, double tKF) {
-  const int s = blockIdx.x, im = blockIdx.y, tid = threadIdx.x;
-  const T* img = im == 0 ? img0 : img1;
-  const double sky = im == 0 ? sky0[s] : sky1[s];
-  const double fwhm = im == 0 ? fwhm0[s] : fwhm1[s];
-  int2* xyOut = (im == 0 ? xy0 : xy1) + (size_t)s * maxSS;
-  double* valOut = (im == 0 ? val0 : val1) + (size_t)s * maxSS;
-  const uint16_t badMask =
-      (uint16_t)((MASK_ALL & ~OK_CONV) & ~(im == 0 ? (BAD_PIXEL_S | SKIP_S) : (BAD_PIXEL_T | SKIP_T)));
-  const uint16_t skipMask = im == 0 ? SKIP_T : SKIP_S;
-  const int4 gm = geom[s];
-  const int cx = gm.x, cy = gm.y, sx = gm.z, sy = gm.w;
-  const double invFwhm = 1.0 / fwhm;
-
-  __shared__ int cand[FS_CHUNK];
-  __shared__ int warpTot[FS_THREADS / 32];
-  __shared__ int sTotal;
-  __shared__ int2 locXY[MAX_MAXSS];
-  __shared__ double locVal[MAX_MAXSS];
-  __shared__ int sCnt;
-  __shared__ double redV[FS_THREADS / 32];
-  __shared__ int redI[FS_THREADS / 32];
-  __shared__ int sMx, sMy, sBad, sSkip;
-  __shared__ double sSum;
-  __shared__ double win[MAX_FSS * MAX_FSS];
-  __shared__ int failX[FS_FAILCACHE], failY[FS_FAILCACHE];
-  __shared__ int nFail;
-  if(tid == 0) {
-    sCnt = 0;
-    nFail = 0;
-  }
-  __syncthreads();
-  const double floorV = sky + tKF * fwhm;
-  double dfrac = 0.9;
-  int passes = 0;
-  const int nPix = fSW * fSW;
-  while(sCnt < maxSS && passes < 256) {
-    passes++;
-    const double alt = sky + (tH - sky) * dfrac;
-    const double lim = floorV < alt ? alt : floorV;  // OpenCL max()
-    for(int base = 0; base < nPix && sCnt < maxSS; base += FS_CHUNK) {
-      // candidate flags for 4 consecutive raster positions per thread
-      int myN = 0;
-      int myIdx[4];
-#pragma unroll
-      for(int k = 0; k < 4; k++) {
-        int r = base + tid * 4 + k;
-        myIdx[k] = -1;
-        if(r < nPix) {
-          int absx = r % fSW + cx, absy = r / fSW + cy;
-          size_t a = (size_t)absx + (size_t)absy * w;
-          if(!(ldMask(mask, a) & badMask)) {
-            double v = (double)img[a];
-            if(!((v - sky) * invFwhm < tKF) && v > lim) myIdx[myN++] = r;
-          }
-        }
-      }
-      int pos = blockExclusiveScan(myN, warpTot, &sTotal);
-      for(int k = 0; k < myN; k++) cand[pos + k] = myIdx[k];
-      const int nCand = sTotal;
-      __syncthreads();
-      for(int ci = 0; ci < nCand; ci++) {
-        const int r = cand[ci];
-        const int absx = r % fSW + cx, absy = r / fSW + cy;
-        // the candidate's own pixel may have been skipped meanwhile
-        if(tid == 0) sSkip = (ldMask(mask, (size_t)absx + (size_t)absy * w) & badMask) ? 1 : 0;
-        __syncthreads();
-        if(sSkip) continue;
-        // local maximum within +-hSS clipped to the fStampWidth window
-        const int x0 = max(absx - hSS, cx), y0 = max(absy - hSS, cy);
-        const int x1 = min(absx + hSS, cx + fSW - 1), y1 = min(absy + hSS, cy + fSW - 1);
-        const int ww = x1 - x0 + 1, wn = ww * (y1 - y0 + 1);
-        double bv = 0.0;
-        int bi = INT_MAX;
-        for(int i = tid; i < wn; i += FS_THREADS) {
-          int kx = x0 + i % ww, ky = y0 + i / ww;
-          size_t ka = (size_t)kx + (size_t)ky * w;
-          if(ldMask(mask, ka) & badMask) continue;
-          double kv = (double)img[ka];
-          if((kv - sky) * invFwhm < tKF) continue;
-          if(kv > bv || (kv == bv && bi != INT_MAX && i < bi)) {
-            if(kv > bv) {
-              bv = kv;
-              bi = i;
-            } else if(i < bi) {
-              bi = i;
-            }
-          }
-        }
-#pragma unroll
-        for(int o = 16; o > 0; o >>= 1) {
-          double ov = __shfl_down_sync(0xffffffffu, bv, o);
-          int oi = __shfl_down_sync(0xffffffffu, bi, o);
-          if(ov > bv || (ov == bv && oi < bi)) {
-            bv = ov;
-            bi = oi;
-          }
-        }
-        if((tid & 31) == 0) {
-          redV[tid >> 5] = bv;
-          redI[tid >> 5] = bi;
-        }
-        __syncthreads();
-        if(tid == 0) {
-          double b = redV[0];
-          int i = redI[0];
-          for(int k = 1; k < FS_THREADS / 32; k++)
-            if(redV[k] > b || (redV[k] == b && redI[k] < i)) {
-              b = redV[k];
-              i = redI[k];
-            }
-          if(i == INT_MAX || !(b > 0.0)) {
-            sMx = absx;
-            sMy = absy;
-          } else {
-            sMx = x0 + i % ww;
-            sMy = y0 + i / ww;
-          }
-          // a window that failed once fails for the rest of the search:
-          // the mask only gains bits while substamps are being found
-          sBad = 0;
-          for(int k = 0; k < nFail; k++)
-            if(failX[k] == sMx && failY[k] == sMy) sBad = 1;
-        }
-        __syncthreads();
-        if(sBad) continue;
-        const int mx = sMx, my = sMy;
-        // checkSStamp (sss.cl:393-428), window clipped to the stamp size
-        const int u0 = max(mx - hSS, cx), v0 = max(my - hSS, cy);
-        const int u1 = min(mx + hSS, cx + sx - 1), v1 = min(my + hSS, cy + sy - 1);
-        const int uw = u1 - u0 + 1, un = uw * (v1 - v0 + 1);
-        int anyBad = 0;
-        for(int i = tid; i < un; i += FS_THREADS) {
-          int kx = u0 + i % uw, ky = v0 + i / uw;
-          size_t ka = (size_t)kx + (size_t)ky * w;
-          if(ldMask(mask, ka) & badMask) anyBad = 1;
-          double v = (double)img[ka];
-          win[i] = ((v - sky) / fwhm > tKF) ? v : NAN;  // NaN marks "not summed"
-        }
-        anyBad = __syncthreads_or(anyBad);
-        if(tid == 0) {
-          double ret = 0.0;
-          if(!anyBad) {
-            for(int i = 0; i < un; i++) {
-              double v = win[i];
-              if(v == v) ret += v;
-            }
-          }
-          sSum = ret;
-          if(ret == 0.0 && nFail < FS_FAILCACHE) {
-            failX[nFail] = mx;
-            failY[nFail] = my;
-            nFail++;
-          }
-        }
-        __syncthreads();
-        const double ret = sSum;
-        if(ret == 0.0) continue;
-        if(tid == 0) {
-          locXY[sCnt] = make_int2(mx, my);
-          locVal[sCnt] = ret;
-        }
-        const int u2 = max(mx - hSS, cx), v2 = max(my - hSS, cy);
-        const int u3 = min(mx + hSS, cx + sx - 1), v3 = min(my + hSS, cy + sy - 1);
-        const int sw = u3 - u2 + 1, sn = sw * (v3 - v2 + 1);
-        for(int i = tid; i < sn; i += FS_THREADS)
-          orMask(mask, (size_t)(u2 + i % sw) + (size_t)(v2 + i / sw) * w, skipMask);
-        __syncthreads();
-        if(tid == 0) sCnt = sCnt + 1;
-        __syncthreads();
-        if(sCnt >= maxSS) break;
-      }
-      __syncthreads();
-    }
-    if(lim == floorV) break;
-    dfrac -= 0.2;
-  }
-  __syncthreads();
-  if(tid == 0) {
-    const int cnt = sCnt;
-    // insertion sort, descending (sortSubStamps, sss.cl:430-446)
-    for(int i = 1; i < cnt; i++)
-      for(int j = i; j > 0 && locVal[j - 1] < locVal[j]; j--) {
-        int2 t = locXY[j - 1];
-        locXY[j - 1] = locXY[j];
-        locXY[j] = t;
-        double tv = locVal[j - 1];
-        locVal[j - 1] = locVal[j];
-        locVal[j] = tv;
-      }
-    for(int i = 0; i < maxSS; i++) {
-      xyOut[i] = i < cnt ? locXY[i] : make_int2(INT_MAX, INT_MAX);
-      valOut[i] = i < cnt ? locVal[i] : -INFINITY;
-    }
-    (im == 0 ? cnt0 : cnt1)[s] = min(cnt, maxSS / 2);
-  }
-}
-
-// ------------------------------------------------ substamp search by maps --
-// The same decisions as k_find_substamps, restructured: between two accepted
-// substamps the mask does not change, so for every pixel of the stamp window
+// ---------------------------------------------------------- substamp search --
+// One CTA per (stamp, image): findSubStamps (cl_kern/sss.cl:448-572).  The
+// reference scans the stamp in raster order, testing each pixel.  Between two
+// accepted substamps the mask does not change, so for every pixel of the stamp window
 // the reference's local-maximum search (sss.cl:494-526) and window check
 // (checkSStamp, :393-428) are tabulated once per mask state:
 //   * a separable sliding-window argmax over the qualifying pixels (largest
@@ -610,7 +398,10 @@ __global__ void __launch_bounds__(FS_THREADS)
 // The accepted substamp's value is the sequential sum of sss.cl:421-424; for
 // FP32 input every summand is a float, all partial sums are exact in FP64
 // whenever sum|v| < 2^52 * (quantum of the smallest |v|), which is checked,
-// and then a parallel sum is the same number.
+// and then a parallel sum is the same number.  The reference's writes of the
+// bad-pixel bit for pixels above threshHigh (sss.cl:416-419, :484-487,
+// :512-515) are unreachable: such pixels carry BAD_INPUT from maskInput
+// (ini.cl:29), which every badMask contains, and that test comes first.
 constexpr int FM_THREADS = 256;
 enum : uint8_t { FL_PRED = 1, FL_NONPOS = 2, FL_KFQ = 4, FL_VPOS = 8 };
 enum : uint8_t { OK_BAD = 1, OK_PRED = 2, OK_NONPOS = 4 };
