@@ -1047,6 +1047,7 @@ void stageCd(xb_ctx* c) {
       c->scalars["cd_kernel_mean" + sfx] = toHost(c, kMean + si, 1)[0];
     }
   }
+  if(mixedMode(c)) checkSolveTimeout(c);
   c->convTemplate = c->merit[1] > c->merit[0] ? 1 : 0;
   c->chosen = c->convTemplate ? 0 : 1;
   c->scalars["merit0"] = c->merit[0];
@@ -1103,6 +1104,7 @@ void stageKsc(xb_ctx* c) {
   c->kscIterations = iteration;
   c->hSol = toHost(c, c->dSol, g.nSol);
   c->singular = toHost(c, f.singular, 1)[0];
+  if(mixedMode(c)) checkSolveTimeout(c);
   c->scalars["ksc_iterations"] = iteration;
   c->scalars["singular"] = c->singular;
   if(c->trace) {

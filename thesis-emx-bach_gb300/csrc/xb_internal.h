@@ -257,8 +257,16 @@ int mixedDotStride(const Geo& g);
 void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
 void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSol, int convImg,
                double* dSig);
-void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* singular);
+void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, int* piv,
+                     int* singular, const int* status);
 void convSubMixed(xb_ctx* c, double* dKernSum);
+
+// global system of the mixed path (xb_ldl.cu): LDL^T on a cluster, refined
+// solve, pivoted LU when a pivot fails.  M is kept; rhs becomes the solution.
+void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, int* singular);
+// Throws XB_ERR_DEVICE_TIMEOUT when a bounded wait of the cluster solve ran
+// out since the last call (synchronises the stream).
+void checkSolveTimeout(xb_ctx* c);
 inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
 
 // Kernel image at normalised position (xf, yf) and its sum into *dOut

@@ -18,6 +18,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 
 #include "xb_device.cuh"
@@ -338,8 +339,10 @@ __global__ void __launch_bounds__(MX_THREADS)
 // doubles, trailing updates with fused multiply-adds.
 template <int CL>
 __global__ void __launch_bounds__(256)
-    k_global_lu_fast(double* __restrict__ M, int n, int* __restrict__ idxOut,
-                     int* __restrict__ singular) {
+    k_global_lu_fast(const double* __restrict__ M, double* __restrict__ F, int n,
+                     int* __restrict__ idxOut, int* __restrict__ singular,
+                     const int* __restrict__ gate) {
+  if(gate != nullptr && !(gate[0] & 1)) return;  // the LDL^T factorisation succeeded
   extern __shared__ double gl_s[];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), tid = threadIdx.x, nt = blockDim.x;
@@ -362,8 +365,10 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   if(sSing) {
     if(rank == 0 && tid == 0) *singular = 1;
-    if(rank == 0)
+    if(rank == 0) {
       for(int i = tid; i <= n; i += nt) idxOut[i] = 0;
+      for(size_t q = tid; q < (size_t)ld * ld; q += nt) F[q] = M[q];  // left as it was
+    }
     cluster.sync();
     return;
   }
@@ -465,7 +470,7 @@ __global__ void __launch_bounds__(256)
   for(int lc = 0; lc < ncol; lc++) {
     const int j = lc * CL + rank + 1;
     if(j > n) break;
-    for(int i = tid; i <= n; i += nt) M[(size_t)i * ld + j] = col[(size_t)lc * ld + i];
+    for(int i = tid; i <= n; i += nt) F[(size_t)i * ld + j] = col[(size_t)lc * ld + i];
   }
   if(rank == 0 && tid == 0) idxOut[0] = 0;
 }
@@ -500,7 +505,9 @@ __device__ void sweepSolve(const double* __restrict__ LU, int n, const int* piv,
 
 __global__ void __launch_bounds__(1024)
     k_solve_refine(const double* __restrict__ LU, const double* __restrict__ A, int n,
-                   const int* __restrict__ piv, double* __restrict__ b) {
+                   const int* __restrict__ piv, double* __restrict__ b,
+                   const int* __restrict__ gate) {
+  if(gate != nullptr && !(gate[0] & 1)) return;  // solved from the LDL^T factors
   extern __shared__ double sv_s[];
   const int tid = threadIdx.x, nt = blockDim.x, ld = n + 1;
   double* x = sv_s;          // n + 1
@@ -790,13 +797,13 @@ void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSo
   XB_LAUNCHED(c);
 }
 
-// LU + refined solve of the (n+1)^2 system in M (row 0 / column 0 unused);
-// rhs (n+1 entries, index 0 unused) is replaced by the solution.
-void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* singular) {
+// The pivoted LU and its refined solve, run only when the LDL^T factorisation
+// flagged a pivot (status bit 0; both kernels return at once otherwise).  M is
+// left intact, the factors go to F, rhs is replaced by the solution.
+void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, int* piv,
+                     int* singular, const int* status) {
   const int ld = n + 1;
-  double* A = buf<double>(c, "mixed_A", (size_t)ld * ld);
-  XB_CUDA(cudaMemcpyAsync(A, M, sizeof(double) * ld * ld, cudaMemcpyDeviceToDevice, c->stream));
-  static int clusterSize = 0;
+  static std::atomic<int> clusterSize{0};
   auto launchLu = [&](auto kernel, int CL) -> cudaError_t {
     const int ncol = (n + CL - 1) / CL;
     const size_t smem = ((size_t)ncol * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
@@ -818,12 +825,12 @@ void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* s
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, M, n, piv, singular);
+    return cudaLaunchKernelEx(&cfg, kernel, M, F, n, piv, singular, status);
   };
   {
-    KT_SCOPE(c, "global_lu");
+    KT_SCOPE(c, "lu_fallback");
     cudaError_t e = cudaErrorUnknown;
-    if(clusterSize != 8) {
+    if(clusterSize.load() != 8) {
       e = launchLu(k_global_lu_fast<16>, 16);
       if(e == cudaSuccess) clusterSize = 16;
       else cudaGetLastError();
@@ -833,11 +840,8 @@ void globalSolveMixed(xb_ctx* c, double* M, int n, double* rhs, int* piv, int* s
       clusterSize = 8;
     }
     XB_LAUNCHED(c);
-  }
-  {
-    KT_SCOPE(c, "global_solve");
     const size_t smem = (size_t)4 * ld * sizeof(double) + (size_t)ld * sizeof(int);
-    k_solve_refine<<<1, 1024, smem, c->stream>>>(M, A, n, piv, rhs);
+    k_solve_refine<<<1, 1024, smem, c->stream>>>(F, M, n, piv, rhs, status);
     XB_LAUNCHED(c);
   }
 }
