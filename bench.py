@@ -250,7 +250,7 @@ def main():
                  "fill_w", "fill_finish", "gram_qb", "stamp_test_fit", "cd_select", "weights",
                  "stamp_dots", "build_matrix", "build_rhs", "global_lu", "global_lubksb",
                  "kernel_sum", "sigs", "cd_merit", "ksc_check", "conv_sub", "gram",
-                 "global_ldl", "lu_fallback", "global_solve"):
+                 "global_ldl", "lu_fallback", "global_solve", "mx_build", "mx_scatter"):
         ms, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}

@@ -898,20 +898,24 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
     XB_LAUNCHED(c);
     }
   }
+  const int bgBase = g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + (cpuRhs ? g.nBG : 0);
   const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
+  if(mixed) {
+    buildSystemMixed(c, si, f.list, nList, bgBase, f.M, dSol);
+  } else {
   { KT_SCOPE(c, "build_matrix");
   k_build_matrix<<<(int)std::min<long long>((nTri + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
       f.list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, dots, f.stride, mixed ? 1 : 0, g.nComp1,
       g.nComp2, g.nBG, g.matSize, f.M);
   XB_LAUNCHED(c);
   }
-  const int bgBase = g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + (cpuRhs ? g.nBG : 0);
   { KT_SCOPE(c, "build_rhs");
   k_build_rhs<<<(g.nSol + 127) / 128, 128, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.B,
                                                           g.qCount, f.wts, dots, f.stride,
                                                           mixed ? 1 : 0, bgBase, g.nComp1,
                                                           g.nComp2, g.nBG, g.nSol, dSol);
   XB_LAUNCHED(c);
+  }
   }
   if(c->trace) {
     const int ld = g.matSize + 1;

@@ -260,6 +260,8 @@ void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSo
 void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, int* piv,
                      int* singular, const int* status);
 void convSubMixed(xb_ctx* c, double* dKernSum);
+void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase, double* M,
+                      double* rhs);
 
 // global system of the mixed path (xb_ldl.cu): LDL^T on a cluster, refined
 // solve, pivoted LU when a pivot fails.  M is kept; rhs becomes the solution.

@@ -13,9 +13,9 @@
 // Factorisation.  Columns are dealt cyclically over the CL CTAs of a cluster
 // and live in shared memory.  Step j (1-based) is owned by CTA (j-1) % CL: it
 // sends the finished column j (unscaled) and r_j = 1/d_j to every other CTA
-// with st.async stores that complete on an mbarrier in the receiver; each CTA
-// then applies a_ik -= a_ij * (a_kj * r_j) to its own columns k > j, rows
-// i >= k.  The owner of column j+1 applies step j to that column first,
+// with one bulk shared-to-shared copy per receiver that completes on an
+// mbarrier in the receiver; each CTA then applies a_ik -= a_ij * (a_kj * r_j)
+// to its own columns k > j, rows i >= k.  The owner of column j+1 applies step j to that column first,
 // factors it and sends it before touching its other columns, so the critical
 // path per step is one shared-memory hop plus one column update.  Receive
 // buffers form a ring of LDL_RING slots per CTA; a slot is refilled only
@@ -24,10 +24,11 @@
 // timer deadline; on expiry the kernel records a timeout and runs to the end
 // without waiting, so the launch always terminates.
 //
-// Solve.  One cluster: CTA 0 runs the triangular solves (blocks of 32 rows, a
-// warp per diagonal block, the other warps update the remaining rows), all
-// CTAs compute the FP64 residual r = b - A x of the original matrix, and
-// CTA 0 solves for the correction, which is added once.
+// Solve.  One cluster: the CTAs invert the 32x32 diagonal blocks of L, CTA 0
+// runs the blocked triangular solves (a block = one small product with its
+// inverse, then the rows below/above it), all CTAs compute the FP64 residual
+// r = b - A x of the original matrix, and CTA 0 solves for the correction,
+// which is added once.
 
 #include <cooperative_groups.h>
 
@@ -76,13 +77,20 @@ __device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ void stAsync2(uint32_t clusterAddr, double a, double b,
-                                         uint32_t clusterBar) {
+// Bulk copy of `bytes` from this CTA's shared memory to another CTA's,
+// completing `bytes` of transactions on that CTA's mbarrier.
+__device__ __forceinline__ void bulkCopyCluster(uint32_t dstCluster, uint32_t srcCta,
+                                                uint32_t bytes, uint32_t barCluster) {
   asm volatile(
-      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(
-          clusterAddr),
-      "d"(a), "d"(b), "r"(clusterBar)
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];" ::"r"(dstCluster),
+      "r"(srcCta), "r"(bytes), "r"(barCluster)
       : "memory");
+}
+// Orders this thread's earlier shared-memory writes before later reads of the
+// async proxy (the bulk copies).
+__device__ __forceinline__ void fenceProxyAsync() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ unsigned long long globalTimer() {
   unsigned long long t;
@@ -102,12 +110,11 @@ __device__ __forceinline__ double recipFast(double d) {
   return fma(x0, fma(e, e, e), x0);
 }
 
-// Bytes step j sends to one receiver: the pair (r_j, 0) at slot entry 0 and
-// the column entries from the even row at or below j+1 up to n (pairs, so the
-// last pair may carry row n+1, which is zero).
-__device__ __forceinline__ uint32_t stepBytes(int j, int n) {
-  const int i0 = (j + 1) & ~1;
-  return 16u * (uint32_t)((n - i0) / 2 + 2);
+// Bytes step j sends to one receiver: entries [i0-2, LC) of the column, i0
+// the even row at or below j+1 (entry i0-2 carries r_j; LC is even, so the
+// size is a multiple of 16 bytes and both ends are 16-byte aligned).
+__device__ __forceinline__ uint32_t stepBytes(int j, int LC) {
+  return 8u * (uint32_t)(LC - ((j + 1) & ~1) + 2);
 }
 
 // Bounded wait on a local mbarrier phase; false (and the timeout flags set)
@@ -130,7 +137,7 @@ __device__ __forceinline__ bool waitPhase(uint32_t bar, uint32_t parity,
 
 // status[0] bit 0: a pivot was not positive and finite (LU fallback);
 // status[1] bit 0: a wait ran out of time.  F receives d_k on the diagonal and
-// l_ik (i > k) in row k (F[k][i], the upper triangle); rinv[k] = 1/d_k.
+// l_ik (i > k) in both triangles (F[k][i] and F[i][k]); rinv[k] = 1/d_k.
 template <int CL>
 __global__ void __launch_bounds__(LDL_THREADS)
     k_global_ldl(const double* __restrict__ M, double* __restrict__ F, double* __restrict__ rinv,
@@ -146,8 +153,7 @@ __global__ void __launch_bounds__(LDL_THREADS)
   double* col = ldl_s;                               // ncol x LC
   double* slot = col + (size_t)ncol * LC;            // LDL_RING x LC
   double* rvec = slot + (size_t)LDL_RING * LC;       // LC
-  double* cbuf = rvec + LC;                          // ncol, padded to even
-  unsigned long long* bars = (unsigned long long*)(cbuf + ((ncol + 1) & ~1));
+  unsigned long long* bars = (unsigned long long*)(rvec + LC);
   // bars[0..LDL_RING) full (receive) barriers, bars[LDL_RING] the empty barrier
   __shared__ int sErr;
   const unsigned long long deadline = globalTimer() + LDL_WAIT_NS;
@@ -168,7 +174,7 @@ __global__ void __launch_bounds__(LDL_THREADS)
     for(int r = 0; r < LDL_RING; r++)
       for(int j = r + 1; j <= n - 1; j += LDL_RING)
         if((j - 1) % CL != rank) {
-          mbarArriveExpect(smemAddr(&bars[r]), stepBytes(j, n));
+          mbarArriveExpect(smemAddr(&bars[r]), stepBytes(j, LC));
           break;
         }
   }
@@ -179,54 +185,44 @@ __global__ void __launch_bounds__(LDL_THREADS)
   uint32_t emptyPhase = 0;
   volatile int* vErr = &sErr;
 
-  // Send the finished column jp (owned here) to every other CTA.
-  auto produce = [&](int jp) {
-    const double* cp = col + (size_t)((jp - 1) / CL) * LC;
-    const int rs = (jp - 1) % LDL_RING;
-    if(jp > LDL_RING) {
-      waitPhase(smemAddr(&bars[LDL_RING]), emptyPhase, deadline, vErr, status);
-      emptyPhase ^= 1u;
+  // Pivot of the finished column jp (owned here): r = 1/d is stored in rvec
+  // and at entry i0-2 of the column (a row above the diagonal, never used
+  // again), where it travels with the column.  One thread.
+  auto pivotStore = [&](int jp) {
+    double* cp = col + (size_t)((jp - 1) / CL) * LC;
+    const double d = cp[jp];
+    double r = recipFast(d);
+    if(!(d > 0.0) || !isfinite(r)) {
+      atomicOr(status, 1);
+      r = 0.0;
     }
-    const uint32_t slotA = smemAddr(slot + (size_t)rs * LC);
-    const uint32_t fullA = smemAddr(&bars[rs]);
-    if(warp == 0) {
-      const double d = cp[jp];
-      double r = recipFast(d);
-      if(!(d > 0.0) || !isfinite(r)) {
-        if(lane == 0) atomicOr(status, 1);
-        r = 0.0;
-      }
-      if(lane < CL - 1) {
-        const int dst = lane < rank ? lane : lane + 1;
-        stAsync2(mapaRank(slotA, dst), r, 0.0, mapaRank(fullA, dst));
-      }
-      if(lane == 0) rvec[jp] = r;
-    }
-    const int i0 = (jp + 1) & ~1, P = (n - i0) / 2 + 1;
-    for(int e = tid; e < (CL - 1) * P; e += LDL_THREADS) {
-      const int q = e / P, i = i0 + 2 * (e - q * P);
-      const int dst = q < rank ? q : q + 1;
-      const double2 v = *reinterpret_cast<const double2*>(cp + i);
-      stAsync2(mapaRank(slotA + (uint32_t)i * 8u, dst), v.x, v.y, mapaRank(fullA, dst));
-    }
+    rvec[jp] = r;
+    cp[((jp + 1) & ~1) - 2] = r;
   };
-
-  // The last pivot is only used by its owner: it is not sent.
-  auto lastPivot = [&]() {
+  // Copy column jp, entries [i0-2, LC), to the same place in every other
+  // CTA's receive slot, completing on that CTA's full barrier.  Called by all
+  // threads after the column's writes were fenced for the async proxy and
+  // the CTA synchronised; thread 0 waits for the slot and issues the copies.
+  auto sendColumn = [&](int jp) {
     if(tid == 0) {
-      const double d = col[(size_t)((n - 1) / CL) * LC + n];
-      double r = recipFast(d);
-      if(!(d > 0.0) || !isfinite(r)) {
-        atomicOr(status, 1);
-        r = 0.0;
-      }
-      rvec[n] = r;
+      if(jp > LDL_RING) waitPhase(smemAddr(&bars[LDL_RING]), emptyPhase, deadline, vErr, status);
+      const int rs = (jp - 1) % LDL_RING;
+      const uint32_t off = (uint32_t)(((jp + 1) & ~1) - 2) * 8u;
+      const uint32_t src = smemAddr(col + (size_t)((jp - 1) / CL) * LC) + off;
+      const uint32_t dstSlot = smemAddr(slot + (size_t)rs * LC) + off;
+      const uint32_t fullA = smemAddr(&bars[rs]);
+      const uint32_t bytes = stepBytes(jp, LC);
+      for(int q = 0; q < CL; q++)
+        if(q != rank) bulkCopyCluster(mapaRank(dstSlot, q), src, bytes, mapaRank(fullA, q));
     }
+    if(jp > LDL_RING) emptyPhase ^= 1u;
   };
 
   if(rank == 0) {
-    if(n > 1) produce(1);
-    else lastPivot();
+    if(tid == 0) pivotStore(1);
+    fenceProxyAsync();
+    __syncthreads();
+    if(n > 1) sendColumn(1);
   }
   for(int j = 1; j < n; j++) {
     const int rs = (j - 1) % LDL_RING;
@@ -239,35 +235,31 @@ __global__ void __launch_bounds__(LDL_THREADS)
       waitPhase(smemAddr(&bars[rs]), (phaseBits >> rs) & 1u, deadline, vErr, status);
       phaseBits ^= 1u << rs;
     }
-    const double r = own ? rvec[j] : a[0];
-    const int lcStart = (j - rank + CL - 1) / CL;  // first local column k > j
-    for(int lc = lcStart + tid; lc < ncol; lc += LDL_THREADS) {
-      const int k = lc * CL + rank + 1;
-      if(k <= n) cbuf[lc] = a[k] * r;
-    }
+    const double r = own ? rvec[j] : a[((j + 1) & ~1) - 2];
     if(!own && tid == 0) rvec[j] = r;
-    __syncthreads();
-    const bool ahead = j % CL == rank;  // this CTA owns column j + 1
+    const int lcStart = (j - rank + CL - 1) / CL;  // first local column k > j
+    const bool ahead = j % CL == rank;             // this CTA owns column j + 1
     if(ahead) {
       double* c1 = col + (size_t)lcStart * LC;
-      const double cf = cbuf[lcStart];
+      const double cf = a[j + 1] * r;
       for(int i = j + 1 + tid; i <= n; i += LDL_THREADS) c1[i] = fma(-a[i], cf, c1[i]);
+      if(tid == 0) pivotStore(j + 1);  // row j+1 was this thread's first
+      fenceProxyAsync();
       __syncthreads();
-      if(j + 1 < n) produce(j + 1);
-      else lastPivot();
+      if(j + 1 < n) sendColumn(j + 1);
     }
     for(int lc = lcStart + (ahead ? 1 : 0) + warp; lc < ncol; lc += NW) {
       const int k = lc * CL + rank + 1;
       if(k > n) break;
       double* ck = col + (size_t)lc * LC;
-      const double cf = cbuf[lc];
+      const double cf = a[k] * r;
       for(int i = k + lane; i <= n; i += 32) ck[i] = fma(-a[i], cf, ck[i]);
     }
     __syncthreads();
     if(!own && tid == 0) {
       for(int jn = j + LDL_RING; jn <= n - 1; jn += LDL_RING)
         if((jn - 1) % CL != rank) {
-          mbarArriveExpect(smemAddr(&bars[rs]), stepBytes(jn, n));
+          mbarArriveExpect(smemAddr(&bars[rs]), stepBytes(jn, LC));
           break;
         }
       if(j + LDL_RING <= n - 1)
@@ -280,8 +272,11 @@ __global__ void __launch_bounds__(LDL_THREADS)
     if(k > n) break;
     const double* ck = col + (size_t)lc * LC;
     const double rk = rvec[k];
-    for(int i = k + tid; i <= n; i += LDL_THREADS)
-      F[(size_t)k * ld + i] = i == k ? ck[k] : ck[i] * rk;
+    for(int i = k + tid; i <= n; i += LDL_THREADS) {
+      const double v = i == k ? ck[k] : ck[i] * rk;
+      F[(size_t)k * ld + i] = v;  // row k: l_ik, i > k
+      F[(size_t)i * ld + k] = v;  // row i: l_ik, k < i
+    }
     if(tid == 0) rinv[k] = rk;
   }
   cluster.sync();  // no CTA leaves while another may still address its shared memory
@@ -291,75 +286,152 @@ __global__ void __launch_bounds__(LDL_THREADS)
 namespace {
 
 constexpr int SV_THREADS = 1024;
-constexpr int SV_NB = 32;
+constexpr int SV_NB = 32;  // diagonal block size
+constexpr int SV_AW = 4;   // warps of a 32x32 block product (8 terms each)
 
-// L y = b then x = L^-T D^-1 y in place on x[1..n] (shared), CTA-wide.
-// U[k][i] = l_ik for i > k (row k of F).  blk: SV_NB x (SV_NB + 1) doubles.
+// Inverse of the unit lower-triangular diagonal block q of L (rows/cols
+// [1 + 32q, 1 + 32q + 32), padded with the identity past n) into Linv
+// (32 x 32, row-major), by recursive doubling: for a 2m block
+// [[A, 0], [C, B]] the inverse's lower-left part is -B^-1 (C A^-1).
+// CTA-wide; X is 32 x 33, T 256 doubles of shared memory.
+__device__ void invertDiagBlock(const double* __restrict__ F, int n, int q, double* X, double* T,
+                                double* __restrict__ Linv) {
+  const int tid = threadIdx.x, ld = n + 1, s = 1 + q * SV_NB;
+  constexpr int XL = SV_NB + 1;
+  for(int e = tid; e < SV_NB * SV_NB; e += SV_THREADS) {
+    const int t = e / SV_NB, u = e % SV_NB;
+    double v = t == u ? 1.0 : 0.0;
+    if(t > u && s + t <= n) v = F[(size_t)(s + t) * ld + s + u];  // L[t][u] (kept in X's lower part)
+    X[t * XL + u] = v;
+  }
+  __syncthreads();
+  // X's strictly lower part holds L until each level overwrites its blocks
+  for(int m = 1; m < SV_NB; m *= 2) {
+    const int nPair = SV_NB / (2 * m), cnt = nPair * m * m;
+    // T = C A^-1 for every pair block
+    for(int e = tid; e < cnt; e += SV_THREADS) {
+      const int p = e / (m * m), a = (e / m) % m, b = e % m, o = p * 2 * m;
+      double acc = 0.0;
+      for(int c = b; c < m; c++)  // A^-1 is unit lower: entries c >= b
+        acc = fma(X[(o + m + a) * XL + o + c], c == b ? 1.0 : X[(o + c) * XL + o + b], acc);
+      T[e] = acc;
+    }
+    __syncthreads();
+    // lower-left <- -B^-1 T
+    for(int e = tid; e < cnt; e += SV_THREADS) {
+      const int p = e / (m * m), a = (e / m) % m, b = e % m, o = p * 2 * m;
+      double acc = T[e];  // the unit diagonal of B^-1
+      for(int c = 0; c < a; c++) acc = fma(X[(o + m + a) * XL + o + m + c], T[p * m * m + c * m + b], acc);
+      X[(o + m + a) * XL + o + b] = -acc;
+    }
+    __syncthreads();
+  }
+  for(int e = tid; e < SV_NB * SV_NB; e += SV_THREADS)
+    Linv[(size_t)q * SV_NB * SV_NB + e] = X[(e / SV_NB) * XL + e % SV_NB];
+  __syncthreads();
+}
+
+// x <- L^-T D^-1 L^-1 x on x[1..n] (shared), CTA-wide, with the inverses of
+// the diagonal blocks in Li (shared, nB x 32 x 32).  Per block: the 32x32
+// product with the inverse (warps 0-3, eight terms each), then the next
+// block's rows (warps 0-3) and, at the same time, the rows beyond it
+// (warps 4-31, one row per thread).  part: SV_AW x 32 doubles.
 __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restrict__ rinv, int n,
-                            double* x, double* blk) {
+                            const double* Li, double* x, double* part) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, ld = n + 1;
-  constexpr int BL = SV_NB + 1;
-  // forward, right-looking by blocks of rows [s, e)
-  for(int s = 1; s <= n; s += SV_NB) {
-    const int e = min(s + SV_NB, n + 1), nb = e - s;
-    for(int q = tid; q < SV_NB * SV_NB; q += SV_THREADS) {
-      const int jj = q / SV_NB, t = q % SV_NB;  // blk[jj][t] = l_{s+t, s+jj}
-      blk[jj * BL + t] = (jj < nb && t < nb && t > jj) ? F[(size_t)(s + jj) * ld + s + t] : 0.0;
-    }
-    __syncthreads();
-    if(warp == 0) {
-      double v = lane < nb ? x[s + lane] : 0.0;
+  const int nB = (n + SV_NB - 1) / SV_NB;
+  // ---- forward: L y = x
+  for(int K = 0; K < nB; K++) {
+    const int s = 1 + K * SV_NB, nb = min(SV_NB, n + 1 - s);
+    const double* Lk = Li + (size_t)K * SV_NB * SV_NB;
+    if(warp < SV_AW) {  // y_K = Linv_K x_K
+      double acc = 0.0;
 #pragma unroll
-      for(int jj = 0; jj < SV_NB; jj++) {
-        const double yj = __shfl_sync(0xffffffffu, v, jj);
-        v = fma(-blk[jj * BL + lane], yj, v);
+      for(int u = 0; u < SV_NB / SV_AW; u++) {
+        const int t = warp * (SV_NB / SV_AW) + u;
+        if(t < nb) acc = fma(Lk[lane * SV_NB + t], x[s + t], acc);
       }
-      if(lane < nb) x[s + lane] = v;
+      part[warp * 32 + lane] = acc;
     }
     __syncthreads();
-    for(int i = e + tid; i <= n; i += SV_THREADS) {
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-      int jj = 0;
-      for(; jj + 4 <= nb; jj += 4) {
-        a0 = fma(F[(size_t)(s + jj) * ld + i], x[s + jj], a0);
-        a1 = fma(F[(size_t)(s + jj + 1) * ld + i], x[s + jj + 1], a1);
-        a2 = fma(F[(size_t)(s + jj + 2) * ld + i], x[s + jj + 2], a2);
-        a3 = fma(F[(size_t)(s + jj + 3) * ld + i], x[s + jj + 3], a3);
+    if(warp == 0 && lane < nb)
+      x[s + lane] = (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
+    __syncthreads();
+    const int s2 = s + SV_NB, nb2 = min(SV_NB, n + 1 - s2);  // next block
+    if(warp < SV_AW) {
+      if(nb2 > 0) {
+        double acc = 0.0;
+#pragma unroll
+        for(int u = 0; u < SV_NB / SV_AW; u++) {
+          const int t = warp * (SV_NB / SV_AW) + u;
+          if(t < nb && lane < nb2) acc = fma(F[(size_t)(s + t) * ld + s2 + lane], x[s + t], acc);
+        }
+        part[warp * 32 + lane] = acc;
       }
-      for(; jj < nb; jj++) a0 = fma(F[(size_t)(s + jj) * ld + i], x[s + jj], a0);
-      x[i] -= (a0 + a1) + (a2 + a3);
+    } else {
+      for(int i = s2 + SV_NB + (tid - SV_AW * 32); i <= n; i += SV_THREADS - SV_AW * 32) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        for(int t = 0; t + 4 <= nb; t += 4) {
+          a0 = fma(F[(size_t)(s + t) * ld + i], x[s + t], a0);
+          a1 = fma(F[(size_t)(s + t + 1) * ld + i], x[s + t + 1], a1);
+          a2 = fma(F[(size_t)(s + t + 2) * ld + i], x[s + t + 2], a2);
+          a3 = fma(F[(size_t)(s + t + 3) * ld + i], x[s + t + 3], a3);
+        }
+        for(int t = nb & ~3; t < nb; t++) a0 = fma(F[(size_t)(s + t) * ld + i], x[s + t], a0);
+        x[i] -= (a0 + a1) + (a2 + a3);
+      }
     }
+    __syncthreads();
+    if(warp == 0 && nb2 > 0 && lane < nb2)
+      x[s2 + lane] -= (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
     __syncthreads();
   }
   for(int i = 1 + tid; i <= n; i += SV_THREADS) x[i] *= rinv[i];
   __syncthreads();
-  // backward: x_k = z_k - sum_{i>k} l_ik x_i, blocks from the bottom
-  const int nBlk = (n + SV_NB - 1) / SV_NB;
-  for(int b = nBlk - 1; b >= 0; b--) {
-    const int s = 1 + b * SV_NB, e = min(s + SV_NB, n + 1), nb = e - s;
-    for(int q = tid; q < SV_NB * SV_NB; q += SV_THREADS) {
-      const int t = q / SV_NB, ii = q % SV_NB;  // blk[t][ii] = l_{s+ii, s+t}
-      blk[t * BL + ii] = (t < nb && ii < nb && ii > t) ? F[(size_t)(s + t) * ld + s + ii] : 0.0;
-    }
-    // tails: row s + warp against the final x beyond the block
-    if(warp < nb) {
-      const int k = s + warp;
-      double a = 0.0;
-      for(int i = e + lane; i <= n; i += 32) a = fma(F[(size_t)k * ld + i], x[i], a);
+  // ---- backward: L^T x = z, blocks from the bottom; (Linv_K)^T on the block
+  for(int K = nB - 1; K >= 0; K--) {
+    const int s = 1 + K * SV_NB, nb = min(SV_NB, n + 1 - s);
+    const double* Lk = Li + (size_t)K * SV_NB * SV_NB;
+    if(warp < SV_AW) {
+      double acc = 0.0;
 #pragma unroll
-      for(int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if(lane == 0) x[k] -= a;
+      for(int u = 0; u < SV_NB / SV_AW; u++) {
+        const int t = warp * (SV_NB / SV_AW) + u;
+        if(t < nb) acc = fma(Lk[t * SV_NB + lane], x[s + t], acc);
+      }
+      part[warp * 32 + lane] = acc;
     }
     __syncthreads();
-    if(warp == 0) {
-      double v = lane < nb ? x[s + lane] : 0.0;
+    if(warp == 0 && lane < nb)
+      x[s + lane] = (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
+    __syncthreads();
+    const int s2 = s - SV_NB;  // previous block (full size)
+    if(warp < SV_AW) {
+      if(K > 0) {
+        double acc = 0.0;
 #pragma unroll
-      for(int ii = SV_NB - 1; ii >= 0; ii--) {
-        const double xi = __shfl_sync(0xffffffffu, v, ii);
-        v = fma(-blk[lane * BL + ii], xi, v);
+        for(int u = 0; u < SV_NB / SV_AW; u++) {
+          const int t = warp * (SV_NB / SV_AW) + u;  // row s+t of L, column s2+lane
+          if(t < nb) acc = fma(F[(size_t)(s + t) * ld + s2 + lane], x[s + t], acc);
+        }
+        part[warp * 32 + lane] = acc;
       }
-      if(lane < nb) x[s + lane] = v;
+    } else {
+      for(int k = 1 + (tid - SV_AW * 32); k < s2; k += SV_THREADS - SV_AW * 32) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        for(int t = 0; t + 4 <= nb; t += 4) {
+          a0 = fma(F[(size_t)(s + t) * ld + k], x[s + t], a0);
+          a1 = fma(F[(size_t)(s + t + 1) * ld + k], x[s + t + 1], a1);
+          a2 = fma(F[(size_t)(s + t + 2) * ld + k], x[s + t + 2], a2);
+          a3 = fma(F[(size_t)(s + t + 3) * ld + k], x[s + t + 3], a3);
+        }
+        for(int t = nb & ~3; t < nb; t++) a0 = fma(F[(size_t)(s + t) * ld + k], x[s + t], a0);
+        x[k] -= (a0 + a1) + (a2 + a3);
+      }
     }
+    __syncthreads();
+    if(warp == 0 && K > 0)
+      x[s2 + lane] -= (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
     __syncthreads();
   }
 }
@@ -367,30 +439,39 @@ __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restri
 }  // namespace
 
 // Refined solve on a cluster: rhs (n+1 entries, index 0 unused) is replaced by
-// the solution.  With status bit 0 set the LU factors and pivots of the
-// fallback are used instead (F holds the LU of the pivoted kernel).
+// the solution.  With status bit 0 set the pivoted LU solves the system
+// instead and this kernel returns at once.  Linv: global scratch for the
+// inverses of the diagonal blocks (ceil(n/32) x 32 x 32).
 template <int CL>
 __global__ void __launch_bounds__(SV_THREADS)
     k_ldl_solve(const double* __restrict__ A, const double* __restrict__ F,
                 const double* __restrict__ rinv, int n, double* __restrict__ rhs,
-                const int* __restrict__ status) {
+                const int* __restrict__ status, double* __restrict__ Linv) {
   extern __shared__ __align__(16) double sv_s[];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ld = n + 1, LX = (n + 2) & ~1;
-  double* x = sv_s;          // LX: solution, then correction (CTA 0)
-  double* b = x + LX;        // LX: right-hand side, then residual
-  double* x1 = b + LX;       // LX: first solution
-  double* blk = x1 + LX;     // SV_NB x (SV_NB + 1)
+  const int ld = n + 1, LX = (n + 2) & ~1, nB = (n + SV_NB - 1) / SV_NB;
+  double* x = sv_s;                  // LX: solution, then correction (CTA 0)
+  double* b = x + LX;                // LX: right-hand side, then residual
+  double* x1 = b + LX;               // LX: first solution
+  double* part = x1 + LX;            // SV_AW x 32
+  double* Li = part + SV_AW * 32;    // nB x 32 x 32 (CTA 0); inversion scratch elsewhere
   if(status[0] & 1) return;  // the LU fallback solves this system
+  {
+    double* X = Li + (rank == 0 ? (size_t)nB * SV_NB * SV_NB : 0);
+    double* T = X + SV_NB * (SV_NB + 1);
+    for(int q = rank; q < nB; q += CL) invertDiagBlock(F, n, q, X, T, Linv);
+  }
+  cluster.sync();
   if(rank == 0) {
+    for(int e = tid; e < nB * SV_NB * SV_NB; e += SV_THREADS) Li[e] = Linv[e];
     for(int i = tid; i < LX; i += SV_THREADS) {
       const double v = i >= 1 && i <= n ? rhs[i] : 0.0;
       b[i] = v;
       x[i] = v;
     }
     __syncthreads();
-    ldlSolveCta(F, rinv, n, x, blk);
+    ldlSolveCta(F, rinv, n, Li, x, part);
     for(int i = tid; i < LX; i += SV_THREADS) x1[i] = x[i];
   }
   cluster.sync();
@@ -398,11 +479,10 @@ __global__ void __launch_bounds__(SV_THREADS)
   {
     const double* x0 = cluster.map_shared_rank(x1, 0);
     double* b0 = cluster.map_shared_rank(b, 0);
-    double* xl = x;  // local copy of x1 (CTA 0 copies onto itself harmlessly later)
     if(rank != 0)
-      for(int i = tid; i < LX; i += SV_THREADS) xl[i] = x0[i];
+      for(int i = tid; i < LX; i += SV_THREADS) x[i] = x0[i];
     __syncthreads();
-    const double* xs = rank == 0 ? x1 : xl;
+    const double* xs = rank == 0 ? x1 : x;
     constexpr int NWv = SV_THREADS / 32;
     for(int i = 1 + rank * NWv + warp; i <= n; i += CL * NWv) {
       double a = 0.0;
@@ -416,7 +496,7 @@ __global__ void __launch_bounds__(SV_THREADS)
   if(rank == 0) {
     for(int i = tid; i < LX; i += SV_THREADS) x[i] = i >= 1 && i <= n ? b[i] : 0.0;
     __syncthreads();
-    ldlSolveCta(F, rinv, n, x, blk);
+    ldlSolveCta(F, rinv, n, Li, x, part);
     for(int i = 1 + tid; i <= n; i += SV_THREADS) rhs[i] = x1[i] + x[i];
   }
 }
@@ -424,15 +504,15 @@ __global__ void __launch_bounds__(SV_THREADS)
 template __global__ void k_global_ldl<8>(const double*, double*, double*, int, int*);
 template __global__ void k_global_ldl<16>(const double*, double*, double*, int, int*);
 template __global__ void k_ldl_solve<8>(const double*, const double*, const double*, int, double*,
-                                        const int*);
+                                        const int*, double*);
 template __global__ void k_ldl_solve<16>(const double*, const double*, const double*, int, double*,
-                                         const int*);
+                                         const int*, double*);
 
 namespace {
 
 size_t ldlSmemBytes(int n, int CL) {
   const int LC = (n + 3) & ~1, ncol = (n + CL - 1) / CL;
-  return ((size_t)ncol * LC + (size_t)LDL_RING * LC + LC + ((ncol + 1) & ~1)) * sizeof(double) +
+  return ((size_t)ncol * LC + (size_t)LDL_RING * LC + LC) * sizeof(double) +
          (LDL_RING + 1) * sizeof(unsigned long long);
 }
 
@@ -492,13 +572,17 @@ void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, 
   luFallbackSolve(c, M, F, n, rhs, piv, singular, status);
   {
     KT_SCOPE(c, "global_solve");
-    const size_t smem = ((size_t)3 * ((n + 2) & ~1) + SV_NB * (SV_NB + 1)) * sizeof(double);
+    const int nB = (n + SV_NB - 1) / SV_NB;
+    double* Linv = buf<double>(c, "ldl_linv", (size_t)nB * SV_NB * SV_NB);
+    const size_t smem = ((size_t)3 * ((n + 2) & ~1) + SV_AW * 32 + (size_t)nB * SV_NB * SV_NB +
+                         SV_NB * (SV_NB + 1) + 256) *
+                        sizeof(double);
     if(clusterSize.load() == 16)
       XB_CUDA(launchCluster(c, k_ldl_solve<16>, 16, SV_THREADS, smem, (const double*)M,
-                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status));
+                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status, Linv));
     else
       XB_CUDA(launchCluster(c, k_ldl_solve<8>, 8, SV_THREADS, smem, (const double*)M,
-                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status));
+                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status, Linv));
     XB_LAUNCHED(c);
   }
 }

@@ -716,6 +716,158 @@ __global__ void k_border_f32(const float* __restrict__ O, int w, int h, int hK, 
   }
 }
 
+// ------------------------------------------------ global matrix and RHS ---
+// Every entry of createMatrix / createScProd (cdkscUtil.cpp:307-475) is a sum
+// over the fitted stamps of one per-stamp number (a Q entry, a W dot product
+// or a B entry) times a spatial factor: a product of two kernel weights, one
+// weight, or 1.  The weights are monomials x^a y^b of the substamp position,
+// so a product of two is the monomial of the summed exponents.  The sums are
+// therefore the products X (rows: per-stamp numbers) x Y (columns: the
+// monomials up to twice the kernel order, zero for a stamp without a
+// substamp, plus an unmasked 1), computed split over chunks of 32 stamps
+// into partials P[split][row][col]; k_mx_scatter adds the splits in order
+// and places every matrix and RHS entry.
+//   X rows: [Q pairs (qa, qb), 2 <= qa <= nC1+1, 1 <= qb <= qa]
+//           [Q(1,1)] [dots entries 0..stride) [B entries 1..nC1+1]
+constexpr int MXB_ROWS = 64, MXB_T = 32, MXB_MAXC = 32;
+
+__device__ __forceinline__ int mxPairRow(int qa, int qb) { return (qa - 1) * qa / 2 - 1 + (qb - 1); }
+
+__global__ void __launch_bounds__(256)
+    k_mx_build(const int* __restrict__ list, int nList, const int* __restrict__ count,
+               const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
+               const double* __restrict__ Q, int qc, const double* __restrict__ dots, int stride,
+               const double* __restrict__ B, const int2* __restrict__ monoExp, int nMono, int w,
+               int h, int nC1, int nRows, double* __restrict__ P) {
+  __shared__ double Xs[MXB_ROWS][MXB_T + 1];
+  __shared__ double Ys[MXB_T][MXB_MAXC];
+  __shared__ int sS[MXB_T];
+  const int tid = threadIdx.x, split = blockIdx.y, t0 = split * MXB_T;
+  const int nt = min(MXB_T, nList - t0), row0 = blockIdx.x * MXB_ROWS, NC = nMono + 1;
+  const int nQP = mxPairRow(nC1 + 2, 1);  // Q pairs
+  if(tid < MXB_T) sS[tid] = tid < nt ? list[t0 + tid] : -1;
+  __syncthreads();
+  for(int e = tid; e < MXB_T * NC; e += 256) {
+    const int tt = e / NC, cI = e % NC, st = sS[tt];
+    double v = 0.0;
+    if(st >= 0) {
+      if(cI == nMono) {
+        v = 1.0;
+      } else if(cur[st] < count[st]) {
+        const int2 c = ssxy[(size_t)st * maxSS + cur[st]];
+        const int2 ex = monoExp[cI];
+        v = ipowD(floatNormD(c.x, w), ex.x) * ipowD(floatNormD(c.y, h), ex.y);
+      }
+    }
+    Ys[tt][cI] = v;
+  }
+  for(int e = tid; e < MXB_ROWS * MXB_T; e += 256) {
+    const int r = e / MXB_T, tt = e % MXB_T, row = row0 + r, st = sS[tt];
+    double v = 0.0;
+    if(st >= 0 && row < nRows) {
+      if(row < nQP) {
+        int qa = (int)((sqrt(8.0 * (double)(row + 1) + 1.0) - 1.0) * 0.5) + 1;  // first guess
+        while(mxPairRow(qa + 1, 1) <= row) qa++;
+        while(mxPairRow(qa, 1) > row) qa--;
+        const int qb = row - mxPairRow(qa, 1) + 1;
+        v = Q[(size_t)st * qc * qc + (size_t)qa * qc + qb];
+      } else if(row == nQP) {
+        v = Q[(size_t)st * qc * qc + qc + 1];
+      } else if(row < nQP + 1 + stride) {
+        v = dots[(size_t)st * stride + (row - nQP - 1)];
+      } else {
+        v = B[(size_t)st * qc + 1 + (row - nQP - 1 - stride)];
+      }
+    }
+    Xs[r][tt] = v;
+  }
+  __syncthreads();
+  const int r = tid >> 2, cg0 = tid & 3;
+  double acc[MXB_MAXC / 4];
+#pragma unroll
+  for(int u = 0; u < MXB_MAXC / 4; u++) acc[u] = 0.0;
+  for(int tt = 0; tt < nt; tt++) {
+    const double x = Xs[r][tt];
+#pragma unroll
+    for(int u = 0; u < MXB_MAXC / 4; u++)
+      if(cg0 + 4 * u < NC) acc[u] = fma(x, Ys[tt][cg0 + 4 * u], acc[u]);
+  }
+  if(row0 + r < nRows) {
+    double* out = P + ((size_t)split * nRows + row0 + r) * NC;
+#pragma unroll
+    for(int u = 0; u < MXB_MAXC / 4; u++)
+      if(cg0 + 4 * u < NC) out[cg0 + 4 * u] = acc[u];
+  }
+}
+
+// Lower triangle of the global matrix (mirrored), row/column 0 zeroed, and
+// the RHS (nSol entries; bgBase selects the background projection form).
+__global__ void __launch_bounds__(256)
+    k_mx_scatter(const double* __restrict__ P, int nSplit, int nRows, int nMono,
+                 const int2* __restrict__ kp, const int* __restrict__ monoIdx, int monoDim,
+                 int nC1, int nC2, int nBG, int stride, int bgBase, int matSize, int nSol,
+                 double* __restrict__ M, double* __restrict__ rhs) {
+  const int ld = matSize + 1, nComp = nC1 * nC2, NC = nMono + 1;
+  const int nQP = mxPairRow(nC1 + 2, 1), dotRow0 = nQP + 1, bRow0 = nQP + 1 + stride;
+  const long long nTri = (long long)matSize * (matSize + 1) / 2;
+  auto sumP = [&](int xr, int cI) {
+    double v = 0.0;
+    for(int sp = 0; sp < nSplit; sp++) v += P[((size_t)sp * nRows + xr) * NC + cI];
+    return v;
+  };
+  auto mono = [&](int a, int b) { return monoIdx[a * monoDim + b]; };
+  for(long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nTri + nSol + ld;
+      e += (long long)gridDim.x * blockDim.x) {
+    if(e < nTri) {
+      int r = (int)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
+      while((long long)(r + 1) * (r + 2) / 2 <= e) r++;
+      while((long long)r * (r + 1) / 2 > e) r--;
+      const int row = r + 1, col = (int)(e - (long long)r * (r + 1) / 2) + 1;
+      double v;
+      if(row == 1) {
+        v = sumP(nQP, nMono);
+      } else if(row <= nComp + 1) {
+        const int i = row - 2, i1 = i / nC2, i2 = i % nC2;
+        if(col == 1) {
+          v = sumP(mxPairRow(i1 + 2, 1), mono(kp[i2].x, kp[i2].y));
+        } else {
+          const int j = col - 2, j1 = j / nC2, j2 = j % nC2;
+          v = sumP(mxPairRow(i1 + 2, j1 + 2), mono(kp[i2].x + kp[j2].x, kp[i2].y + kp[j2].y));
+        }
+      } else {
+        const int ib = row - (nComp + 2);
+        if(col == 1) {
+          v = sumP(dotRow0 + nC1 * nBG + ib, nMono);
+        } else if(col <= nComp + 1) {
+          const int i1 = (col - 2) / nC2 + 1, i2 = (col - 2) % nC2;
+          v = sumP(dotRow0 + (i1 - 1) * nBG + ib, mono(kp[i2].x, kp[i2].y));
+        } else {
+          const int jb = col - (nComp + 2);
+          v = sumP(dotRow0 + nC1 * nBG + nBG + ib * nBG + jb, nMono);
+        }
+      }
+      M[(size_t)row * ld + col] = v;
+      M[(size_t)col * ld + row] = v;
+    } else if(e < nTri + nSol) {
+      const int id = (int)(e - nTri);
+      double v = 0.0;
+      if(id == 1) {
+        v = sumP(bRow0, mono(0, 0));
+      } else if(id >= 2 && id < nComp + 2) {
+        const int i = (id - 2) / nC2 + 1, j = (id - 2) % nC2;
+        v = sumP(bRow0 + i, mono(kp[j].x, kp[j].y));
+      } else if(id >= nComp + 2 && id < nComp + 2 + nBG) {
+        v = sumP(dotRow0 + bgBase + (id - (nComp + 2)), mono(0, 0));
+      }
+      rhs[id] = v;
+    } else {
+      const int i = (int)(e - nTri - nSol);
+      M[i] = 0.0;
+      M[(size_t)i * ld] = 0.0;
+    }
+  }
+}
+
 }  // namespace
 
 // ============================================================ host side ===
@@ -842,6 +994,54 @@ void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, 
     XB_LAUNCHED(c);
     const size_t smem = (size_t)4 * ld * sizeof(double) + (size_t)ld * sizeof(int);
     k_solve_refine<<<1, 1024, smem, c->stream>>>(F, M, n, piv, rhs, status);
+    XB_LAUNCHED(c);
+  }
+}
+
+// Global matrix and RHS of the mixed path for the stamps list[0..nList) of
+// set si (weights from the current substamps, W dots per stamp).
+void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase, double* M,
+                      double* rhs) {
+  const Geo& g = c->g;
+  StampSetDev& S = c->set[si];
+  const int K = c->p.kernelOrder, monoDim = 2 * K + 1;
+  const int nMono = triNum(2 * K + 1);
+  if(nMono + 1 > MXB_MAXC)
+    throw XbError{XB_ERR_UNSUPPORTED, "kernel order too high for the mixed build"};
+  std::vector<int2> mexp;
+  std::vector<int> midx(monoDim * monoDim, 0);
+  for(int a = 0; a <= 2 * K; a++)
+    for(int b = 0; a + b <= 2 * K; b++) {
+      midx[a * monoDim + b] = (int)mexp.size();
+      mexp.push_back(make_int2(a, b));
+    }
+  std::vector<int2> kp(g.nComp2);
+  for(int k = 0; k < g.nComp2; k++) kp[k] = make_int2(c->basis.kpX[k], c->basis.kpY[k]);
+  int2* dExp = buf<int2>(c, "mx_exp", mexp.size());
+  int* dIdx = buf<int>(c, "mx_idx", midx.size());
+  int2* dKp = buf<int2>(c, "mx_kp", kp.size());
+  toDevice(c, dExp, mexp);
+  toDevice(c, dIdx, midx);
+  toDevice(c, dKp, kp);
+  const int stride = mixedDotStride(g);
+  const int nQP = (g.nComp1 + 1) * (g.nComp1 + 2) / 2 - 1;
+  const int nRows = nQP + 1 + stride + g.nComp1 + 1;
+  const int nSplit = (nList + MXB_T - 1) / MXB_T;
+  double* P = buf<double>(c, "mx_partials", (size_t)std::max(nSplit, 1) * nRows * (nMono + 1));
+  if(nSplit > 0) {
+    KT_SCOPE(c, "mx_build");
+    k_mx_build<<<dim3((nRows + MXB_ROWS - 1) / MXB_ROWS, nSplit), 256, 0, c->stream>>>(
+        dList, nList, S.count, S.cur, S.ssxy, g.maxSS, S.Q, g.qCount, S.dots, stride, S.B, dExp,
+        nMono, c->w, c->h, g.nComp1, nRows, P);
+    XB_LAUNCHED(c);
+  }
+  {
+    KT_SCOPE(c, "mx_scatter");
+    const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
+    const long long total = nTri + g.nSol + g.matSize + 1;
+    k_mx_scatter<<<(int)std::min<long long>((total + 255) / 256, (long long)c->smCount * 4), 256,
+                   0, c->stream>>>(P, nSplit, nRows, nMono, dKp, dIdx, monoDim, g.nComp1,
+                                   g.nComp2, g.nBG, stride, bgBase, g.matSize, g.nSol, M, rhs);
     XB_LAUNCHED(c);
   }
 }
