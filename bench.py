@@ -2,9 +2,9 @@
 """Throughput of the GB300 X-BACH difference-imaging path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--mode plain|mixed]
+                    [--mode mixed|plain] [--cpu-runs R]
 
-Workload: BASELINE configuration 2 - a 2048x2048 FP32 template/science pair
+Workload: a 2048x2048 FP32 template/science pair
 (seeded synthetic field: 20k sources, FWHM varying across the field, 1 %
 cosmic-ray pixels, 40 saturated stars, detector saturation 6e4), 16x16 stamps,
 49 basis functions, spatial kernel order 2, background order 1.  One step is
@@ -42,7 +42,7 @@ sys.path.insert(0, str(REPO / "tests"))
 
 METRIC = "difference-images/s at 2048², chosen vs plain GPU at ≤1e-3σ; % HBM/TC peak"
 UNIT = "difference-images/s"
-WORKLOAD = ("config 2: 2048x2048 FP32 template/science pair, 20k sources, FWHM 2.2-3.2/3.0-4.2 px, "
+WORKLOAD = ("2048x2048 FP32 template/science pair, 20k sources, FWHM 2.2-3.2/3.0-4.2 px, "
             "1% cosmic-ray pixels, 40 saturated stars, saturation 6e4 (threshHigh), 16x16 stamps, "
             "49 basis functions (3 Gaussians, degrees 6/4/2), kernel order 2, background order 1")
 
@@ -126,13 +126,15 @@ def cpu_frames_per_s(T, S, info, runs):
     T64, S64 = T.astype("float64"), S.astype("float64")
     threads = os.cpu_count() or 1
     times = []
+    last = None
     for _ in range(runs):
+        last = None
         t0 = time.perf_counter()
         r = o.run(p, T64, S64, nthreads=threads)
         times.append(time.perf_counter() - t0)
         assert r.status == 0, r.status
-        del r
-    return runs / sum(times), threads, times
+        last = r
+    return runs / sum(times), threads, times, last
 
 
 def run_reference(args):
@@ -143,17 +145,17 @@ def run_reference(args):
     T, S, info = make_pair(2)
     if args.warmup > 0:
         cpu_frames_per_s(T, S, info, args.warmup)
-    fps, threads, times = cpu_frames_per_s(T, S, info, args.steps)
+    fps, threads, times, _ = cpu_frames_per_s(T, S, info, args.steps)
     total = sum(times)
     line = {
         "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded config-2 field)",
+        "data": "synthetic (seeded 2048x2048 crowded field)",
         "config": {"workload": WORKLOAD, "implementation": "FP64 C++ restatement of the reference "
                    "CPU path (the reference needs OpenCL + CCfits, absent here)"},
         "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full config-2 frame pairs, one per step"},
+                         "sample": f"{args.steps} full 2048x2048 frame pairs, one per step"},
         "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -177,13 +179,41 @@ def roofline_for(name, ms_per_launch, n_pix, mode, hbm_peak):
             "algorithmic_bytes_per_launch": traffic_bytes, "ms_per_launch": ms_per_launch}
 
 
+def run_result(xbach, cx):
+    return {"diff": cx.image(xbach.XB_IMG_DIFF), "conv": cx.image(xbach.XB_IMG_CONV),
+            "solution": cx.solution(), "kernSum": cx.scalar("kernSum"),
+            "convTemplate": cx.scalar("convTemplate")}
+
+
+def accuracy(xbach, ctx, pctx, oracle_res, T, S, params):
+    """Chosen vs plain GPU (acceptance: diff within 1e-3 sigma) and both
+    against the FP64 oracle on the same frame pair."""
+    from xbach import accuracy as acc
+    n_comp, n_bg = acc.layout(params)
+    chosen, plain = run_result(xbach, ctx), run_result(xbach, pctx)
+    out = {"chosen_vs_plain": acc.compare(chosen, plain, T, S, n_comp, n_bg),
+           "sigma_definition": "sqrt(|target| + |conv| + 2*5^2) ADU, gain 1"}
+    if oracle_res is not None:
+        ref = {"diff": oracle_res.image("diff"), "conv": oracle_res.image("conv"),
+               "solution": oracle_res.array("solution", "float64"),
+               "kernSum": oracle_res.scalar("kernSum"),
+               "convTemplate": oracle_res.scalar("convTemplate")}
+        out["chosen_vs_fp64_oracle"] = acc.compare(chosen, ref, T, S, n_comp, n_bg)
+        out["plain_vs_fp64_oracle"] = acc.compare(plain, ref, T, S, n_comp, n_bg)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"],
+                    help="mixed = the chosen pipeline (headline); plain = the FP64 path alone")
+    ap.add_argument("--batch", type=int, default=8,
+                    help="frame pairs per step, run concurrently (1 = one pair per step)")
+    ap.add_argument("--workers", type=int, default=8, help="concurrent frames of a batch")
     ap.add_argument("--cpu-runs", type=int, default=2)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -205,46 +235,63 @@ def main():
     import xbach
     from xbach.synth import make_pair
 
-    T, S, info = make_pair(2, frame=rank)
+    B = max(1, args.batch)
+    frames = [make_pair(2, frame=rank * B + i) for i in range(B)]
+    T, S, info = frames[0]
     h, w = T.shape
     n_pix = w * h
     mode = xbach.XB_MODE_PLAIN if args.mode == "plain" else xbach.XB_MODE_MIXED
-    ctx = xbach.Context(frame_params(xbach, info, mode), device=local)
-    dT = torch.from_numpy(T).cuda()
-    dS = torch.from_numpy(S).cuda()
+    params = frame_params(xbach, info, mode)
+    dT = [torch.from_numpy(f[0]).cuda() for f in frames]
+    dS = [torch.from_numpy(f[1]).cuda() for f in frames]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.ExternalStream(ctx.stream())
 
-    def pipeline():
-        ctx.init_device(dT.data_ptr(), dS.data_ptr(), w, h)
-        ctx.sss()
-        ctx.cmv()
-        ctx.cd()
-        ctx.ksc()
-        ctx.conv()
-        ctx.sub()
+    def make_pipeline(cx, i=0):
+        def pipeline():
+            cx.init_device(dT[i].data_ptr(), dS[i].data_ptr(), w, h)
+            cx.sss()
+            cx.cmv()
+            cx.cd()
+            cx.ksc()
+            cx.conv()
+            cx.sub()
+        return pipeline
 
-    for _ in range(args.warmup):
-        pipeline()
-    torch.cuda.synchronize()
-    ctx.set_option("time_kernels", 1)
-    launches0 = ctx.launches()
-    total_ms = 0.0
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+    def timed(run, st, steps):
+        ms = 0.0
+        for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             if world > 1:
                 dist.barrier()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            pipeline()
-            e1.record(stream)
+            e0.record(st)
+            run()
+            e1.record(st)
             e1.synchronize()
-            total_ms += e0.elapsed_time(e1)
+            ms += e0.elapsed_time(e1)
         torch.cuda.synchronize()
-    launches = ctx.launches() - launches0
+        return ms
+
+    def max_over_ranks(ms):
+        if world == 1:
+            return ms
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- one frame pair per step: per-kernel breakdown ----
+    ctx = xbach.Context(params, device=local)
+    cst = torch.cuda.ExternalStream(ctx.stream())
+    single = make_pipeline(ctx)
+    for _ in range(args.warmup):
+        single()
+    torch.cuda.synchronize()
+    ctx.set_option("time_kernels", 1)
+    launches_single0 = ctx.launches()
+    single_ms = max_over_ranks(timed(single, cst, args.steps))
+    launches_single = ctx.launches() - launches_single0
     kernels = {}
     for name in ("mask_input", "spread_mask", "stamp_stats", "find_substamps", "compact_stamps",
                  "fill_w", "fill_finish", "gram_qb", "stamp_test_fit", "cd_select", "weights",
@@ -255,47 +302,60 @@ def main():
         if n:
             kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}
     ctx.set_option("time_kernels", 0)
-    clocks = clk.summary()
-    t_max = total_ms
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * args.steps / (t_max / 1000.0)
+    single_value = world * args.steps / (single_ms / 1000.0)
 
-    # ---- end to end through xb_run with pinned host buffers ----
-    hT = torch.from_numpy(T).pin_memory()
-    hS = torch.from_numpy(S).pin_memory()
-    hC = torch.empty((h, w), dtype=torch.float32).pin_memory()
-    hD = torch.empty((h, w), dtype=torch.float32).pin_memory()
-    L = xbach.lib()
+    # ---- the headline: B frame pairs per step through the batch API ----
+    jst = torch.cuda.Stream()
+    if B > 1:
+        batch = xbach.Batch(params, device=local, workers=max(1, min(args.workers, B)))
+        batch.set_stream(jst.cuda_stream)
+        dC = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
+        dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
 
-    def run_e2e():
-        rc = L.xb_run(ctx.h, ctypes.c_void_p(hT.data_ptr()), ctypes.c_void_p(hS.data_ptr()), w, h,
-                      ctypes.c_void_p(hC.data_ptr()), ctypes.c_void_p(hD.data_ptr()))
-        if rc:
-            raise RuntimeError(L.xb_last_error(ctx.h).decode())
+        def run_batch():
+            batch.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], [w] * B,
+                           [h] * B, [t.data_ptr() for t in dC], [t.data_ptr() for t in dD],
+                           device=True)
 
-    run_e2e()
-    e2e_ms = 0.0
-    for _ in range(args.steps):
-        flush.zero_()
+        for _ in range(args.warmup):
+            run_batch()
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        run_e2e()
-        e1.record(stream)
-        e1.synchronize()
-        e2e_ms += e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
-           "h2d_bytes_per_step": 2 * 4 * n_pix, "d2h_bytes_per_step": 2 * 4 * n_pix}
+        workers = [batch.worker(i) for i in range(batch.n_workers)]
+        l0 = sum(wk.launches() for wk in workers)
+        with ClockSampler(local) as clk:
+            t_max = max_over_ranks(timed(run_batch, jst, args.steps))
+        launches = sum(wk.launches() for wk in workers) - l0
+        clocks = clk.summary()
+    else:
+        with ClockSampler(local) as clk:
+            t_max = max_over_ranks(timed(single, cst, args.steps))
+        launches = launches_single
+        clocks = clk.summary()
+    value = world * B * args.steps / (t_max / 1000.0)
+
+    # ---- end to end: host frames (pinned) in, host images out ----
+    hT = [torch.from_numpy(f[0]).pin_memory() for f in frames]
+    hS = [torch.from_numpy(f[1]).pin_memory() for f in frames]
+    hC = [torch.empty((h, w), dtype=torch.float32).pin_memory() for _ in range(B)]
+    hD = [torch.empty((h, w), dtype=torch.float32).pin_memory() for _ in range(B)]
+    if B > 1:
+        def run_e2e():
+            batch.run_ptrs([t.data_ptr() for t in hT], [t.data_ptr() for t in hS], [w] * B,
+                           [h] * B, [t.data_ptr() for t in hC], [t.data_ptr() for t in hD])
+        est = jst
+    else:
+        L = xbach.lib()
+
+        def run_e2e():
+            rc = L.xb_run(ctx.h, ctypes.c_void_p(hT[0].data_ptr()), ctypes.c_void_p(hS[0].data_ptr()),
+                          w, h, ctypes.c_void_p(hC[0].data_ptr()), ctypes.c_void_p(hD[0].data_ptr()))
+            if rc:
+                raise RuntimeError(L.xb_last_error(ctx.h).decode())
+        est = cst
+    run_e2e()
+    e2e_ms = max_over_ranks(timed(run_e2e, est, args.steps))
+    e2e = {"value": world * B * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+           "h2d_bytes_per_step": B * 2 * 4 * n_pix, "d2h_bytes_per_step": B * 2 * 4 * n_pix}
 
     if rank != 0:
         if world > 1:
@@ -314,17 +374,38 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.mode == "plain" else "f32",
-        "data": "synthetic (seeded config-2 field)",
-        "config": {"workload": WORKLOAD, "mode": args.mode, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every step (256 MB write)",
+        "data": "synthetic (seeded 2048x2048 crowded fields, one seed per frame pair)",
+        "config": {"workload": WORKLOAD, "mode": args.mode,
+                   "frames_per_step": B, "concurrent_frames": min(args.workers, B) if B > 1 else 1,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every step (256 MB write); each step's inputs exceed L2",
                    "inputs": "device-resident FP32 T,S"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+        "single_frame": {"value": single_value, "unit": UNIT,
+                         "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single},
         "dominant_kernel": dominant, "kernels": kernels,
     }
+    oracle_res = None
     if world == 1 and args.cpu_runs > 0:
-        fps, threads, _ = cpu_frames_per_s(T, S, info, args.cpu_runs)
+        fps, threads, _, oracle_res = cpu_frames_per_s(T, S, info, args.cpu_runs)
         line["cpu_baseline"] = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{args.cpu_runs} full config-2 frame pairs"}
+                                "sample": f"{args.cpu_runs} full 2048x2048 frame pairs"}
+    if args.mode == "mixed":
+        # the plain FP64 GPU pipeline, one pair per step: the denominator of the
+        # chosen-vs-plain ratio, and the acceptance reference
+        pctx = xbach.Context(frame_params(xbach, info, xbach.XB_MODE_PLAIN), device=local)
+        make_pipeline(pctx)()
+        p_steps = max(1, min(args.steps, 3))
+        p_ms = timed(make_pipeline(pctx), torch.cuda.ExternalStream(pctx.stream()), p_steps)
+        line["plain_gpu"] = {"value": p_steps / (p_ms / 1000.0), "unit": UNIT,
+                             "ms_per_step": p_ms / p_steps, "steps": p_steps}
+        line["chosen_over_plain"] = value / line["plain_gpu"]["value"]
+        make_pipeline(ctx)()
+        torch.cuda.synchronize()
+        line["accuracy"] = accuracy(xbach, ctx, pctx, oracle_res, T, S, params)
+        if B > 1:
+            same = bool(torch.equal(dD[0].cpu(), torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))))
+            line["accuracy"]["batch_frame0_equals_single"] = same
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

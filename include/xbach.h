@@ -213,6 +213,39 @@ int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w, int h,
                            double* dFwhm, void* stream, char* err,
                            size_t errCap);
 
+/* ---- batches of frame pairs ---------------------------------------------- */
+/* No counterpart in the reference, whose main (src/main.cpp) runs one pair
+ * per process.  A batch owns nWorkers contexts, each with its own stream and
+ * host thread; the frames of a run are taken from one queue in order and run
+ * through the whole stage sequence (init .. sub) concurrently on the GPU.
+ * Frames may differ in size.  Results are per frame and identical to xb_run
+ * on a single context. */
+typedef struct xb_batch xb_batch;
+int xb_batch_create(const xb_params* p, int device, int nWorkers, xb_batch** out);
+int xb_batch_destroy(xb_batch* b);
+const char* xb_batch_last_error(const xb_batch* b);
+/* Host frames: T[i], S[i] are w[i] x h[i] FP32 arrays (pinned memory makes
+ * the uploads asynchronous); conv[i], diff[i] receive the outputs (either
+ * may be NULL).  frameStatus[i] and kernSum[i] (each may be NULL) receive
+ * each frame's status and kernel sum.  Returns XB_OK when every frame
+ * succeeded, else the status of the first failing frame (its message in
+ * xb_batch_last_error). */
+int xb_batch_run(xb_batch* b, int nFrames, const float* const* T, const float* const* S,
+                 const int* w, const int* h, float* const* conv, float* const* diff,
+                 int* frameStatus, double* kernSum);
+/* Device frames: the same with device pointers for inputs and outputs. */
+int xb_batch_run_device(xb_batch* b, int nFrames, const float* const* dT,
+                        const float* const* dS, const int* w, const int* h,
+                        float* const* dConv, float* const* dDiff, int* frameStatus,
+                        double* kernSum);
+/* Worker context i (options such as "time_kernels", timers, launch counts). */
+int xb_batch_worker(xb_batch* b, int i, xb_ctx** ctx);
+/* Joins a caller's cudaStream_t to every later run: the workers' first
+ * launches wait for the work already queued on `stream`, and work queued on
+ * `stream` after the run waits for every worker, so CUDA events recorded on
+ * `stream` before and after a run bracket all of its GPU work.  NULL detaches. */
+int xb_batch_set_stream(xb_batch* b, void* stream);
+
 /* ---- FITS I/O (src/fitsUtil.cpp:8-64 without CCfits) -------------------- */
 /* Reads the primary HDU (BITPIX -32 or -64) into a newly malloc'ed FP64
  * array (free with xb_free).  Returns XB_ERR_IO / XB_ERR_UNSUPPORTED. */

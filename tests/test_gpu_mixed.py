@@ -1,6 +1,6 @@
 """The mixed-precision (chosen) path against the plain path and the oracle.
 
-Acceptance (BASELINE metric): the chosen difference image is within 1e-3 of
+Acceptance (the throughput metric's accuracy condition): the chosen difference image is within 1e-3 of
 the per-pixel noise sigma of the plain GPU result,
 sigma_pix = sqrt(|S| + |conv| + 2 sigma_rn^2) with the frames' read noise
 sigma_rn = 5 ADU (gain 1), over pixels both paths leave unmasked.
@@ -48,8 +48,8 @@ def test_same_stamp_sets_and_direction(both):
 # test01 (the reference's 330x330 golden case) has a global system with
 # cond ~6e13 and a negative kernel sum; there even rounding the plain path's
 # own FP64 W to FP32 moves the difference image by 1.2e-3 sigma, so FP32
-# storage of W cannot meet 1e-3 sigma on it.  The BASELINE workloads
-# (configs 1 and 2) are held to the metric's 1e-3 sigma.
+# storage of W cannot meet 1e-3 sigma on it.  The synthetic 512^2 and 2048^2
+# field presets 1 and 2 are held to the metric's 1e-3 sigma.
 SIGMA_BAR = {"test01": 1e-2, "config1": 1e-3, "config2": 1e-3}
 KSUM_BAR = {"test01": 1e-4, "config1": 1e-5, "config2": 1e-5}
 

@@ -57,7 +57,9 @@ EXPORTS = [
     "xb_sub", "xb_run", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
     "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
-    "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc",
+    "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc", "xb_batch_create",
+    "xb_batch_destroy", "xb_batch_last_error", "xb_batch_run", "xb_batch_run_device",
+    "xb_batch_worker", "xb_batch_set_stream",
 ]
 
 
@@ -100,6 +102,15 @@ def lib():
     L.xb_fits_read.argtypes = [ctypes.c_char_p, P(vp), P(i), P(i)]
     L.xb_fits_write.argtypes = [ctypes.c_char_p, vp, i, i]
     L.xb_free.argtypes = [vp]
+    L.xb_batch_create.argtypes = [P(XbParams), i, i, P(vp)]
+    L.xb_batch_destroy.argtypes = [vp]
+    L.xb_batch_last_error.argtypes = [vp]
+    L.xb_batch_last_error.restype = ctypes.c_char_p
+    L.xb_batch_run.argtypes = [vp, i, P(vp), P(vp), P(i), P(i), P(vp), P(vp), P(i), P(d)]
+    L.xb_batch_run_device.argtypes = [vp, i, P(vp), P(vp), P(i), P(i), P(vp), P(vp), P(i),
+                                      P(d)]
+    L.xb_batch_worker.argtypes = [vp, i, P(vp)]
+    L.xb_batch_set_stream.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -253,3 +264,88 @@ class Context:
     @property
     def hgt(self):
         return int(self.scalar("h"))
+
+
+class _Borrowed(Context):
+    """A worker context owned by a Batch (not destroyed here)."""
+
+    def __init__(self, handle, params):
+        self.L = lib()
+        self.params = params
+        self.h = handle
+
+    def close(self):
+        self.h = None
+
+    __del__ = close
+
+
+class Batch:
+    """Independent frame pairs run concurrently by `workers` contexts, each
+    on its own stream and host thread (an `xb_batch`)."""
+
+    def __init__(self, params=None, device=0, workers=8):
+        self.L = lib()
+        self.params = params if params is not None else default_params()
+        h = ctypes.c_void_p()
+        rc = self.L.xb_batch_create(ctypes.byref(self.params), device, workers, ctypes.byref(h))
+        if rc != 0:
+            raise XbError(rc, "xb_batch_create failed")
+        self.h = h
+        self.n_workers = workers
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.xb_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_stream(self, stream):
+        """Join a cudaStream_t handle (int) to later runs (0 detaches)."""
+        if self.L.xb_batch_set_stream(self.h, ctypes.c_void_p(stream or None)):
+            raise XbError(5, "xb_batch_set_stream failed")
+
+    def worker(self, i):
+        c = ctypes.c_void_p()
+        if self.L.xb_batch_worker(self.h, i, ctypes.byref(c)):
+            raise IndexError(i)
+        return _Borrowed(c, self.params)
+
+    @staticmethod
+    def _ptrs(vals):
+        return (ctypes.c_void_p * max(len(vals), 1))(*[ctypes.c_void_p(v) for v in vals])
+
+    def _finish(self, rc, n, st, ks):
+        if rc != 0:
+            raise XbError(rc, self.L.xb_batch_last_error(self.h).decode())
+        return [int(st[i]) for i in range(n)], [float(ks[i]) for i in range(n)]
+
+    def run(self, Ts, Ss, convs=None, diffs=None):
+        """Host frames: lists of FP32 numpy arrays (outputs: preallocated FP32
+        arrays or None).  Returns (statuses, kernel sums)."""
+        n = len(Ts)
+        Ts = [np.ascontiguousarray(t, dtype=np.float32) for t in Ts]
+        Ss = [np.ascontiguousarray(s, dtype=np.float32) for s in Ss]
+        w = (ctypes.c_int * max(n, 1))(*[t.shape[1] for t in Ts])
+        h = (ctypes.c_int * max(n, 1))(*[t.shape[0] for t in Ts])
+        cv = self._ptrs([c.ctypes.data for c in convs]) if convs is not None else None
+        df = self._ptrs([d.ctypes.data for d in diffs]) if diffs is not None else None
+        st = (ctypes.c_int * max(n, 1))()
+        ks = (ctypes.c_double * max(n, 1))()
+        rc = self.L.xb_batch_run(self.h, n, self._ptrs([t.ctypes.data for t in Ts]),
+                                 self._ptrs([s.ctypes.data for s in Ss]), w, h, cv, df, st, ks)
+        return self._finish(rc, n, st, ks)
+
+    def run_ptrs(self, T_ptrs, S_ptrs, ws, hs, conv_ptrs=None, diff_ptrs=None, device=False):
+        """Frames given as raw pointers (host or, with device=True, device)."""
+        n = len(T_ptrs)
+        w = (ctypes.c_int * max(n, 1))(*ws)
+        h = (ctypes.c_int * max(n, 1))(*hs)
+        cv = self._ptrs(conv_ptrs) if conv_ptrs is not None else None
+        df = self._ptrs(diff_ptrs) if diff_ptrs is not None else None
+        st = (ctypes.c_int * max(n, 1))()
+        ks = (ctypes.c_double * max(n, 1))()
+        f = self.L.xb_batch_run_device if device else self.L.xb_batch_run
+        rc = f(self.h, n, self._ptrs(T_ptrs), self._ptrs(S_ptrs), w, h, cv, df, st, ks)
+        return self._finish(rc, n, st, ks)

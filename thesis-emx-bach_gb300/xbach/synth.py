@@ -46,7 +46,7 @@ def _render(img, xs, ys, fluxes, sigmas):
 
 
 def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over):
-    """Returns (template, science, info) for BASELINE configuration `config`.
+    """Returns (template, science, info) for field preset `config` (see CONFIGS).
 
     frame: index of the pair within a batch (changes the seed).
     """
