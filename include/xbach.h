@@ -68,8 +68,12 @@ extern "C" {
  * quantity that feeds a stamp / substamp / rejection decision is computed in
  * the reference's operation order, so the decision sets are bit-identical to
  * the CPU oracle.
- * XB_MODE_MIXED: FP32 basis convolutions, 3xTF32 tensor-core Gram matrices,
- * FP64 LU + one iterative-refinement step, FP32 full-frame convolution. */
+ * XB_MODE_MIXED: FP32 basis convolutions and W; per-stamp Gram matrices on the
+ * tensor cores from exact fixed-point BF16 slices of W (FP64-accurate); the
+ * global system by FP64 LDL^T (pivoted LU if a pivot fails) plus one FP64
+ * iterative-refinement step; FP32 full-frame convolution.  Decision sets
+ * match the plain mode; the difference image stays within 1e-3 of the
+ * per-pixel noise of the plain result on the synthetic workloads. */
 #define XB_MODE_PLAIN 0
 #define XB_MODE_MIXED 1
 
@@ -120,7 +124,10 @@ const char* xb_last_error(const xb_ctx* ctx);
  * results of every stage for xb_get_array (parity checks; costs copies).
  * "time_kernels" (0/1): time the main kernels with CUDA events on the
  * context stream; xb_get_scalar("kt:<kernel>:ms" / "kt:<kernel>:n") returns
- * the accumulated milliseconds / launch count (setting it resets them). */
+ * the accumulated milliseconds / launch count (setting it resets them).
+ * "gram_fp64" (0/1, mixed mode): compute the per-stamp Gram matrices with
+ * FP64 accumulation on the CUDA cores instead of the exact tensor-core
+ * slicing (a cross-check; the results agree to rounding). */
 int xb_set_option(xb_ctx* ctx, const char* name, long long value);
 
 /* ---- stage API (include/bach.h:66-87) ------------------------------------ */

@@ -75,3 +75,27 @@ def test_diff_within_1e3_sigma_of_plain(both):
     # masks agree except where the FP32 good-fraction test sits on 0.99
     mp, mm = plain.array("mask", np.uint16), mixed.array("mask", np.uint16)
     assert np.mean(mp != mm) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["test01", "config1"])
+def test_tensor_core_gram_matches_fp64_gram(name, test01):
+    """Q and B from the tensor-core slicing agree with the FP64 CUDA-core
+    accumulation of the same FP32 W.  The slicing rounds every element to
+    2^-36 of its row maximum (the only approximation; the slice products are
+    exact), which moves a Gram entry by ~1e-11 of the largest entry --
+    three orders below the FP32 storage of W itself."""
+    import xbach
+    T, S, kw = case(name, test01)
+    out = {}
+    for fp64 in (0, 1):
+        ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED, **kw), trace=True)
+        ctx.set_option("gram_fp64", fp64)
+        ctx.init(T, S)
+        ctx.sss()
+        ctx.cmv()
+        out[fp64] = {k: ctx.array(k, np.float64) for k in ("Q0", "Q1", "B0", "B1")}
+    for k in ("Q0", "Q1", "B0", "B1"):
+        a, b = out[0][k], out[1][k]
+        scale = np.max(np.abs(b))
+        assert scale > 0
+        assert np.max(np.abs(a - b)) <= 1e-10 * scale, (k, np.max(np.abs(a - b)) / scale)

@@ -177,6 +177,8 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
   } else if(n == "time_kernels") {
     c->timeKernels = value != 0;
     c->kt.total.clear();
+  } else if(n == "gram_fp64") {
+    c->gramFp64 = value != 0;
   } else {
     return XB_ERR_ARG;
   }

@@ -152,6 +152,7 @@ struct xb_ctx {
   long long launches = 0;
   int trace = 0;
   int timeKernels = 0;
+  int gramFp64 = 0;  // mixed mode: FP64 CUDA-core Gram instead of the tensor cores (checks)
   xb::KTimers kt;
   std::string lastError;
   std::map<std::string, std::vector<uint8_t>> arrays;
@@ -266,9 +267,16 @@ void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase
 // global system of the mixed path (xb_ldl.cu): LDL^T on a cluster, refined
 // solve, pivoted LU when a pivot fails.  M is kept; rhs becomes the solution.
 void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, int* singular);
-// Throws XB_ERR_DEVICE_TIMEOUT when a bounded wait of the cluster solve ran
-// out since the last call (synchronises the stream).
+// Device status words of the mixed path: [0] bit 0 = an LDL^T pivot failed
+// (per solve), [1] bit 0 = a bounded device-side wait ran out (sticky until
+// checkSolveTimeout reports it).  Zeroed when first allocated.
+int* deviceStatus(xb_ctx* c);
+// Throws XB_ERR_DEVICE_TIMEOUT when a bounded wait of the cluster solve or
+// the tensor-core Gram ran out since the last call (synchronises the stream).
 void checkSolveTimeout(xb_ctx* c);
+// Tensor-core Gram of the mixed path (xb_gram_tc.cu) into G (nList x R x R);
+// false when the shape is outside its limits.
+bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G);
 inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
 
 // Kernel image at normalised position (xf, yf) and its sum into *dOut

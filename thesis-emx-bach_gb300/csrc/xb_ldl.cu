@@ -543,12 +543,17 @@ cudaError_t launchCluster(xb_ctx* c, Kern kernel, int CL, int threads, size_t sm
 
 }  // namespace
 
-void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, int* singular) {
-  const int ld = n + 1;
+int* deviceStatus(xb_ctx* c) {
   const bool fresh = c->pool.find("ldl_status") == c->pool.end();
   int* status = buf<int>(c, "ldl_status", 2);
   if(fresh) XB_CUDA(cudaMemsetAsync(status, 0, 2 * sizeof(int), c->stream));
-  else XB_CUDA(cudaMemsetAsync(status, 0, sizeof(int), c->stream));
+  return status;
+}
+
+void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, int* singular) {
+  const int ld = n + 1;
+  int* status = deviceStatus(c);
+  XB_CUDA(cudaMemsetAsync(status, 0, sizeof(int), c->stream));
   double* F = buf<double>(c, "ldl_F", (size_t)ld * ld);
   double* rinv = buf<double>(c, "ldl_rinv", ld);
   // 16-CTA clusters where the device allows them, else 8
@@ -595,7 +600,7 @@ void checkSolveTimeout(xb_ctx* c) {
   XB_CUDA(cudaStreamSynchronize(c->stream));
   if(st[1]) {
     XB_CUDA(cudaMemsetAsync((int*)it->second.p + 1, 0, sizeof(int), c->stream));
-    throw XbError{XB_ERR_DEVICE_TIMEOUT, "cluster solve: a bounded wait ran out of time"};
+    throw XbError{XB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out of time"};
   }
 }
 

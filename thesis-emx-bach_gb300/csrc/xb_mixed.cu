@@ -913,7 +913,9 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
       throw XbError{XB_ERR_UNSUPPORTED, "too many basis functions for the Gram kernel"};
     double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
     dim3 grid(nList, GM_SPLIT);
-    if(c->imgIsF64)
+    if(gramTensorCores(c, si, dList, nList, other, G)) {
+      // exact tensor-core Gram (xb_gram_tc.cu)
+    } else if(c->imgIsF64)
       k_gram_mixed<double><<<grid, MX_THREADS, smem, c->stream>>>(
           (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
           g.wRows, ldW, S.Wf, G);
