@@ -195,19 +195,28 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
 #pragma unroll
       for(int sl = 0; sl < GT_S; sl++) q[sl][0] = q[sl][1] = q[sl][2] = q[sl][3] = 0u;
       if(r < R) {
-        const double scale = __longlong_as_double((long long)(1023 + 35 - expo[r]) << 52);
+        const int er = expo[r];
 #pragma unroll
         for(int e = 0; e < 8; e++) {
           const int k = k0 + e;
           float x = 0.f;
           if(k < K) x = r < wRows ? Ws[(size_t)r * ldW + k] : imgRow[k];
-          // |x| <= 2^e (1 - 2^-24), so |z| <= 2^35 - 2^11: five digits suffice
-          const long long z = __double2ll_rn((double)x * scale);
-          const unsigned long long mag = (unsigned long long)(z < 0 ? -z : z);
+          // |Z| = round(|x| 2^(35 - e_r)) from the float's fields, in integers:
+          // x = m 2^(ex - 150) (m with its hidden bit), so Z = m 2^sh.  As
+          // |x| <= 2^e_r (1 - 2^-24), |Z| <= 2^35 - 2^11: five digits suffice.
+          const uint32_t xb = __float_as_uint(x);
+          const int ex = (int)((xb >> 23) & 0xFFu);
+          const uint32_t m = (xb & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
+          const int sh = (ex ? ex : 1) - 150 + 35 - er;
+          unsigned long long mag;
+          if(sh >= 0) mag = (unsigned long long)m << sh;
+          else if(sh > -40) mag = ((unsigned long long)m + (1ull << (-sh - 1))) >> (-sh);
+          else mag = 0;
+          const bool neg = (xb >> 31) != 0;
 #pragma unroll
           for(int sl = 0; sl < GT_S; sl++) {
             const int dgt = (int)((mag >> (7 * (GT_S - 1 - sl))) & 127u);
-            const __nv_bfloat16 hb = __float2bfloat16_rn((float)(z < 0 ? -dgt : dgt));
+            const __nv_bfloat16 hb = __float2bfloat16_rn((float)(neg ? -dgt : dgt));
             const uint32_t bits = (uint32_t)__bfloat16_as_ushort(hb);
             q[sl][e >> 1] |= bits << ((e & 1) * 16);
           }
