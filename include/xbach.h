@@ -125,6 +125,11 @@ const char* xb_last_error(const xb_ctx* ctx);
  * "time_kernels" (0/1): time the main kernels with CUDA events on the
  * context stream; xb_get_scalar("kt:<kernel>:ms" / "kt:<kernel>:n") returns
  * the accumulated milliseconds / launch count (setting it resets them).
+ * "rank" (0/1/2): reorder every stamp's substamps by the learned ranker
+ * after sss (needs xb_ranker_set): 1 moves the candidates whose accept
+ * probability is below "rank_tau" (thousandths, default 500) behind the
+ * others, keeping the reference's order within each group; 2 sorts all by
+ * score.
  * "gram_fp64" (0/1, mixed mode): compute the per-stamp Gram matrices with
  * FP64 accumulation on the CUDA cores instead of the exact tensor-core
  * slicing (a cross-check; the results agree to rounding). */
@@ -252,6 +257,35 @@ int xb_batch_worker(xb_batch* b, int i, xb_ctx** ctx);
  * `stream` after the run waits for every worker, so CUDA events recorded on
  * `stream` before and after a run bracket all of its GPU work.  NULL detaches. */
 int xb_batch_set_stream(xb_batch* b, void* stream);
+
+/* ---- learned substamp ranking -------------------------------------------- */
+/* No counterpart in the reference.  A small network (a 3-layer CNN over the
+ * 2x31x31 template/science window pair plus an MLP over 16 window
+ * statistics, 2161 FP32 parameters) scores every candidate substamp; with
+ * option "rank" on and weights loaded, xb_sss reorders each stamp's
+ * candidates by descending score, so the ones the ksc fit would reject are
+ * tried last.  The ksc sigma-clip check still judges every pick. */
+int xb_ranker_param_count(void);
+/* Loads the network's parameters (host array of xb_ranker_param_count()). */
+int xb_ranker_set(xb_ctx* ctx, const float* weights, int n);
+/* Features of every candidate substamp of stamp set `set` (0: stamps found on
+ * the template, 1: on the science) after xb_sss: stats (n x 16), pix
+ * (n x 2 x 31 x 31), and each candidate's stamp index and slot.  With all
+ * four arrays NULL only *nOut is set.  cap is the capacity in candidates. */
+int xb_ranker_features(xb_ctx* ctx, int set, float* stats, float* pix, int* stamp, int* slot,
+                       int cap, int* nOut);
+/* Training and inference kernels on device arrays (stream: cudaStream_t).
+ * forward: logits of n candidates.  grad: per-sample gradients of the
+ * weighted binary cross-entropy (dGradPerSample: n x param_count scratch),
+ * their batch mean in dGrad, per-sample losses in dLoss; dWeight may be
+ * NULL.  adam: one Adam step (b1 0.9, b2 0.999, eps 1e-8; step >= 1). */
+int xb_ranker_forward(const float* dW, const float* dStats, const float* dPix, int n,
+                      float* dLogit, void* stream);
+int xb_ranker_grad(const float* dW, const float* dStats, const float* dPix, const float* dLabel,
+                   const float* dWeight, int n, float* dGradPerSample, float* dGrad,
+                   float* dLoss, void* stream);
+int xb_ranker_adam(float* dW, const float* dGrad, float* dM, float* dV, int step, float lr,
+                   void* stream);
 
 /* ---- FITS I/O (src/fitsUtil.cpp:8-64 without CCfits) -------------------- */
 /* Reads the primary HDU (BITPIX -32 or -64) into a newly malloc'ed FP64

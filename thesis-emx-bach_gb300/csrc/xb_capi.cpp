@@ -179,6 +179,12 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->kt.total.clear();
   } else if(n == "gram_fp64") {
     c->gramFp64 = value != 0;
+  } else if(n == "rank") {
+    if(value < 0 || value > 2) return XB_ERR_ARG;
+    c->rank = (int)value;
+  } else if(n == "rank_tau") {
+    if(value <= 0 || value >= 1000) return XB_ERR_ARG;
+    c->rankTau = (int)value;
   } else {
     return XB_ERR_ARG;
   }

@@ -153,6 +153,9 @@ struct xb_ctx {
   int trace = 0;
   int timeKernels = 0;
   int gramFp64 = 0;  // mixed mode: FP64 CUDA-core Gram instead of the tensor cores (checks)
+  int rank = 0;          // learned substamp order after sss: 1 demote, 2 sort
+  int rankTau = 500;     // demotion threshold of the accept probability, 1/1000
+  float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
   xb::KTimers kt;
   std::string lastError;
   std::map<std::string, std::vector<uint8_t>> arrays;
@@ -274,6 +277,8 @@ int* deviceStatus(xb_ctx* c);
 // Throws XB_ERR_DEVICE_TIMEOUT when a bounded wait of the cluster solve or
 // the tensor-core Gram ran out since the last call (synchronises the stream).
 void checkSolveTimeout(xb_ctx* c);
+// Learned substamp ranking (xb_ranker.cu): reorder both sets' substamps.
+void rankSubstamps(xb_ctx* c);
 // Tensor-core Gram of the mixed path (xb_gram_tc.cu) into G (nList x R x R);
 // false when the shape is outside its limits.
 bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G);

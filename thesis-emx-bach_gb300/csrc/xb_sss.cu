@@ -802,6 +802,7 @@ void stageSss(xb_ctx* c) {
     S.h_count = toHost(c, S.count, S.n);
     S.h_cur.assign(S.n, 0);
   }
+  if(c->rank && c->rankW) rankSubstamps(c);  // learned order of each stamp's substamps
   if(c->trace) {
     for(int im = 0; im < 2; im++) {
       const std::string sfx = std::to_string(im);

@@ -59,7 +59,8 @@ EXPORTS = [
     "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
     "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc", "xb_batch_create",
     "xb_batch_destroy", "xb_batch_last_error", "xb_batch_run", "xb_batch_run_device",
-    "xb_batch_worker", "xb_batch_set_stream",
+    "xb_batch_worker", "xb_batch_set_stream", "xb_ranker_param_count", "xb_ranker_set",
+    "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
 ]
 
 
@@ -111,6 +112,12 @@ def lib():
                                       P(d)]
     L.xb_batch_worker.argtypes = [vp, i, P(vp)]
     L.xb_batch_set_stream.argtypes = [vp, vp]
+    L.xb_ranker_param_count.argtypes = []
+    L.xb_ranker_set.argtypes = [vp, vp, i]
+    L.xb_ranker_features.argtypes = [vp, i, vp, vp, vp, vp, i, P(i)]
+    L.xb_ranker_forward.argtypes = [vp, vp, vp, i, vp, vp]
+    L.xb_ranker_grad.argtypes = [vp, vp, vp, vp, vp, i, vp, vp, vp, vp]
+    L.xb_ranker_adam.argtypes = [vp, vp, vp, vp, i, ctypes.c_float, vp]
     _lib = L
     return L
 
