@@ -125,6 +125,12 @@ const char* xb_last_error(const xb_ctx* ctx);
  * "time_kernels" (0/1): time the main kernels with CUDA events on the
  * context stream; xb_get_scalar("kt:<kernel>:ms" / "kt:<kernel>:n") returns
  * the accumulated milliseconds / launch count (setting it resets them).
+ * "autotune" (0/1, default 1): the first launch of a tunable kernel for a
+ * frame shape times its tile-shape variants (identical results) and keeps
+ * the fastest for the process (XB_TUNE_CACHE=<file> persists the choices);
+ * xb_get_scalar("tune:<kernel>") reports the choice.  0 uses the defaults.
+ * "tune_variant" (-1 default): launch variant k of every tunable kernel
+ * (checks that the variants agree).
  * "rank" (0/1/2): reorder every stamp's substamps by the learned ranker
  * after sss (needs xb_ranker_set): 1 moves the candidates whose accept
  * probability is below "rank_tau" (thousandths, default 500) behind the

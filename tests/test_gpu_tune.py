@@ -1,0 +1,28 @@
+"""The autotuner: every tile-shape variant of a tunable kernel gives the same
+images, and the tuner records the variant it chose."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_conv_variants_identical_and_choice_recorded():
+    import xbach
+    from xbach.synth import make_pair
+    T, S, info = make_pair(1)
+    kw = dict(stampsx=info["stamps"], stampsy=info["stamps"], threshHigh=info["threshHigh"],
+              mode=xbach.XB_MODE_MIXED)
+    images = []
+    for v in range(3):
+        ctx = xbach.Context(xbach.default_params(**kw))
+        ctx.set_option("tune_variant", v)
+        ctx.run_all(T, S)
+        images.append((ctx.image(xbach.XB_IMG_DIFF, f64=False),
+                       ctx.image(xbach.XB_IMG_CONV, f64=False)))
+    for v in (1, 2):
+        assert np.array_equal(images[0][0], images[v][0]), v
+        assert np.array_equal(images[0][1], images[v][1]), v
+    ctx = xbach.Context(xbach.default_params(**kw))
+    ctx.run_all(T, S)  # autotune on (default)
+    assert int(ctx.scalar("tune:conv_sub_f32")) in (0, 1, 2)
+    assert np.array_equal(ctx.image(xbach.XB_IMG_DIFF, f64=False), images[0][0])

@@ -182,6 +182,10 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
   } else if(n == "rank") {
     if(value < 0 || value > 2) return XB_ERR_ARG;
     c->rank = (int)value;
+  } else if(n == "autotune") {
+    c->autotune = value != 0;
+  } else if(n == "tune_variant") {
+    c->tuneForce = value < 0 ? -1 : (int)value;
   } else if(n == "rank_tau") {
     if(value <= 0 || value >= 1000) return XB_ERR_ARG;
     c->rankTau = (int)value;

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -155,6 +156,8 @@ struct xb_ctx {
   int gramFp64 = 0;  // mixed mode: FP64 CUDA-core Gram instead of the tensor cores (checks)
   int rank = 0;          // learned substamp order after sss: 1 demote, 2 sort
   int rankTau = 500;     // demotion threshold of the accept probability, 1/1000
+  int autotune = 1;      // time the variants of tunable kernels on first use
+  int tuneForce = -1;    // >= 0: launch this variant of every tunable kernel
   float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
   xb::KTimers kt;
   std::string lastError;
@@ -277,6 +280,10 @@ int* deviceStatus(xb_ctx* c);
 // Throws XB_ERR_DEVICE_TIMEOUT when a bounded wait of the cluster solve or
 // the tensor-core Gram ran out since the last call (synchronises the stream).
 void checkSolveTimeout(xb_ctx* c);
+// Autotuner (xb_tune.cpp): the variant of a tunable kernel to launch for
+// (kernel, device, shape); times all nVariants through `launch` on first use.
+int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
+                 const std::function<void(int)>& launch);
 // Learned substamp ranking (xb_ranker.cu): reorder both sets' substamps.
 void rankSubstamps(xb_ctx* c);
 // Tensor-core Gram of the mixed path (xb_gram_tc.cu) into G (nList x R x R);

@@ -537,10 +537,9 @@ __global__ void __launch_bounds__(1024)
 }
 
 // -------------------------------------------------- conv + sub in FP32 ----
-// Four kernel blocks (84 columns) x one block row (21 rows) per CTA; each
+// BX kernel blocks (BX*21 columns) x one block row (21 rows) per CTA; each
 // thread produces seven adjacent pixels of one block row, streaming the image
-// row through registers.
-constexpr int CV_BX = 4;  // blocks per CTA along x
+// row through registers.  BX (2, 4 or 8) is chosen by the autotuner.
 struct ConvArgsF {
   int w, h, hK, fK, nPSF, kOrder, bgOrder, nComp, scaleConv;
   float tH, tL;
@@ -561,7 +560,7 @@ __device__ __forceinline__ uint16_t afterMaskF(float t, float tH, float tL) {
   return m;
 }
 
-template <int FK>
+template <int FK, int CV_BX>
 __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     k_conv_sub_f32(const float* __restrict__ I, const float* __restrict__ O,
                    const double* __restrict__ sol, const double* __restrict__ Kt,
@@ -648,6 +647,36 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
       for(int q = 0; q < PX; q++) acc[q] = fmaf(kk, win[q + ii], acc[q]);
     }
   }
+  // sum of |k| over the good pixels under the kernel, for pixels whose
+  // window holds a bad one: the same register-blocked pass over 0/1 flags,
+  // in the reference's tap order (adding |k| or 0 rounds like the
+  // conditional sum of the plain kernel)
+  bool anyq[PX];
+  bool need = false;
+#pragma unroll
+  for(int q = 0; q < PX; q++) {
+    unsigned char o = 0;
+    for(int jj = 0; jj < FK; jj++) o |= rowBad[ly + jj][lx0 + q];
+    anyq[q] = o != 0;
+    need |= anyq[q];
+  }
+  float uks[PX];
+#pragma unroll
+  for(int q = 0; q < PX; q++) uks[q] = 0.f;
+  if(need) {
+    for(int jj = 0; jj < FK; jj++) {
+      float gw[PX + FK - 1];
+#pragma unroll
+      for(int q = 0; q < PX + FK - 1; q++) gw[q] = bad[ly + jj][lx0 + q] ? 0.f : 1.f;
+      const float* krow = kb + (FK - 1 - jj) * FK;
+#pragma unroll
+      for(int ii = 0; ii < FK; ii++) {
+        const float kk = fabsf(krow[FK - 1 - ii]);
+#pragma unroll
+        for(int q = 0; q < PX; q++) uks[q] = fmaf(kk, gw[q + ii], uks[q]);
+      }
+    }
+  }
 #pragma unroll
   for(int q = 0; q < PX; q++) {
     const int x = x0 + HK + lx0 + q, y = y0 + HK + ly;
@@ -670,14 +699,8 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     const uint16_t cm = convMaskF(tc, a.tH, a.tL);
     uint16_t nm = cm;
     if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
-    unsigned char any = 0;
-    for(int jj = 0; jj < FK; jj++) any |= rowBad[ly + jj][lx0 + q];
-    if(any) {
-      float uks = 0.f;
-      for(int jj = 0; jj < FK; jj++)
-        for(int ii = 0; ii < FK; ii++)
-          if(!bad[ly + jj][lx0 + q + ii]) uks += fabsf(kb[(FK - 1 - ii) + (FK - 1 - jj) * FK]);
-      if((uks / aks[b]) < 0.99f) nm |= BAD_OUTPUT | BAD_CONV;
+    if(anyq[q]) {
+      if((uks[q] / aks[b]) < 0.99f) nm |= BAD_OUTPUT | BAD_CONV;
       else nm |= OK_CONV;
     }
     const float o = O[id];
@@ -1071,13 +1094,29 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   a.tH = (float)c->p.threshHigh;
   a.tL = (float)c->p.threshLow;
   const int xSteps = (c->w + g.fK - 1) / g.fK, ySteps = (c->h + g.fK - 1) / g.fK;
-  dim3 grid((xSteps + CV_BX - 1) / CV_BX, ySteps);
+  auto launch = [&](int variant) {
+    const float *Ii = (const float*)c->img[I], *Oi = (const float*)c->img[O];
+    switch(variant) {
+      case 0:
+        k_conv_sub_f32<21, 4><<<dim3((xSteps + 3) / 4, ySteps), 4 * 63, 0, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+        break;
+      case 1:
+        k_conv_sub_f32<21, 2><<<dim3((xSteps + 1) / 2, ySteps), 2 * 63, 0, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+        break;
+      default:
+        k_conv_sub_f32<21, 8><<<dim3((xSteps + 7) / 8, ySteps), 8 * 63, 0, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+        break;
+    }
+    XB_LAUNCHED(c);
+  };
+  // blocks per CTA: 4 (default), 2 or 8; the three give identical images
+  const int v = tunedVariant(c, "conv_sub_f32", (long long)c->w * 100003LL + c->h, 3, launch);
   {
     KT_SCOPE(c, "conv_sub");
-    k_conv_sub_f32<21><<<grid, CV_BX * 21 * 3, 0, c->stream>>>(
-        (const float*)c->img[I], (const float*)c->img[O], c->dSol, Kt, dKernSum, a, c->mask,
-        c->convF, c->diffF);
-    XB_LAUNCHED(c);
+    launch(v);
   }
   const long long n = (long long)c->w * c->h;
   k_border_f32<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
