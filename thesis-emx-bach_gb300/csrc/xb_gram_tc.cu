@@ -50,10 +50,18 @@ constexpr int GT_P1LD = 256 + 4, GT_P2LD = 64 + 4, GT_P3LD = 128 + 4;  // P3: sl
 constexpr size_t GT_P_BYTES = (size_t)(128 * GT_P1LD + 128 * GT_P2LD + 64 * GT_P3LD) * 4;
 constexpr size_t GT_SMEM = (GT_P_BYTES > 2 * (size_t)GT_BUF ? GT_P_BYTES : 2 * (size_t)GT_BUF) + 1024;
 constexpr unsigned long long GT_WAIT_NS = 2000000000ull;
+constexpr int GT_STAGE = GT_RB * GT_KC * 4;            // one FP32 W chunk (16 KB)
+static_assert(2 * GT_BUF + 2 * GT_STAGE <= (int)GT_P_BYTES, "staging fits the epilogue area");
 
 __device__ __forceinline__ uint32_t smemU32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
+__device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitOne() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ unsigned long long gtTimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -183,11 +191,31 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
 
+  // W chunks arrive one ahead through cp.async into two FP32 staging
+  // buffers behind the operand buffers (the epilogue reuses the area later);
+  // columns at or past ldW are not copied (the slicer zeroes k >= K).
+  float* stage = (float*)(buf + 2 * GT_BUF);
+  auto fetch = [&](int ch) {
+    float* st = stage + (ch & 1) * (GT_STAGE / 4);
+    for(int u = tid; u < GT_RB * (GT_KC / 4); u += GT_THREADS) {
+      const int r = u / (GT_KC / 4), k = ch * GT_KC + (u % (GT_KC / 4)) * 4;
+      if(r < wRows && k < ldW) cpAsync16(smemU32(st + r * GT_KC + (k - ch * GT_KC)), Ws + (size_t)r * ldW + k);
+    }
+    cpAsyncCommit();
+  };
+  fetch(0);
   for(int ch = 0; ch < nChunk; ch++) {
     const int b = ch & 1;
     unsigned char* B = buf + b * GT_BUF;
+    if(ch + 1 < nChunk) {
+      fetch(ch + 1);
+      cpAsyncWaitOne();
+    } else {
+      cpAsyncWaitAll();
+    }
     if(ch >= 2 && !gtWait(smemU32(&bars[b]), ((ch - 2) >> 1) & 1, deadline)) sErr = 1;
     __syncthreads();
+    const float* stc = stage + (ch & 1) * (GT_STAGE / 4);
     // 16-byte units: (row, 8 consecutive k) -> 5 slice units
     for(int u = tid; u < GT_RB * (GT_KC / 8); u += GT_THREADS) {
       const int r = u % GT_RB, kg = u / GT_RB, k0 = ch * GT_KC + kg * 8;  // rows fastest
@@ -200,7 +228,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
         for(int e = 0; e < 8; e++) {
           const int k = k0 + e;
           float x = 0.f;
-          if(k < K) x = r < wRows ? Ws[(size_t)r * ldW + k] : imgRow[k];
+          if(k < K) x = r < wRows ? stc[r * GT_KC + (k - ch * GT_KC)] : imgRow[k];
           // |Z| = round(|x| 2^(35 - e_r)) from the float's fields, in integers:
           // x = m 2^(ex - 150) (m with its hidden bit), so Z = m 2^sh.  As
           // |x| <= 2^e_r (1 - 2^-24), |Z| <= 2^35 - 2^11: five digits suffice.

@@ -569,12 +569,15 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
                    float* __restrict__ diffF) {
   constexpr int HK = FK / 2, NK = FK * FK, PX = 7, TPR = FK / PX;  // threads per block row
   constexpr int TW = CV_BX * FK + 2 * HK, TH = FK + 2 * HK;
-  __shared__ float tile[TH][TW + 1];
-  __shared__ unsigned char bad[TH][TW + 1];
+  // row padding with at most 2-way bank conflicts for the pixel loop's lanes
+  constexpr int TPAD = CV_BX == 4 ? 2 : (CV_BX == 2 ? 0 : 1);
+  __shared__ float tile[TH][TW + TPAD];
+  __shared__ unsigned char bad[TH][TW + TPAD];
   __shared__ unsigned char rowBad[TH][CV_BX * FK];  // OR of bad over the x window
   __shared__ float kern[CV_BX][NK];
   __shared__ double poly[CV_BX][16];
   __shared__ float aks[CV_BX];
+  __shared__ float bgc[16];  // background coefficients (getBackground), FP32
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int xB0 = blockIdx.x * CV_BX, yB = blockIdx.y;
   const int x0 = xB0 * FK, y0 = yB * FK;   // tile origin; block pixels start at +HK
@@ -622,7 +625,11 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     for(int p = 0; p < NK; p++) s += fabsf(kern[tid][p]);
     aks[tid] = s;
   }
+  const int nBgC = (a.bgOrder + 1) * (a.bgOrder + 2) / 2;
+  if(tid < nBgC && tid < 16) bgc[tid] = (float)sol[a.nComp + 2 + tid];
   __syncthreads();
+  const float hxF = 0.5f * (float)a.w, hyF = 0.5f * (float)a.h;
+  const float ihxF = 1.f / hxF, ihyF = 1.f / hyF;
   const float kernSum = (float)*kernSumPtr;
   const float invKernMult = a.scaleConv ? 1.f / kernSum : 1.f;
   const float convFactor = a.scaleConv ? kernSum : 1.f;
@@ -681,19 +688,20 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
   for(int q = 0; q < PX; q++) {
     const int x = x0 + HK + lx0 + q, y = y0 + HK + ly;
     if(x >= a.w - HK || y >= a.h - HK) continue;
-    // background polynomial (getBackground, cd.cl:444-467), FP64
-    const double bxf = (x - 0.5 * a.w) / (0.5 * a.w), byf = (y - 0.5 * a.h) / (0.5 * a.h);
-    double bgv = 0.0, ax = 1.0;
-    int k = a.nComp + 2;
+    // background polynomial (getBackground, cd.cl:444-467) in FP32: the
+    // terms are O(1e3) ADU, so FP32 rounding moves a pixel by ~1e-4 ADU
+    const float bxf = ((float)x - hxF) * ihxF, byf = ((float)y - hyF) * ihyF;
+    float bgv = 0.f, ax = 1.f;
+    int k = 0;
     for(int i = 0; i <= a.bgOrder; i++) {
-      double ay = 1.0;
+      float ay = 1.f;
       for(int j = 0; j <= a.bgOrder - i; j++) {
-        bgv = fma(sol[k++], ax * ay, bgv);
+        bgv = fmaf(bgc[k++], ax * ay, bgv);
         ay *= byf;
       }
       ax *= bxf;
     }
-    const float v = (acc[q] + (float)bgv) * invKernMult;
+    const float v = (acc[q] + bgv) * invKernMult;
     const size_t id = (size_t)x + (size_t)y * a.w;
     const float tc = tile[ly + HK][lx0 + q + HK];
     const uint16_t cm = convMaskF(tc, a.tH, a.tL);
