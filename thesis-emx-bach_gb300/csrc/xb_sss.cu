@@ -35,12 +35,12 @@ __device__ __forceinline__ int satFloorToInt(double v) {
 struct Ran1 {
   long long ix1, ix2, ix3;
   int idum, iff;
-  __device__ void init(int seed) {
+  __host__ __device__ void init(int seed) {
     idum = seed;
     iff = 0;
     ix1 = ix2 = ix3 = 0;
   }
-  __device__ double next(double* r) {
+  __host__ __device__ double next(double* r) {
     const long long M1 = 259200, IA1 = 7141, IC1 = 54773;
     const long long M2 = 134456, IA2 = 8121, IC2 = 28411;
     const long long M3 = 243000, IA3 = 4561, IC3 = 51349;
@@ -99,6 +99,65 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int* warpTot, int* tota
 // One CTA per stamp: sampleStamp + pad + sortSamples (sss.cl:148-217),
 // maskStamp (:224-255), sigmaClip with maxIter 3 (bachUtil.cpp:255-266,
 // bach.cl:129-184) and createHistogram (sss.cl:257-391).
+//
+// Every stamp seeds ran1 with -666, so all stamps draw the same sequence:
+// with `draws` (that sequence, precomputed on the host) the 32 candidates of
+// a sampling round are formed in parallel; without it lane 0 runs ran1.
+// The clip test |v - m| * inv > alpha is monotone in v on each side of m, so
+// each clip round first finds the exact thresholds v_lo < m < v_hi where it
+// turns true (a 32-ary search of one warp over the ordered doubles) and then
+// compares pixels against them.  The histogram bin floor((v - lbv) / bs) of
+// an FP32 pixel comes from an FP32 estimate whose error is bounded per pass;
+// only pixels within that bound of a bin edge redo it in FP64.  All decisions
+// and sums are those of the reference's order.
+
+// Order-preserving map of doubles (no NaN) to 64-bit keys and back.
+__device__ __forceinline__ unsigned long long dKey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double keyD(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ bool clipOut(double v, double m, double inv, double alpha) {
+  return fabs(v - m) * inv > alpha;
+}
+
+// One warp: the key of the first double (walking away from m, upwards when
+// up, downwards otherwise) at which clipOut turns true; `none` when it never
+// does.  clipOut is false at m and monotone along the walk.
+__device__ unsigned long long clipEdge(double m, double inv, double alpha, bool up, bool* none) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long kEnd = dKey(up ? INFINITY : -INFINITY);
+  unsigned long long lo = dKey(m), hi = kEnd;  // clipOut(lo) false, clipOut(hi) true
+  *none = !clipOut(up ? INFINITY : -INFINITY, m, inv, alpha);
+  if(*none) return kEnd;
+  for(int guard = 0; guard < 40; guard++) {
+    const unsigned long long span = up ? hi - lo : lo - hi;
+    if(span <= 1) break;
+    unsigned long long step = span / 33;
+    if(step == 0) step = 1;
+    const unsigned long long off = (unsigned long long)(lane + 1) * step;
+    const bool valid = off < span;
+    const unsigned long long k = up ? lo + off : lo - off;
+    const bool p = valid && clipOut(keyD(k), m, inv, alpha);
+    const unsigned bal = __ballot_sync(0xffffffffu, p);
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    if(bal) {
+      const int j = __ffs(bal) - 1;
+      const unsigned long long kj = __shfl_sync(0xffffffffu, k, j);
+      const unsigned long long kprev = __shfl_sync(0xffffffffu, k, j > 0 ? j - 1 : 0);
+      hi = kj;
+      if(j > 0) lo = kprev;
+    } else {
+      const int jl = 31 - __clz(vmask);
+      lo = __shfl_sync(0xffffffffu, k, jl);
+    }
+  }
+  return hi;
+}
+
 template <class T>
 __global__ void __launch_bounds__(ST_THREADS)
     k_stamp_stats(const T* __restrict__ img, uint16_t* __restrict__ mask,
@@ -106,24 +165,30 @@ __global__ void __launch_bounds__(ST_THREADS)
                   double* __restrict__ good, uint8_t* __restrict__ clip,
                   double* __restrict__ chunkBuf, int maxChunks,
                   double sigClipAlpha, double iqRange, double* __restrict__ skyOut,
-                  double* __restrict__ fwhmOut) {
+                  double* __restrict__ fwhmOut, const double* __restrict__ draws) {
   const int s = blockIdx.x;
   const int4 gm = geom[s];  // cx, cy, sx, sy
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr bool F32 = sizeof(T) == 4;
   __shared__ double samples[PADDED];
   __shared__ double rtab[98];
   __shared__ int cand[32];
   __shared__ int sCount;
   __shared__ int warpTot[ST_THREADS / 32];
   __shared__ int sTotal;
-  __shared__ double sMean, sStd, sInv;
+  __shared__ double sMean, sStd, sInv, sSum, sSum2;
   __shared__ int sPrev, sCurr, sClip, sDone;
   __shared__ int bins[256];
   __shared__ int okCount;
   __shared__ double hLower, hUpper, hSky, hBinSize, hLowerBinVal;
   __shared__ int hState;  // 0 continue, 1 stop (setFwhm), 2 stop (no fwhm)
+  __shared__ double tLo, tHi;          // clip thresholds of the current round
+  __shared__ float fLo, fHi;           // the same, rounded outward to float
+  __shared__ int tNoLo, tNoHi, tDirect;
+  __shared__ float bLbv, bInv, bDelta;  // FP32 bin estimate of the current pass
+  __shared__ int bExact;
 
-  // ---- phase A: random sampling (warp 0, RNG on lane 0) ----
+  // ---- phase A: random sampling (warp 0) ----
   if(tid < 32) {
     Ran1 rng;
     if(lane == 0) {
@@ -134,18 +199,27 @@ __global__ void __launch_bounds__(ST_THREADS)
     int cnt = 0, iter = 0;
     while(cnt < NSAMPLES && iter < numPix) {
       int b = min(32, numPix - iter);
-      if(lane == 0) {
-        for(int k = 0; k < b; k++) {
-          int rx = (int)floor(rng.next(rtab) * (int)gm.z);
-          int ry = (int)floor(rng.next(rtab) * (int)gm.w);
-          cand[k] = (rx + gm.x) + (ry + gm.y) * w;
+      int idx = 0;
+      if(draws) {
+        if(lane < b) {
+          const int rx = (int)floor(draws[2 * (iter + lane)] * (int)gm.z);
+          const int ry = (int)floor(draws[2 * (iter + lane) + 1] * (int)gm.w);
+          idx = (rx + gm.x) + (ry + gm.y) * w;
         }
+      } else {
+        if(lane == 0) {
+          for(int k = 0; k < b; k++) {
+            int rx = (int)floor(rng.next(rtab) * (int)gm.z);
+            int ry = (int)floor(rng.next(rtab) * (int)gm.w);
+            cand[k] = (rx + gm.x) + (ry + gm.y) * w;
+          }
+        }
+        __syncwarp();
+        if(lane < b) idx = cand[lane];
       }
-      __syncwarp();
       bool ok = false;
       double v = 0.0;
       if(lane < b) {
-        int idx = cand[lane];
         v = (double)img[idx];
         ok = !(mask[idx] > 0 || fabs(v) <= 1e-10);
       }
@@ -183,31 +257,37 @@ __global__ void __launch_bounds__(ST_THREADS)
   __syncthreads();
 
   // ---- phase B: ordered compaction of good pixels (maskStamp) ----
+  // each thread owns a contiguous run of the stamp's pixel indices, so one
+  // block scan keeps the ascending order
   double* gd = good + (size_t)s * fSW * fSW;
   uint8_t* cl = clip + (size_t)s * fSW * fSW;
-  int nGood = 0;
-  for(int base = 0; base < fSW * fSW; base += ST_THREADS) {
-    int idxS = base + tid;
-    bool ok = false;
-    double pix = 0.0;
-    if(idxS < fSW * fSW) {
-      int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
-      if(xI < w && yI < h) {
-        size_t id = (size_t)xI + (size_t)yI * w;
-        pix = (double)img[id];
-        if(!(mask[id] > 0 || pix <= 1e-10)) {
-          if(isnan(pix)) mask[id] |= NAN_PIXEL | BAD_INPUT;
-          else ok = true;
-        }
+  const int nPixS = fSW * fSW, per = (nPixS + ST_THREADS - 1) / ST_THREADS;
+  const int i0 = min(tid * per, nPixS), i1 = min(i0 + per, nPixS);
+  int myGood = 0;
+  for(int idxS = i0; idxS < i1; idxS++) {
+    const int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
+    if(xI < w && yI < h) {
+      const size_t id = (size_t)xI + (size_t)yI * w;
+      const double pix = (double)img[id];
+      if(!(mask[id] > 0 || pix <= 1e-10)) {
+        if(isnan(pix)) mask[id] |= NAN_PIXEL | BAD_INPUT;
+        else myGood++;
       }
     }
-    int pos = blockExclusiveScan(ok ? 1 : 0, warpTot, &sTotal);
-    if(ok) {
-      gd[nGood + pos] = pix;
-      cl[nGood + pos] = 0;
+  }
+  int pos = blockExclusiveScan(myGood, warpTot, &sTotal);
+  const int nGood = sTotal;
+  for(int idxS = i0; idxS < i1 && myGood > 0; idxS++) {
+    const int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
+    if(xI < w && yI < h) {
+      const size_t id = (size_t)xI + (size_t)yI * w;
+      const double pix = (double)img[id];
+      if(!(mask[id] > 0 || pix <= 1e-10)) {
+        gd[pos] = pix;
+        cl[pos] = 0;
+        pos++;
+      }
     }
-    nGood += sTotal;
-    __syncthreads();
   }
 
   // ---- phase C: sigma clip, maxIter 3 (bachUtil.cpp:34-128) ----
@@ -223,6 +303,35 @@ __global__ void __launch_bounds__(ST_THREADS)
   }
   __syncthreads();
   const int nChunks = (nGood + 31) / 32;
+  // exact clip thresholds for (m, inv) into tLo/tHi (warp 0; all threads call)
+  auto thresholds = [&](double m, double inv) {
+    if(warp == 0) {
+      const bool direct = !isfinite(m) || isnan(inv);
+      if(!direct) {
+        bool noHi, noLo;
+        const unsigned long long kh = clipEdge(m, inv, sigClipAlpha, true, &noHi);
+        const unsigned long long kl = clipEdge(m, inv, sigClipAlpha, false, &noLo);
+        if(lane == 0) {
+          tHi = keyD(kh);
+          tLo = keyD(kl);
+          fHi = __double2float_ru(tHi);  // f >= tHi  <=>  f >= fHi for a float f
+          fLo = __double2float_rd(tLo);
+          tNoHi = noHi;
+          tNoLo = noLo;
+        }
+      }
+      if(lane == 0) tDirect = direct;
+    }
+    __syncthreads();
+  };
+  auto isClipped = [&](double v, double m, double inv) -> bool {
+    if(tDirect) return clipOut(v, m, inv, sigClipAlpha);
+    if(F32) {
+      const float f = (float)v;  // exact: v came from a float pixel
+      return (!tNoHi && f >= fHi) || (!tNoLo && f <= fLo);
+    }
+    return (!tNoHi && v >= tHi) || (!tNoLo && v <= tLo);
+  };
   for(int it = 0; it < 3; it++) {
     if(sDone || sCurr == sPrev) break;
     if(sPrev <= 1) {
@@ -247,12 +356,19 @@ __global__ void __launch_bounds__(ST_THREADS)
       cS2[c] = a2;
     }
     __syncthreads();
+    // the two sequential chunk sums run on two warps
     if(tid == 0) {
-      double sum = 0.0, sum2 = 0.0;
-      for(int c = 0; c < nChunks; c++) {
-        sum += cS[c];
-        sum2 += cS2[c];
-      }
+      double sum = 0.0;
+      for(int c = 0; c < nChunks; c++) sum += cS[c];
+      sSum = sum;
+    } else if(tid == 32) {
+      double sum2 = 0.0;
+      for(int c = 0; c < nChunks; c++) sum2 += cS2[c];
+      sSum2 = sum2;
+    }
+    __syncthreads();
+    if(tid == 0) {
+      const double sum = sSum, sum2 = sSum2;
       double n = (double)sCurr;
       double m = sum / n;
       double sd = sqrt((sum2 - n * m * m) / (double)(sCurr - 1));
@@ -262,10 +378,11 @@ __global__ void __launch_bounds__(ST_THREADS)
       sClip = 0;
     }
     __syncthreads();
-    int myClip = 0;
     const double m = sMean, inv = sInv;
+    thresholds(m, inv);
+    int myClip = 0;
     for(int k = tid; k < nGood; k += ST_THREADS)
-      if(cl[k] == 0 && fabs(gd[k] - m) * inv > sigClipAlpha) {
+      if(cl[k] == 0 && isClipped(gd[k], m, inv)) {
         cl[k] = 1;
         myClip++;
       }
@@ -276,6 +393,7 @@ __global__ void __launch_bounds__(ST_THREADS)
   }
   __syncthreads();
   const double mean = sMean, invStd = 1.0 / sStd;
+  thresholds(mean, invStd);
 
   // ---- phase D: histogram sky / robust sigma (sss.cl:257-391) ----
   if(tid == 0) {
@@ -294,19 +412,47 @@ __global__ void __launch_bounds__(ST_THREADS)
       break;
     }
     for(int i = tid; i < 256; i += ST_THREADS) bins[i] = 0;
-    if(tid == 0) okCount = 0;
+    if(tid == 0) {
+      okCount = 0;
+      // FP32 estimate q' of q = (v - lbv) / bs: |q' - q| <= delta for |q| <= 512
+      // (lbv and 1/bs rounded to float, one FP32 rounding each in the
+      // subtraction and the product; the FP64 q itself is within 2^-51 |q|)
+      const double lbv = hLowerBinVal, bs = hBinSize;
+      const double delta = fabs(lbv) / bs * 0x1p-23 + 512.0 * 0x1p-21;
+      const bool ok = F32 && bs > 0.0 && isfinite(bs) && isfinite(lbv) && delta < 0.125;
+      bExact = ok ? 0 : 1;
+      bLbv = (float)lbv;
+      bInv = (float)(1.0 / bs);
+      bDelta = (float)delta;
+    }
     __syncthreads();
     const double lbv = hLowerBinVal, bs = hBinSize;
+    const bool exactAll = bExact != 0;
+    const float fl = bLbv, fi = bInv, fd = bDelta;
     int myOk = 0;
     for(int i = tid; i < gm.z * gm.w; i += ST_THREADS) {
       int x = i % gm.z, y = i / gm.z;
       size_t id = (size_t)(gm.x + x) + (size_t)(gm.y + y) * w;
       double v = (double)img[id];
       if(mask[id] != 0 || v <= 1e-10) continue;
-      if(fabs(v - mean) * invStd > sigClipAlpha) continue;
-      int index = satFloorToInt((v - lbv) / bs);
-      index = index == INT_MAX ? INT_MAX : index + 1;
-      index = min(max(index, 0), 255);
+      if(isClipped(v, mean, invStd)) continue;
+      int index = -1;
+      if(!exactAll) {
+        const float q = ((float)v - fl) * fi;
+        if(q > 300.f) {
+          index = 255;
+        } else if(q < -50.f) {
+          index = 0;
+        } else {
+          const float f0 = floorf(q), fr = q - f0;
+          if(fr > fd && fr < 1.f - fd) index = min(max((int)f0 + 1, 0), 255);
+        }
+      }
+      if(index < 0) {
+        index = satFloorToInt((v - lbv) / bs);
+        index = index == INT_MAX ? INT_MAX : index + 1;
+        index = min(max(index, 0), 255);
+      }
       atomicAdd(&bins[index], 1);
       myOk++;
     }
@@ -674,23 +820,44 @@ __global__ void k_reset_skip(uint16_t* mask, long long n) {
 
 }  // namespace
 
+// The ran1 sequence of seed -666 (the seed of every stamp, sss.cl:81-146),
+// n draws, generated once per context and size.
+static const double* ran1Draws(xb_ctx* c, int n) {
+  const std::string key = "ran1_draws";
+  auto it = c->pool.find(key);
+  const bool have = it != c->pool.end() && it->second.bytes >= (size_t)n * sizeof(double) &&
+                    c->scalars.count("ran1_draws_n") && c->scalars["ran1_draws_n"] >= n;
+  double* d = buf<double>(c, key, n);
+  if(!have) {
+    std::vector<double> h(n);
+    Ran1 rng;
+    double r[98];
+    rng.init(-666);
+    for(int i = 0; i < n; i++) h[i] = rng.next(r);
+    toDevice(c, d, h);
+    c->scalars["ran1_draws_n"] = n;
+  }
+  return d;
+}
+
 static void sssPass(xb_ctx* c, int* nKept) {
   const Geo& g = c->g;
   const int fSW = c->fStampWidth, nAll = c->nAll;
   const int maxChunks = (fSW * fSW + 31) / 32;
   double* chunkBuf = c->dWork;  // sized by stageSss
+  const double* draws = ran1Draws(c, 2 * fSW * fSW);
   for(int im = 0; im < 2; im++) {
     { KT_SCOPE(c, "stamp_stats");
     if(c->imgIsF64)
       k_stamp_stats<double><<<nAll, ST_THREADS, 0, c->stream>>>(
           (const double*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
           c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
-          c->p.iqRange, c->skyAll[im], c->fwhmAll[im]);
+          c->p.iqRange, c->skyAll[im], c->fwhmAll[im], draws);
     else
       k_stamp_stats<float><<<nAll, ST_THREADS, 0, c->stream>>>(
           (const float*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
           c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
-          c->p.iqRange, c->skyAll[im], c->fwhmAll[im]);
+          c->p.iqRange, c->skyAll[im], c->fwhmAll[im], draws);
     XB_LAUNCHED(c);
     }
   }
@@ -911,7 +1078,7 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
   // compaction, chunk sums before they are summed).
   xb::k_stamp_stats<float><<<nStamps, xb::ST_THREADS, 0, (cudaStream_t)stream>>>(
       dImg, dMask, reinterpret_cast<const int4*>(dGeom), w, h, fStampWidth, good, clip, chunks,
-      maxChunks, sigClipAlpha, iqRange, dSky, dFwhm);
+      maxChunks, sigClipAlpha, iqRange, dSky, dFwhm, nullptr);
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
   return XB_OK;
