@@ -782,6 +782,305 @@ __global__ void __launch_bounds__(FM_THREADS)
   }
 }
 
+// ------------------------------------------- substamp search in shared memory --
+// The decisions of k_find_substamps_maps for FP32 images, with the stamp's
+// pixels and every map in shared memory (15 B per pixel, one CTA per SM):
+// keys are the float bit patterns (ordered like the doubles of the reference
+// for positive values), the bad map is updated in place after an acceptance
+// (the skip bit it sets is part of this image's bad mask, and no other CTA
+// touches this image's bits of the stamp), and the two static predicates
+// (v - sky) / fwhm > tKF and !((v - sky) * (1/fwhm) < tKF), monotone in v,
+// become compares against their exact thresholds, found once per stamp by a
+// warp search over the ordered doubles; so does the pass threshold v > lim.
+constexpr int FS_T = 512;
+
+// One warp: smallest key in (lo, hi] at which pred turns true, given
+// pred(lo) false and pred(hi) true (pred monotone between them).
+template <class P>
+__device__ unsigned long long warpFirstTrue(unsigned long long lo, unsigned long long hi, P pred) {
+  const int lane = threadIdx.x & 31;
+  for(int guard = 0; guard < 40; guard++) {
+    const unsigned long long span = hi - lo;
+    if(span <= 1) break;
+    unsigned long long step = span / 33;
+    if(step == 0) step = 1;
+    const unsigned long long off = (unsigned long long)(lane + 1) * step;
+    const bool valid = off < span;
+    const unsigned long long k = lo + off;
+    const bool t = valid && pred(keyD(k));
+    const unsigned bal = __ballot_sync(0xffffffffu, t);
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    if(bal) {
+      const int j = __ffs(bal) - 1;
+      const unsigned long long kj = __shfl_sync(0xffffffffu, k, j);
+      const unsigned long long kp = __shfl_sync(0xffffffffu, k, j > 0 ? j - 1 : 0);
+      hi = kj;
+      if(j > 0) lo = kp;
+    } else {
+      lo = __shfl_sync(0xffffffffu, k, 31 - __clz(vmask));
+    }
+  }
+  return hi;
+}
+
+size_t fsSmemBytes(int n) { return (size_t)n * n * 15 + 64; }
+
+__global__ void __launch_bounds__(FS_T, 1)
+    k_find_substamps_sm(const float* __restrict__ img0, const float* __restrict__ img1,
+                        uint16_t* __restrict__ mask, const int4* __restrict__ geom,
+                        const double* __restrict__ sky0, const double* __restrict__ fwhm0,
+                        const double* __restrict__ sky1, const double* __restrict__ fwhm1,
+                        int2* __restrict__ xy0, double* __restrict__ val0, int* __restrict__ cnt0,
+                        int2* __restrict__ xy1, double* __restrict__ val1, int* __restrict__ cnt1,
+                        int w, int fSW, int hSS, int maxSS, double tH, double tKF) {
+  extern __shared__ __align__(16) unsigned char fs_s[];
+  const int s = blockIdx.x, im = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = FS_T / 32;
+  const float* img = im == 0 ? img0 : img1;
+  const double sky = im == 0 ? sky0[s] : sky1[s];
+  const double fwhm = im == 0 ? fwhm0[s] : fwhm1[s];
+  int2* xyOut = (im == 0 ? xy0 : xy1) + (size_t)s * maxSS;
+  double* valOut = (im == 0 ? val0 : val1) + (size_t)s * maxSS;
+  const uint16_t badMask =
+      (uint16_t)((MASK_ALL & ~OK_CONV) & ~(im == 0 ? (BAD_PIXEL_S | SKIP_S) : (BAD_PIXEL_T | SKIP_T)));
+  const uint16_t skipMask = im == 0 ? SKIP_T : SKIP_S;
+  const int4 gm = geom[s];
+  const int cx = gm.x, cy = gm.y, sx = gm.z, sy = gm.w, n = fSW, N = n * n;
+  const double invFwhm = 1.0 / fwhm;
+  float* V = (float*)fs_s;                 // N pixel values
+  uint32_t* key = (uint32_t*)(V + N);      // N (0: not a local-maximum candidate)
+  uint16_t* arg = (uint16_t*)(key + N);    // N (0xFFFF: none)
+  uint8_t* flags = (uint8_t*)(arg + N);    // N
+  uint8_t* bad = flags + N;                // N
+  uint8_t* hx = bad + N;                   // N (0xFF: none)
+  uint8_t* rowf = hx + N;                  // N
+  uint8_t* okw = rowf + N;                 // N
+  __shared__ int2 locXY[MAX_MAXSS];
+  __shared__ double locVal[MAX_MAXSS];
+  __shared__ int sBest;
+  __shared__ double rA[NW], rB[NW];
+  __shared__ double sSum;
+  __shared__ float sfP, sfK, sfLim;
+  __shared__ int sDirect;
+
+  for(int ly = warp; ly < n; ly += NW)
+    for(int lx = lane; lx < n; lx += 32) {
+      const size_t a = (size_t)(cx + lx) + (size_t)(cy + ly) * w;
+      V[ly * n + lx] = img[a];
+      bad[ly * n + lx] = (ldMask(mask, a) & badMask) ? 1 : 0;
+    }
+  // exact thresholds of the two static predicates
+  if(warp == 0) {
+    auto pr = [&](double v) { return (v - sky) / fwhm > tKF; };
+    auto kq = [&](double v) { return !((v - sky) * invFwhm < tKF); };
+    const bool direct = !(fwhm > 0.0 && isfinite(fwhm) && isfinite(sky) && isfinite(invFwhm) &&
+                          pr(INFINITY) && !pr(-INFINITY) && kq(INFINITY) && !kq(-INFINITY));
+    if(!direct) {
+      const unsigned long long kLo = dKey(-INFINITY), kHi = dKey(INFINITY);
+      const unsigned long long kP = warpFirstTrue(kLo, kHi, pr);
+      const unsigned long long kK = warpFirstTrue(kLo, kHi, kq);
+      if(lane == 0) {
+        sfP = __double2float_ru(keyD(kP));  // pr(v) <=> v >= sfP for a float v
+        sfK = __double2float_ru(keyD(kK));
+      }
+    }
+    if(lane == 0) sDirect = direct;
+  }
+  __syncthreads();
+  const bool direct = sDirect != 0;
+  const float fP = sfP, fK = sfK;
+  for(int p = tid; p < N; p += FS_T) {
+    const float f = V[p];
+    bool pr, kq;
+    if(direct) {
+      pr = ((double)f - sky) / fwhm > tKF;
+      kq = !(((double)f - sky) * invFwhm < tKF);
+    } else {
+      pr = f >= fP;
+      kq = isnan(f) || f >= fK;
+    }
+    const bool vpos = f > 0.f;
+    uint8_t fl = 0;
+    if(pr) fl |= FL_PRED;
+    if(pr && !vpos) fl |= FL_NONPOS;
+    if(kq) fl |= FL_KFQ;
+    if(vpos) fl |= FL_VPOS;
+    flags[p] = fl;
+  }
+  __syncthreads();
+  // maps of the current bad state (keys, window argmax, window ORs)
+  auto build = [&]() {
+    for(int p = tid; p < N; p += FS_T) {
+      const uint8_t fl = flags[p];
+      key[p] = (!bad[p] && (fl & FL_KFQ) && (fl & FL_VPOS)) ? __float_as_uint(V[p]) : 0u;
+    }
+    __syncthreads();
+    for(int ly = warp; ly < n; ly += NW)
+      for(int lx = lane; lx < n; lx += 32) {
+        const int row = ly * n;
+        uint32_t bk = 0;
+        int bi = 0xFF;
+        for(int x = max(lx - hSS, 0); x <= min(lx + hSS, n - 1); x++) {
+          const uint32_t k = key[row + x];
+          if(k > bk) {  // ascending x: ties keep the smallest x
+            bk = k;
+            bi = x;
+          }
+        }
+        hx[row + lx] = bk ? (uint8_t)bi : (uint8_t)0xFF;
+        uint8_t o = 0;
+        for(int x = max(lx - hSS, 0); x <= min(lx + hSS, sx - 1); x++) {
+          const uint8_t f = flags[row + x];
+          o |= bad[row + x] ? OK_BAD : 0;
+          o |= (f & FL_PRED) ? OK_PRED : 0;
+          o |= (f & FL_NONPOS) ? OK_NONPOS : 0;
+        }
+        rowf[row + lx] = o;
+      }
+    __syncthreads();
+    for(int ly = warp; ly < n; ly += NW)
+      for(int lx = lane; lx < n; lx += 32) {
+        uint32_t bk = 0;
+        int bi = 0xFFFF;
+        for(int y = max(ly - hSS, 0); y <= min(ly + hSS, n - 1); y++) {
+          const uint8_t xx = hx[y * n + lx];
+          if(xx == 0xFF) continue;
+          const uint32_t k = key[y * n + xx];
+          if(k > bk) {  // ascending y: the first row keeps ties
+            bk = k;
+            bi = y * n + xx;
+          }
+        }
+        arg[ly * n + lx] = (uint16_t)bi;
+        uint8_t o = 0;
+        for(int y = max(ly - hSS, 0); y <= min(ly + hSS, sy - 1); y++) o |= rowf[y * n + lx];
+        okw[ly * n + lx] = o;
+      }
+    __syncthreads();
+  };
+  build();
+  const double floorV = sky + tKF * fwhm;
+  double dfrac = 0.9;
+  int cnt = 0, passes = 0;
+  while(cnt < maxSS && passes < 256) {
+    passes++;
+    const double alt = sky + (tH - sky) * dfrac;
+    const double lim = floorV < alt ? alt : floorV;  // OpenCL max()
+    if(tid == 0) sfLim = __double2float_rd(lim);    // v > lim <=> v > sfLim for a float v
+    __syncthreads();
+    const float fLim = sfLim;
+    int start = 0;
+    while(cnt < maxSS && start < N) {
+      int mine = INT_MAX;
+      for(int p0 = start; p0 < N && mine == INT_MAX; p0 += 4 * FS_T) {
+        for(int k = 0; k < 4; k++) {
+          const int p = p0 + k * FS_T + tid;
+          if(p >= N || p >= mine) break;
+          if(bad[p] || !(flags[p] & FL_KFQ)) continue;
+          if(!(V[p] > fLim)) continue;
+          const int m = arg[p] != 0xFFFF ? arg[p] : p;
+          const uint8_t o = okw[m];
+          if(!(o & OK_BAD) && (o & OK_PRED)) {
+            mine = p;
+            break;
+          }
+        }
+        mine = __reduce_min_sync(0xffffffffu, mine);
+        if(tid == 0) sBest = INT_MAX;
+        __syncthreads();
+        if(lane == 0 && mine != INT_MAX) atomicMin(&sBest, mine);
+        __syncthreads();
+        mine = sBest;
+        __syncthreads();
+      }
+      if(mine == INT_MAX) break;
+      const int p = mine, m = arg[p] != 0xFFFF ? arg[p] : p;
+      const int mx = cx + m % n, my = cy + m / n;
+      const int u0 = max(mx - hSS, cx), v0 = max(my - hSS, cy);
+      const int u1 = min(mx + hSS, cx + sx - 1), v1 = min(my + hSS, cy + sy - 1);
+      const int uw = u1 - u0 + 1, un = uw * (v1 - v0 + 1);
+      // value of the substamp: sum of the thresholded pixels in raster order
+      double part = 0.0, amin = INFINITY;
+      for(int i = tid; i < un; i += FS_T) {
+        const int lx = u0 + i % uw - cx, ly = v0 + i / uw - cy;
+        if(flags[ly * n + lx] & FL_PRED) {
+          const double v = (double)V[ly * n + lx];
+          part += v;
+          amin = fmin(amin, fabs(v));
+        }
+      }
+#pragma unroll
+      for(int o = 16; o > 0; o >>= 1) {
+        part += __shfl_down_sync(0xffffffffu, part, o);
+        amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
+      }
+      if(lane == 0) {
+        rA[warp] = part;
+        rB[warp] = amin;
+      }
+      __syncthreads();
+      if(tid == 0) {
+        double t = 0.0, mn = INFINITY;
+        for(int i = 0; i < NW; i++) {
+          t += rA[i];
+          mn = fmin(mn, rB[i]);
+        }
+        int exact = 0;
+        if(!(okw[m] & OK_NONPOS) && mn > 0.0 && mn < INFINITY) {
+          int e;
+          frexp(mn, &e);                           // mn in [2^(e-1), 2^e)
+          const double quantum = ldexp(1.0, e - 1 - 23);
+          exact = t < ldexp(quantum, 52) ? 1 : 0;  // t = sum|v| here (all v > 0)
+        }
+        if(!exact) {
+          t = 0.0;
+          for(int yy = v0; yy <= v1; yy++)
+            for(int xx = u0; xx <= u1; xx++) {
+              const int q = (yy - cy) * n + (xx - cx);
+              if(flags[q] & FL_PRED) t += (double)V[q];
+            }
+        }
+        sSum = t;
+      }
+      __syncthreads();
+      const double ret = sSum;
+      start = p + 1;
+      if(ret == 0.0) continue;
+      if(tid == 0) {
+        locXY[cnt] = make_int2(mx, my);
+        locVal[cnt] = ret;
+      }
+      cnt++;
+      for(int i = tid; i < un; i += FS_T) {
+        const int gx = u0 + i % uw, gy = v0 + i / uw;
+        orMask(mask, (size_t)gx + (size_t)gy * w, skipMask);
+        bad[(gy - cy) * n + (gx - cx)] = 1;  // skipMask is part of badMask
+      }
+      __syncthreads();
+      if(cnt < maxSS) build();
+    }
+    if(cnt >= maxSS || lim == floorV) break;
+    dfrac -= 0.2;
+  }
+  __syncthreads();
+  if(tid == 0) {
+    for(int i = 1; i < cnt; i++)
+      for(int j = i; j > 0 && locVal[j - 1] < locVal[j]; j--) {
+        int2 t = locXY[j - 1];
+        locXY[j - 1] = locXY[j];
+        locXY[j] = t;
+        double tv = locVal[j - 1];
+        locVal[j - 1] = locVal[j];
+        locVal[j] = tv;
+      }
+    for(int i = 0; i < maxSS; i++) {
+      xyOut[i] = i < cnt ? locXY[i] : make_int2(INT_MAX, INT_MAX);
+      valOut[i] = i < cnt ? locVal[i] : -INFINITY;
+    }
+    (im == 0 ? cnt0 : cnt1)[s] = min(cnt, maxSS / 2);
+  }
+}
+
 // removeEmptyStamps (src/sssUtil.cpp:106-197, sss.cl:574-638): keep stamps
 // with at least one substamp in ascending original order.  One CTA per image.
 __global__ void __launch_bounds__(256)
@@ -865,7 +1164,16 @@ static void sssPass(xb_ctx* c, int* nKept) {
   { KT_SCOPE(c, "find_substamps");
   const size_t perCta = ((size_t)fSW * fSW * 18 + 255) / 256 * 256;
   unsigned char* scratch = buf<unsigned char>(c, "fm_scratch", (size_t)2 * nAll * perCta);
-  if(c->imgIsF64)
+  const size_t fsSmem = fsSmemBytes(fSW);
+  if(!c->imgIsF64 && fSW <= 120) {
+    XB_CUDA(cudaFuncSetAttribute(k_find_substamps_sm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fsSmem));
+    k_find_substamps_sm<<<grid, FS_T, fsSmem, c->stream>>>(
+        (const float*)c->img[0], (const float*)c->img[1], c->mask, c->geomAll, c->skyAll[0],
+        c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0], c->ssvalAll[0], c->cntAll[0],
+        c->ssxyAll[1], c->ssvalAll[1], c->cntAll[1], c->w, fSW, g.hSS, g.maxSS, c->p.threshHigh,
+        c->p.threshKernFit);
+  } else if(c->imgIsF64)
     k_find_substamps_maps<double><<<grid, FM_THREADS, 0, c->stream>>>(
         (const double*)c->img[0], (const double*)c->img[1], c->mask, c->geomAll,
         c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0],
