@@ -931,10 +931,18 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
     globalSolveMixed(c, f.M, n, dSol, f.piv, f.singular);
     return;
   }
-  constexpr int CL = 8;
-  const int ncol = (n + CL - 1) / CL;
-  const size_t smem = ((size_t)ncol * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
-  XB_CUDA(cudaFuncSetAttribute(k_global_lu<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // 8 CTAs, or 16 when 8 cannot hold the columns (the same products in the
+  // same order either way)
+  int maxSmem = 0;
+  XB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  auto luSmem = [&](int cl) {
+    return ((size_t)((n + cl - 1) / cl) * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
+  };
+  const int CL = luSmem(8) <= (size_t)maxSmem ? 8 : 16;
+  const size_t smem = luSmem(CL);
+  auto luKernel = CL == 8 ? k_global_lu<8> : k_global_lu<16>;
+  XB_CUDA(cudaFuncSetAttribute(luKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if(CL > 8) XB_CUDA(cudaFuncSetAttribute(luKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(256);
@@ -948,7 +956,7 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   { KT_SCOPE(c, "global_lu");
-  XB_CUDA(cudaLaunchKernelEx(&cfg, k_global_lu<CL>, f.M, n, f.piv, f.singular));
+  XB_CUDA(cudaLaunchKernelEx(&cfg, luKernel, f.M, n, f.piv, f.singular));
   XB_LAUNCHED(c);
   }
   const size_t smemS = (size_t)(2 * (n + 1)) * sizeof(double) + (size_t)(n + 1) * sizeof(int);

@@ -133,9 +133,9 @@ __global__ void __launch_bounds__(MX_THREADS)
 // the normal matrices are ill-conditioned (cond ~1e14), and an FP32
 // accumulation moves the fitted kernel sum by up to 9 %, while FP32 storage of
 // W itself (a consistent design matrix) moves it by ~1e-7.  Each stamp's
-// lower triangle is split over GM_SPLIT CTAs; k_gram_scatter then fills Q
+// lower triangle is split over gridDim.y CTAs; k_gram_scatter then fills Q
 // (createQ), B (createB) and the global-matrix dot table.
-constexpr int GM_KT = 32, GM_SPLIT = 6, GM_E = 1;
+constexpr int GM_KT = 32, GM_SPLIT = 6;
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
     k_gram_mixed(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(MX_THREADS)
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS, R = wRows + 1;
   const int nEnt = R * (R + 1) / 2;
-  const int per = (nEnt + GM_SPLIT - 1) / GM_SPLIT, e0 = blockIdx.y * per;
+  const int per = (nEnt + gridDim.y - 1) / gridDim.y, e0 = blockIdx.y * per;
   double* tile = gm_s;  // R x (GM_KT + 1)
   const float* Ws = W + (size_t)s * wRows * ldW;
   const bool live = cur[s] < count[s];
@@ -940,10 +940,10 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     KT_SCOPE(c, "gram");
     const int R = g.wRows + 1;
     const size_t smem = (size_t)R * (GM_KT + 1) * sizeof(double);
-    if((R * (R + 1) / 2 + GM_SPLIT - 1) / GM_SPLIT > GM_E * MX_THREADS)
-      throw XbError{XB_ERR_UNSUPPORTED, "too many basis functions for the Gram kernel"};
+    // one Gram entry per thread of the split CTAs
+    const int split = std::max(GM_SPLIT, (R * (R + 1) / 2 + MX_THREADS - 1) / MX_THREADS);
     double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
-    dim3 grid(nList, GM_SPLIT);
+    dim3 grid(nList, split);
     if(gramTensorCores(c, si, dList, nList, other, G)) {
       // exact tensor-core Gram (xb_gram_tc.cu)
     } else if(c->imgIsF64)

@@ -22,7 +22,19 @@ CONFIGS = {
     2: dict(size=2048, n_src=20000, fwhm_t=(2.2, 3.2), fwhm_s=(3.0, 4.2),
             flux=(1e3, 1e6), cr_frac=0.01, n_sat=40, stamps=16,
             saturation=6e4),
+    # 3072x3072 crowded field, 80k sources down to 1e2 ADU, FWHM varying
+    # across the field, 20x20 stamps; fitted with 4 Gaussians (sigma
+    # 0.6/1.2/2.4/4.8, degrees 6/4/3/2 -> 59 functions), kernel order 3,
+    # background order 2 (see PARAMS_3)
+    3: dict(size=3072, n_src=80000, fwhm_t=(2.2, 3.2), fwhm_s=(3.0, 4.2),
+            flux=(1e2, 1e6), cr_frac=0.0, n_sat=0, stamps=20,
+            saturation=None),
 }
+
+# Basis and orders of preset 3 (keyword arguments of xbach.default_params).
+PARAMS_3 = dict(nGauss=4, dg=[6, 4, 3, 2],
+                bg=[1 / (2 * 0.6 ** 2), 1 / (2 * 1.2 ** 2), 1 / (2 * 2.4 ** 2), 1 / (2 * 4.8 ** 2)],
+                kernelOrder=3, backgroundOrder=2)
 
 
 def _render(img, xs, ys, fluxes, sigmas):
