@@ -138,7 +138,15 @@ const char* xb_last_error(const xb_ctx* ctx);
  * score.
  * "gram_fp64" (0/1, mixed mode): compute the per-stamp Gram matrices with
  * FP64 accumulation on the CUDA cores instead of the exact tensor-core
- * slicing (a cross-check; the results agree to rounding). */
+ * slicing (a cross-check; the results agree to rounding).
+ * "graph" (0/1, mixed mode only): xb_run, xb_run_device and batches replay
+ * each frame as one captured CUDA graph.  The host decisions of the stages
+ * (kept-stamp counts, the sss retry, the cd test lists and direction, the ksc
+ * refit loop) run on the device as conditional nodes; the first frame of a
+ * shape (size and parameters) runs stage by stage and is captured, later
+ * frames of that shape replay it with one synchronisation.  Results are the
+ * stage-by-stage results bit for bit.  Ignored while "trace", "rank" or
+ * "time_kernels" is on. */
 int xb_set_option(xb_ctx* ctx, const char* name, long long value);
 
 /* ---- stage API (include/bach.h:66-87) ------------------------------------ */
@@ -172,6 +180,11 @@ int xb_sub(xb_ctx* ctx);
 /* All of init..sub in order (fin = reading the images back). */
 int xb_run(xb_ctx* ctx, const float* T, const float* S, int w, int h,
            float* convOut, float* diffOut);
+/* All of init..sub from device images to device images (dConv/dDiff may be
+ * NULL); the frame graph path when option "graph" is on.  The caller's input
+ * buffers are only read during the call. */
+int xb_run_device(xb_ctx* ctx, const float* dT, const float* dS, int w, int h,
+                  float* dConv, float* dDiff);
 
 /* ---- results -------------------------------------------------------------- */
 #define XB_IMG_CONV 0 /* convolved image, the `-o` output (default diff.fits) */

@@ -1,0 +1,156 @@
+"""Frame graphs (option "graph", mixed mode): a replayed frame writes the
+images and decisions of the stage-by-stage run bit for bit, across frames of
+one shape, across several shapes on one context, through the sss retry and
+the no-substamp exit, and inside batches."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DECISIONS = ("convTemplate", "ksc_iterations", "sss_retry", "merit0", "merit1", "kernSum",
+             "singular")
+
+
+def _stage_by_stage(params, T, S):
+    import xbach
+    ctx = xbach.Context(params)
+    ctx.run_all(T, S)
+    return (ctx.image(xbach.XB_IMG_CONV, f64=False), ctx.image(xbach.XB_IMG_DIFF, f64=False),
+            {k: ctx.scalar(k) for k in DECISIONS}, ctx.solution())
+
+
+def _check_same(ctx, ref, tag):
+    """Bit-identical images, decisions and solution (NaN matches NaN: a
+    degenerate fit must degenerate the same way)."""
+    import xbach
+    conv, diff, dec, sol = ref
+    assert np.array_equal(ctx.image(xbach.XB_IMG_DIFF, f64=False), diff, equal_nan=True), tag
+    assert np.array_equal(ctx.image(xbach.XB_IMG_CONV, f64=False), conv, equal_nan=True), tag
+    for k, v in dec.items():
+        assert np.array_equal(ctx.scalar(k), v, equal_nan=True), (tag, k)
+    assert np.array_equal(ctx.solution(), sol, equal_nan=True), tag
+
+
+def _pairs(n, config=1, **kw):
+    from xbach.synth import make_pair
+    out = []
+    for f in range(n):
+        T, S, info = make_pair(config, frame=f, **kw)
+        out.append((T, S, info))
+    return out
+
+
+def test_graph_replays_equal_stage_by_stage():
+    import xbach
+    fr = _pairs(3)
+    info = fr[0][2]
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=info["stamps"],
+                                  stampsy=info["stamps"], threshHigh=info["threshHigh"])
+    ctx = xbach.Context(params)
+    ctx.set_option("graph", 1)
+    order = [0, 1, 2, 0, 2]  # first call captures, the rest replay
+    for step, i in enumerate(order):
+        T, S, _ = fr[i]
+        ctx.run(T, S)
+        if step == 0:
+            assert ctx.scalar("graph_captured") == 1
+        else:
+            assert ctx.scalar("graph_replay") == 1
+        _check_same(ctx, _stage_by_stage(params, T, S), (step, i))
+        assert ctx.launches() > 0
+
+
+def test_graph_shapes_share_a_context(test01):
+    import xbach
+    a = (test01["T"].astype(np.float32), test01["S"].astype(np.float32))
+    T1, S1, _ = _pairs(1)[0]
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED)
+    ctx = xbach.Context(params)
+    ctx.set_option("graph", 1)
+    refs = {0: _stage_by_stage(params, *a), 1: _stage_by_stage(params, T1, S1)}
+    for step, i in enumerate([0, 1, 0, 1, 1, 0]):
+        T, S = a if i == 0 else (T1, S1)
+        ctx.run(T, S)
+        _check_same(ctx, refs[i], (step, i))
+
+
+def test_graph_through_the_sss_retry():
+    import xbach
+    from xbach.synth import make_pair
+    # few bright sources: fewer than a tenth of the stamps hold a substamp, so
+    # sss repeats its pass (the fit that follows is poorly constrained; the
+    # replay has to reproduce it all the same)
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED)
+    fr, refs = [], []
+    for f in range(12):
+        T, S, _ = make_pair(1, frame=f, n_src=9, flux=(3e4, 1.5e5))
+        try:
+            ref = _stage_by_stage(params, T, S)
+        except xbach.XbError:
+            continue
+        if ref[2]["sss_retry"] == 1:
+            fr.append((T, S))
+            refs.append(ref)
+        if len(fr) == 2:
+            break
+    assert len(fr) == 2, "no sparse field triggered the retry"
+    ctx = xbach.Context(params)
+    ctx.set_option("graph", 1)
+    for step, i in enumerate([0, 1, 0]):
+        ctx.run(*fr[i])
+        _check_same(ctx, refs[i], (step, i))
+
+
+def test_graph_reports_no_substamps():
+    import xbach
+    T, S, _ = _pairs(1)[0]
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED)
+    ctx = xbach.Context(params)
+    ctx.set_option("graph", 1)
+    ctx.run(T, S)  # capture
+    zero = np.zeros_like(T)
+    with pytest.raises(xbach.XbError) as e:
+        ctx.run(zero, zero)  # replay: the device record reports it
+    assert e.value.code == 4  # XB_ERR_NO_SUBSTAMPS
+    ctx.run(T, S)  # the graph stays usable
+    _check_same(ctx, _stage_by_stage(params, T, S), "after")
+
+
+def test_graph_device_frames_and_batches():
+    import torch
+    import xbach
+    fr = _pairs(4)
+    info = fr[0][2]
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=info["stamps"],
+                                  stampsy=info["stamps"], threshHigh=info["threshHigh"])
+    refs = [_stage_by_stage(params, T, S) for T, S, _ in fr]
+    # xb_run_device on one context
+    ctx = xbach.Context(params)
+    ctx.set_option("graph", 1)
+    for step, i in enumerate([0, 1, 2, 3]):
+        T, S, _ = fr[i]
+        dT, dS = torch.from_numpy(T).cuda(), torch.from_numpy(S).cuda()
+        dC, dD = torch.empty_like(dT), torch.empty_like(dT)
+        h, w = T.shape
+        torch.cuda.synchronize()  # the context works on a stream of its own
+        ctx.run_device(dT.data_ptr(), dS.data_ptr(), w, h, dC.data_ptr(), dD.data_ptr())
+        torch.cuda.synchronize()
+        assert np.array_equal(dD.cpu().numpy(), refs[i][1]), step
+        assert np.array_equal(dC.cpu().numpy(), refs[i][0]), step
+    # a batch whose workers replay graphs
+    batch = xbach.Batch(params, workers=2)
+    batch.set_option("graph", 1)
+    for rep in range(2):
+        diffs = [np.empty_like(T) for T, _, _ in fr]
+        st, ks = batch.run([T for T, _, _ in fr], [S for _, S, _ in fr], None, diffs)
+        assert st == [0] * len(fr)
+        for i in range(len(fr)):
+            assert np.array_equal(diffs[i], refs[i][1]), (rep, i)
+            assert ks[i] == refs[i][2]["kernSum"], (rep, i)
+
+
+def test_graph_option_needs_mixed_mode():
+    import xbach
+    ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_PLAIN))
+    with pytest.raises(xbach.XbError):
+        ctx.set_option("graph", 1)

@@ -32,28 +32,7 @@ namespace {
 // caller's device buffers.
 int runDeviceFrame(xb_ctx* c, const float* dT, const float* dS, int w, int h, float* dConv,
                    float* dDiff) {
-  int rc = xb_init_device_f32(c, dT, dS, w, h);
-  if(rc == XB_OK) rc = xb_sss(c);
-  if(rc == XB_OK) rc = xb_cmv(c);
-  if(rc == XB_OK) rc = xb_cd(c, nullptr);
-  if(rc == XB_OK) rc = xb_ksc(c);
-  if(rc == XB_OK) rc = xb_conv(c, nullptr);
-  if(rc == XB_OK) rc = xb_sub(c);
-  if(rc != XB_OK) return rc;
-  const float *conv = nullptr, *diff = nullptr;
-  rc = xb_get_device_images(c, &conv, &diff);
-  if(rc != XB_OK) return rc;
-  const size_t bytes = (size_t)w * h * sizeof(float);
-  cudaError_t e = cudaSuccess;
-  if(dConv) e = cudaMemcpyAsync(dConv, conv, bytes, cudaMemcpyDeviceToDevice, c->stream);
-  if(e == cudaSuccess && dDiff)
-    e = cudaMemcpyAsync(dDiff, diff, bytes, cudaMemcpyDeviceToDevice, c->stream);
-  if(e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if(e != cudaSuccess) {
-    c->lastError = std::string("batch output copy: ") + cudaGetErrorString(e);
-    return XB_ERR_CUDA;
-  }
-  return XB_OK;
+  return xb_run_device(c, dT, dS, w, h, dConv, dDiff);
 }
 
 template <class F>

@@ -160,6 +160,7 @@ int xb_ctx_destroy(xb_ctx* c) {
   if(!c) return XB_ERR_ARG;
   cudaSetDevice(c->device);
   if(c->stream) cudaStreamSynchronize(c->stream);
+  destroyGraphs(c);
   for(auto& kv : c->pool)
     if(kv.second.p) cudaFree(kv.second.p);
   if(c->stream) cudaStreamDestroy(c->stream);
@@ -179,6 +180,12 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->kt.total.clear();
   } else if(n == "gram_fp64") {
     c->gramFp64 = value != 0;
+  } else if(n == "graph") {
+    if(value != 0 && !mixedMode(c)) {
+      c->lastError = "frame graphs are built for the mixed mode";
+      return XB_ERR_UNSUPPORTED;
+    }
+    c->graph = value != 0;
   } else if(n == "rank") {
     if(value < 0 || value > 2) return XB_ERR_ARG;
     c->rank = (int)value;
@@ -277,8 +284,31 @@ int xb_sub(xb_ctx* c) {
   });
 }
 
+int xb_run_device(xb_ctx* c, const float* dT, const float* dS, int w, int h, float* dConv,
+                  float* dDiff) {
+  return guarded(c, [&] {
+    if(!dT || !dS || w <= 0 || h <= 0) throw XbError{XB_ERR_ARG, "bad image"};
+    runFrameDevice(c, dT, dS, w, h, dConv, dDiff);
+  });
+}
+
 int xb_run(xb_ctx* c, const float* T, const float* S, int w, int h, float* convOut,
            float* diffOut) {
+  if(c && c->graph && mixedMode(c)) {
+    // frame graph: inputs to the device, one replay, outputs back
+    int rc = guarded(c, [&] {
+      if(!T || !S || w <= 0 || h <= 0) throw XbError{XB_ERR_ARG, "bad image"};
+      const size_t n = (size_t)w * h;
+      float* dT = buf<float>(c, "run_in0", n);
+      float* dS = buf<float>(c, "run_in1", n);
+      XB_CUDA(cudaMemcpyAsync(dT, T, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+      XB_CUDA(cudaMemcpyAsync(dS, S, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+      runFrameDevice(c, dT, dS, w, h, nullptr, nullptr);
+    });
+    if(rc == XB_OK && convOut) rc = xb_get_image(c, XB_IMG_CONV, convOut);
+    if(rc == XB_OK && diffOut) rc = xb_get_image(c, XB_IMG_DIFF, diffOut);
+    return rc;
+  }
   int rc = xb_init_f32(c, T, w, h, S, w, h);
   if(rc == XB_OK) rc = xb_sss(c);
   if(rc == XB_OK) rc = xb_cmv(c);

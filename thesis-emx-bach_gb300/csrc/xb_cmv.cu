@@ -216,12 +216,13 @@ __global__ void __launch_bounds__(FILL_THREADS)
 // Refill W, Q and B of the listed stamps of set `si`, convolving image
 // `imgConv` and projecting on the other image (fillStamps,
 // src/cmvUtil.cpp:37-187).
-void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
+void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv, const int* liveN) {
   if(nList <= 0) return;
   if(mixedMode(c)) {
-    fillStampsMixed(c, si, dList, nList, imgConv);
+    fillStampsMixed(c, si, dList, nList, imgConv, liveN);
     return;
   }
+  if(liveN) throw XbError{XB_ERR_STATE, "device-counted fills are a mixed-mode path"};
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
   const int nGroups = (int)c->basis.yGroupStart.size() - 1;
@@ -285,7 +286,7 @@ void stageCmv(xb_ctx* c) {
     for(int s = 0; s < S.n; s++) all[s] = s;
     int* dList = buf<int>(c, "fillList" + sfx, std::max(S.n, 1));
     toDevice(c, dList, all);
-    fillStamps(c, si, dList, S.n, si);
+    fillStamps(c, si, dList, S.n, si, S.dN);
   }
   if(c->trace) {
     for(int si = 0; si < 2; si++) {

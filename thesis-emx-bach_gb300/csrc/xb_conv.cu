@@ -209,6 +209,7 @@ void stageConvSub(xb_ctx* c, bool doSub) {
     c->convD = nullptr;
     c->diffD = nullptr;
     convSubMixed(c, ks);
+    if(c->capturing) return;  // a frame graph records the kernel sum on the device
     c->kernSum = toHost(c, ks, 1)[0];
     c->scalars["kernSum"] = c->kernSum;
     if(c->trace) {

@@ -125,8 +125,13 @@ void* poolGet(xb_ctx* c, const char* name, size_t bytes) {
   DevBuf& b = c->pool[name];
   if(b.bytes >= bytes) return b.p;
   if(b.p) {
-    XB_CUDA(cudaStreamSynchronize(c->stream));
-    cudaFree(b.p);
+    if(c->keepBuffers) {
+      // a captured frame graph may still address it: freed with the context
+      c->retired.push_back(b.p);
+    } else {
+      XB_CUDA(cudaStreamSynchronize(c->stream));
+      cudaFree(b.p);
+    }
     b.p = nullptr;
     b.bytes = 0;
   }

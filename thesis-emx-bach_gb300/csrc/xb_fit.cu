@@ -78,8 +78,9 @@ __device__ __forceinline__ void pivotCombine(double& v, int& i, double ov, int o
 constexpr int LU_THREADS = 128;
 __global__ void __launch_bounds__(LU_THREADS)
     k_stamp_test_fit(const double* __restrict__ Q, const double* __restrict__ B, int qc,
-                     double* __restrict__ kernelSums) {
+                     const int* __restrict__ liveN, double* __restrict__ kernelSums) {
   extern __shared__ double lu_s[];
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int s = blockIdx.x, tid = threadIdx.x, n = qc - 1;
   double* a = lu_s;                 // qc * qc
   double* b = a + qc * qc;          // qc
@@ -170,9 +171,10 @@ __global__ void __launch_bounds__(LU_THREADS)
 // sigmaClip of the kernel sums (10 iterations, cdkscUtil.cpp:74-76) and
 // genCdTestStamps (cd.cl:54-94) in ascending order.
 __global__ void __launch_bounds__(256)
-    k_cd_select(const double* __restrict__ ks, int n, double alpha, double sigKernFit,
-                uint8_t* flags, double* cs, double* cs2, int* __restrict__ testIdx,
-                int* __restrict__ nTest, double* __restrict__ stats) {
+    k_cd_select(const double* __restrict__ ks, int n, const int* __restrict__ liveN, double alpha,
+                double sigKernFit, uint8_t* flags, double* cs, double* cs2,
+                int* __restrict__ testIdx, int* __restrict__ nTest, double* __restrict__ stats) {
+  if(liveN) n = *liveN;
   __shared__ double sMean, sStd;
   __shared__ int sh[4];
   __shared__ int warpTot[8];
@@ -198,10 +200,11 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------- spatial weights -----
 // createMatrixWeights (cd.cl:152-180) = the weight loop of CPU createMatrix
 // (cdkscUtil.cpp:331-342).
-__global__ void k_weights(const int* __restrict__ list, int nList, const int* __restrict__ count,
-                          const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
-                          const int2* __restrict__ kp, int nC2, int w, int h,
-                          double* __restrict__ wts) {
+__global__ void k_weights(const int* __restrict__ list, int nList, const int* __restrict__ liveN,
+                          const int* __restrict__ count, const int* __restrict__ cur,
+                          const int2* __restrict__ ssxy, int maxSS, const int2* __restrict__ kp,
+                          int nC2, int w, int h, double* __restrict__ wts) {
+  if(liveN) nList = min(nList, *liveN);
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if(e >= nList * nC2) return;
   int t = e / nC2, k = e % nC2, s = list[t];
@@ -727,9 +730,10 @@ __global__ void __launch_bounds__(SIG_THREADS)
 // + merit = mean / kernelMean, or 666 when nothing survives
 // (cdkscUtil.cpp:234-265).
 __global__ void __launch_bounds__(256)
-    k_cd_merit(const double* __restrict__ sig, int n, const double* __restrict__ kernelMean,
-               double alpha, double* clean, uint8_t* flags, double* cs, double* cs2,
-               double* __restrict__ merit) {
+    k_cd_merit(const double* __restrict__ sig, int n, const int* __restrict__ liveN,
+               const double* __restrict__ kernelMean, double alpha, double* clean, uint8_t* flags,
+               double* cs, double* cs2, double* __restrict__ merit) {
+  if(liveN) n = *liveN;
   __shared__ int warpTot[8];
   __shared__ int sTotal;
   __shared__ double sMean, sStd;
@@ -759,11 +763,13 @@ __global__ void __launch_bounds__(256)
 // list: a stamp advanced in the first pass has chi^2 = -1, which the second
 // pass can never reject, and a refill depends only on the new index.
 __global__ void __launch_bounds__(256)
-    k_ksc_check(const double* __restrict__ sig, int n, const int* __restrict__ count,
-                int* __restrict__ cur, double alpha, double sigKernFit, double* chi2,
-                uint8_t* flags, double* cs, double* cs2, int* __restrict__ refill,
+    k_ksc_check(const double* __restrict__ sig, int n, const int* __restrict__ liveN,
+                const int* __restrict__ count, int* __restrict__ cur, double alpha,
+                double sigKernFit, double* chi2, uint8_t* flags, double* cs, double* cs2,
+                int* __restrict__ refill,
                 int* __restrict__ out /* [0]=nRefill [1]=nPass1 [2]=nPass2 */,
                 int* __restrict__ passOf) {
+  if(liveN) n = *liveN;
   __shared__ int warpTot[8];
   __shared__ int sTotal;
   __shared__ double sMean, sStd;
@@ -869,31 +875,34 @@ static int2* kernelPowers(xb_ctx* c) {
   return d;
 }
 
-// matrix + RHS + LU + solve for the stamps in f.list (nList entries) of set
-// si, with the other image `other`; cpuRhs selects the ksc RHS form.
-static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int other, bool cpuRhs,
-                        double* dSol) {
+// matrix + RHS + LU + solve for the stamps list[0..nList) of set si, with
+// the other image `other`; cpuRhs selects the ksc RHS form.  liveN, when
+// set, holds the live length of the list on the device (nList bounds it).
+static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, const int* list, int nList,
+                        const int* liveN, int other, bool cpuRhs, double* dSol) {
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
+  const bool mixed = mixedMode(c);
+  if(!mixed) {  // the mixed build forms its spatial weights itself
   const int2* kp = kernelPowers(c);
   const int nW = nList * g.nComp2;
   { KT_SCOPE(c, "weights");
-  k_weights<<<(nW + 255) / 256, 256, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.ssxy, g.maxSS,
-                                                    kp, g.nComp2, c->w, c->h, f.wts);
+  k_weights<<<(nW + 255) / 256, 256, 0, c->stream>>>(list, nList, liveN, S.count, S.cur, S.ssxy,
+                                                    g.maxSS, kp, g.nComp2, c->w, c->h, f.wts);
   XB_LAUNCHED(c);
   }
-  const bool mixed = mixedMode(c);
+  }
   const double* dots = mixed ? S.dots : f.dots;  // mixed: filled per stamp by the Gram kernel
   if(nList > 0 && !mixed) {
     const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + g.wCols) * sizeof(double);
     { KT_SCOPE(c, "stamp_dots");
     if(c->imgIsF64)
       k_stamp_dots<double><<<nList, DOT_THREADS, smem, c->stream>>>(
-          f.list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
+          list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
           g.nBG, (const double*)c->img[other], c->w, c->h, f.dots, f.stride);
     else
       k_stamp_dots<float><<<nList, DOT_THREADS, smem, c->stream>>>(
-          f.list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
+          list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
           g.nBG, (const float*)c->img[other], c->w, c->h, f.dots, f.stride);
     XB_LAUNCHED(c);
     }
@@ -901,16 +910,16 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
   const int bgBase = g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + (cpuRhs ? g.nBG : 0);
   const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
   if(mixed) {
-    buildSystemMixed(c, si, f.list, nList, bgBase, f.M, dSol);
+    buildSystemMixed(c, si, list, nList, bgBase, f.M, dSol, liveN);
   } else {
   { KT_SCOPE(c, "build_matrix");
   k_build_matrix<<<(int)std::min<long long>((nTri + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
-      f.list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, dots, f.stride, mixed ? 1 : 0, g.nComp1,
+      list, nList, S.count, S.cur, S.Q, g.qCount, f.wts, dots, f.stride, mixed ? 1 : 0, g.nComp1,
       g.nComp2, g.nBG, g.matSize, f.M);
   XB_LAUNCHED(c);
   }
   { KT_SCOPE(c, "build_rhs");
-  k_build_rhs<<<(g.nSol + 127) / 128, 128, 0, c->stream>>>(f.list, nList, S.count, S.cur, S.B,
+  k_build_rhs<<<(g.nSol + 127) / 128, 128, 0, c->stream>>>(list, nList, S.count, S.cur, S.B,
                                                           g.qCount, f.wts, dots, f.stride,
                                                           mixed ? 1 : 0, bgBase, g.nComp1,
                                                           g.nComp2, g.nBG, g.nSol, dSol);
@@ -967,10 +976,10 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, int nList, int o
 }
 
 static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const double* dSol,
-                        int convImg, double* dSig) {
+                        int convImg, double* dSig, const int* liveN = nullptr) {
   if(nList <= 0) return;
   if(mixedMode(c)) {
-    sigsMixed(c, si, dList, nList, dSol, convImg, dSig);
+    sigsMixed(c, si, dList, nList, dSol, convImg, dSig, liveN);
     return;
   }
   const Geo& g = c->g;
@@ -1018,12 +1027,12 @@ void stageCd(xb_ctx* c) {
     StampSetDev& S = c->set[si];
     if(S.n > 0) {
       { KT_SCOPE(c, "stamp_test_fit");
-      k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, ks[si]);
+      k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, nullptr, ks[si]);
       XB_LAUNCHED(c);
       }
     }
     { KT_SCOPE(c, "cd_select");
-    k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, c->p.sigClipAlpha, c->p.sigKernFit,
+    k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, nullptr, c->p.sigClipAlpha, c->p.sigKernFit,
                                           f.flags, f.cs, f.cs2, testIdx[si], nTest + si,
                                           stats + 2 * si);
     XB_LAUNCHED(c);
@@ -1038,14 +1047,12 @@ void stageCd(xb_ctx* c) {
       c->merit[si] = 666;
       continue;
     }
-    XB_CUDA(cudaMemcpyAsync(f.list, testIdx[si], sizeof(int) * hT[si], cudaMemcpyDeviceToDevice,
-                            c->stream));
-    solveGlobal(c, si, f, hT[si], 1 - si, false, sol);
+    solveGlobal(c, si, f, testIdx[si], hT[si], nullptr, 1 - si, false, sol);
     kernelSumLaunch(c, sol, (0 - 0.5 * c->w) / (0.5 * c->w), (0 - 0.5 * c->h) / (0.5 * c->h), 1,
                     kMean + si);
-    computeSigs(c, si, f.list, hT[si], sol, si, f.sig);
+    computeSigs(c, si, testIdx[si], hT[si], sol, si, f.sig);
     { KT_SCOPE(c, "cd_merit");
-    k_cd_merit<<<1, 256, 0, c->stream>>>(f.sig, hT[si], kMean + si, c->p.sigClipAlpha,
+    k_cd_merit<<<1, 256, 0, c->stream>>>(f.sig, hT[si], nullptr, kMean + si, c->p.sigClipAlpha,
                                          f.scratchD, f.flags, f.cs, f.cs2, merit + si);
     XB_LAUNCHED(c);
     }
@@ -1086,14 +1093,12 @@ void stageKsc(xb_ctx* c) {
   int iteration = 0;
   bool check;
   do {
-    XB_CUDA(cudaMemcpyAsync(f.list, allList, sizeof(int) * std::max(n, 1), cudaMemcpyDeviceToDevice,
-                            c->stream));
-    solveGlobal(c, si, f, n, 1 - si, true, c->dSol);
+    solveGlobal(c, si, f, allList, n, nullptr, 1 - si, true, c->dSol);
     computeSigs(c, si, allList, n, c->dSol, si, f.sig);
     k_zero_ints<<<1, 32, 0, c->stream>>>(outs, 4);
     XB_LAUNCHED(c);
     { KT_SCOPE(c, "ksc_check");
-    k_ksc_check<<<1, 256, 0, c->stream>>>(f.sig, n, S.count, S.cur, c->p.sigClipAlpha,
+    k_ksc_check<<<1, 256, 0, c->stream>>>(f.sig, n, nullptr, S.count, S.cur, c->p.sigClipAlpha,
                                           c->p.sigKernFit, chi2, f.flags, f.cs, f.cs2, refill,
                                           outs, passOf);
     XB_LAUNCHED(c);
@@ -1124,6 +1129,85 @@ void stageKsc(xb_ctx* c) {
     c->put("cur", toHost(c, S.cur, n));
     c->put("solution", c->hSol);
   }
+}
+
+// cd as a frame graph captures it: the kept counts and the test-list
+// lengths stay on the device (S.n is the stamp-grid bound, S.dN the count);
+// each set's global test fit runs in a conditional node when its list is not
+// empty, and its merit is 666 otherwise (cdkscUtil.cpp:234-265).
+void stageCdGraph(xb_ctx* c, long long lCd[2]) {
+  const Geo& g = c->g;
+  const int nMax = std::max(std::max(c->set[0].n, c->set[1].n), 1);
+  FitBuffers f = fitBuffers(c, nMax);
+  double* ks[2] = {buf<double>(c, "cd_ks0", nMax), buf<double>(c, "cd_ks1", nMax)};
+  int* testIdx[2] = {buf<int>(c, "cd_test0", nMax), buf<int>(c, "cd_test1", nMax)};
+  int* nTest = buf<int>(c, "cd_ntest", 2);
+  double* stats = buf<double>(c, "cd_stats", 4);
+  double* dSolCd = buf<double>(c, "cd_sol", 2 * (size_t)std::max(g.nSol, g.matSize + 1));
+  double* kMean = buf<double>(c, "cd_kmean", 2);
+  double* merit = buf<double>(c, "cd_merit", 2);
+  const int qc = g.qCount;
+  const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
+  for(int si = 0; si < 2; si++) {
+    StampSetDev& S = c->set[si];
+    k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, S.dN, ks[si]);
+    XB_LAUNCHED(c);
+    k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, S.dN, c->p.sigClipAlpha, c->p.sigKernFit,
+                                          f.flags, f.cs, f.cs2, testIdx[si], nTest + si,
+                                          stats + 2 * si);
+    XB_LAUNCHED(c);
+  }
+  const int solStride = std::max(g.nSol, g.matSize + 1);
+  for(int si = 0; si < 2; si++) {
+    double* sol = dSolCd + (size_t)si * solStride;
+    const int bound = c->set[si].n;
+    graphSetDouble(c, merit + si, 666.0);
+    lCd[si] = graphIfPositive(c, nTest + si, 1, [&] {
+      solveGlobal(c, si, f, testIdx[si], bound, nTest + si, 1 - si, false, sol);
+      kernelSumLaunch(c, sol, (0 - 0.5 * c->w) / (0.5 * c->w), (0 - 0.5 * c->h) / (0.5 * c->h), 1,
+                      kMean + si);
+      computeSigs(c, si, testIdx[si], bound, sol, si, f.sig, nTest + si);
+      k_cd_merit<<<1, 256, 0, c->stream>>>(f.sig, bound, nTest + si, kMean + si,
+                                           c->p.sigClipAlpha, f.scratchD, f.flags, f.cs, f.cs2,
+                                           merit + si);
+      XB_LAUNCHED(c);
+    });
+  }
+}
+
+// ksc as a frame graph captures it: the reject-and-refit loop is a WHILE
+// node; each pass solves, checks, refills the rejected stamps (count on the
+// device) and continues while refills were made.
+long long stageKscGraph(xb_ctx* c) {
+  const Geo& g = c->g;
+  const int si = c->chosen;
+  StampSetDev& S = c->set[si];
+  const int n = std::max(S.n, 1);  // bound; the kept count is *S.dN
+  FitBuffers f = fitBuffers(c, n);
+  std::vector<int> all(n);
+  for(int s = 0; s < n; s++) all[s] = s;
+  int* allList = buf<int>(c, "ksc_all", n);
+  toDevice(c, allList, all);
+  int* refill = buf<int>(c, "ksc_refill", n);
+  int* passOf = buf<int>(c, "ksc_passof", n);
+  int* outs = buf<int>(c, "ksc_out", 4);
+  double* chi2 = buf<double>(c, "ksc_chi2", n);
+  c->dSol = buf<double>(c, "solution", std::max(g.nSol, g.matSize + 1));
+  k_zero_ints<<<1, 32, 0, c->stream>>>(graphRec(c) + 2, 2);  // iteration count, overflow
+  XB_LAUNCHED(c);
+  const int limit = 4 * n * g.maxSS + 8;
+  return graphWhile(c, [&](cudaGraphConditionalHandle h) {
+    solveGlobal(c, si, f, allList, n, S.dN, 1 - si, true, c->dSol);
+    computeSigs(c, si, allList, n, c->dSol, si, f.sig, S.dN);
+    k_zero_ints<<<1, 32, 0, c->stream>>>(outs, 4);
+    XB_LAUNCHED(c);
+    k_ksc_check<<<1, 256, 0, c->stream>>>(f.sig, n, S.dN, S.count, S.cur, c->p.sigClipAlpha,
+                                          c->p.sigKernFit, chi2, f.flags, f.cs, f.cs2, refill,
+                                          outs, passOf);
+    XB_LAUNCHED(c);
+    fillStamps(c, si, refill, n, si, outs);
+    graphKscContinue(c, h, outs, limit);
+  });
 }
 
 }  // namespace xb

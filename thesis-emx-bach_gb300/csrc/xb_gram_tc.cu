@@ -131,7 +131,7 @@ __device__ __forceinline__ void gtLd16(uint32_t taddr, float* v) {
 template <class T>
 __global__ void __launch_bounds__(GT_THREADS, 1)
     k_gram_tc(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
-              const int* __restrict__ count, const int* __restrict__ cur,
+              const int* __restrict__ liveN, const int* __restrict__ count, const int* __restrict__ cur,
               const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int ldW,
               const float* __restrict__ W, double* __restrict__ Gout, int* __restrict__ timeout) {
   extern __shared__ __align__(1024) unsigned char gt_s[];
@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
   __shared__ unsigned long long bars[2];
   __shared__ uint32_t tmemBase;
   __shared__ int sErr;
+  if(liveN && (int)blockIdx.x >= *liveN) return;  // before any barrier or TMEM allocation
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int fSS = 2 * hSS + 1, K = fSS * fSS, R = wRows + 1;
   const int nChunk = (K + GT_KC - 1) / GT_KC;
@@ -351,15 +352,16 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
 }
 
 template __global__ void k_gram_tc<float>(const float*, int, int, const int*, const int*,
-                                          const int*, const int2*, int, int, int, int,
+                                          const int*, const int*, const int2*, int, int, int, int,
                                           const float*, double*, int*);
 template __global__ void k_gram_tc<double>(const double*, int, int, const int*, const int*,
-                                           const int*, const int2*, int, int, int, int,
-                                           const float*, double*, int*);
+                                           const int*, const int*, const int2*, int, int, int,
+                                           int, const float*, double*, int*);
 
 // Launches the tensor-core Gram for nList stamps; false when the shape is
 // outside its limits (R > 64 rows), so the caller uses the FP64 kernel.
-bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G) {
+bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G,
+                     const int* liveN) {
   const Geo& g = c->g;
   const int R = g.wRows + 1;
   if(c->gramFp64 || R > GT_RB || g.wCols > 1024) return false;
@@ -369,14 +371,14 @@ bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, 
     XB_CUDA(cudaFuncSetAttribute(k_gram_tc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)GT_SMEM));
     k_gram_tc<double><<<nList, GT_THREADS, GT_SMEM, c->stream>>>(
-        (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-        g.wRows, mixedLd(g), S.Wf, G, err);
+        (const double*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
+        g.hSS, g.wRows, mixedLd(g), S.Wf, G, err);
   } else {
     XB_CUDA(cudaFuncSetAttribute(k_gram_tc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)GT_SMEM));
     k_gram_tc<float><<<nList, GT_THREADS, GT_SMEM, c->stream>>>(
-        (const float*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-        g.wRows, mixedLd(g), S.Wf, G, err);
+        (const float*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
+        g.hSS, g.wRows, mixedLd(g), S.Wf, G, err);
   }
   XB_LAUNCHED(c);
   return true;

@@ -73,7 +73,7 @@ struct StampSetDev {
   double* B = nullptr;       // n * bCount
   float* Wf = nullptr;       // mixed mode: FP32 W [n][wRows][ld], ld = wCols padded to 32
   double* dots = nullptr;    // mixed mode: per-stamp dot table of the global matrix
-  std::vector<int> h_count, h_cur;
+  const int* dN = nullptr;   // frame graphs: the kept count on the device (n is its bound)
 };
 
 // Optional per-kernel CUDA-event timing (option "time_kernels"): launches
@@ -93,6 +93,8 @@ struct DevBuf {  // simple grow-only device allocation
   void* p = nullptr;
   size_t bytes = 0;
 };
+
+struct FrameGraphs;  // xb_graph.cu
 
 }  // namespace xb
 
@@ -159,6 +161,17 @@ struct xb_ctx {
   int autotune = 1;      // time the variants of tunable kernels on first use
   int tuneForce = -1;    // >= 0: launch this variant of every tunable kernel
   float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
+  int mxTables = 0;        // the mixed build's monomial tables are on the device
+  // frame graphs (xb_graph.cu)
+  int graph = 0;           // option "graph": whole frames replay as captured CUDA graphs
+  int capturing = 0;       // stage code is being captured: no host reads, no timers
+  int keepBuffers = 0;     // graphs hold pool pointers: a grown buffer is retired, not freed
+  std::vector<void*> retired;
+  cudaStream_t upStream = nullptr;              // uploads made while capturing
+  std::vector<cudaStream_t> bodyStreams;        // conditional-body capture, one per depth
+  int bodyDepth = 0;
+  long long graphRetryLaunches = 0;             // launches of the captured sss retry
+  xb::FrameGraphs* graphs = nullptr;            // instantiated graphs by frame shape
   xb::KTimers kt;
   std::string lastError;
   std::map<std::string, std::vector<uint8_t>> arrays;
@@ -217,11 +230,18 @@ std::vector<T> toHost(xb_ctx* c, const T* d, size_t n) {
   XB_CUDA(cudaStreamSynchronize(c->stream));
   return h;
 }
+// Host tables for the device.  While a frame graph is being captured the
+// copy runs at once on a side stream (the tables are fixed for the frame
+// shape, so replays need no copy node).
+void uploadNow(xb_ctx* c, void* d, const void* h, size_t bytes);
 template <class T>
 void toDevice(xb_ctx* c, T* d, const std::vector<T>& h) {
-  if(!h.empty())
-    XB_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T),
-                            cudaMemcpyHostToDevice, c->stream));
+  if(h.empty()) return;
+  if(c->capturing) {
+    uploadNow(c, d, h.data(), h.size() * sizeof(T));
+    return;
+  }
+  XB_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
 }
 
 // ---- kernel timers --------------------------------------------------------
@@ -232,7 +252,7 @@ struct KtScope {
   const char* name;
   cudaEvent_t a = nullptr;
   KtScope(xb_ctx* ctx, const char* n) : c(ctx), name(n) {
-    if(c->timeKernels) {
+    if(c->timeKernels && !c->capturing) {
       a = ktEvent(c);
       cudaEventRecord(a, c->stream);
     }
@@ -253,7 +273,9 @@ struct KtScope {
 void stageInitMask(xb_ctx* c);
 void stageSss(xb_ctx* c);
 void stageCmv(xb_ctx* c);
-void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
+// liveN (device, optional): the live length of dList; nList bounds it.
+void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
+                const int* liveN = nullptr);
 void stageCd(xb_ctx* c);
 void stageKsc(xb_ctx* c);
 void stageConvSub(xb_ctx* c, bool doSub);
@@ -261,14 +283,15 @@ void stageConvSub(xb_ctx* c, bool doSub);
 // mixed-precision stages (xb_mixed.cu)
 int mixedLd(const Geo& g);
 int mixedDotStride(const Geo& g);
-void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv);
+void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
+                     const int* liveN = nullptr);
 void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSol, int convImg,
-               double* dSig);
+               double* dSig, const int* liveN = nullptr);
 void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, int* piv,
                      int* singular, const int* status);
 void convSubMixed(xb_ctx* c, double* dKernSum);
 void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase, double* M,
-                      double* rhs);
+                      double* rhs, const int* liveN = nullptr);
 
 // global system of the mixed path (xb_ldl.cu): LDL^T on a cluster, refined
 // solve, pivoted LU when a pivot fails.  M is kept; rhs becomes the solution.
@@ -288,8 +311,33 @@ int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
 void rankSubstamps(xb_ctx* c);
 // Tensor-core Gram of the mixed path (xb_gram_tc.cu) into G (nList x R x R);
 // false when the shape is outside its limits.
-bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G);
+bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G,
+                     const int* liveN = nullptr);
 inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
+
+// ---- frame graphs (xb_graph.cu) -------------------------------------------
+// Capture helpers for stage code running under c->capturing: a conditional
+// handle of the graph being captured, a conditional node whose body is
+// captured from body() (returns the launches captured in it), and the
+// device-side setters of the stage decisions.
+cudaGraphConditionalHandle graphHandle(xb_ctx* c, unsigned dflt);
+long long graphBody(xb_ctx* c, cudaGraphConditionalHandle h, bool loop,
+                    const std::function<void()>& body);
+void graphSssRetry(xb_ctx* c, const int* nKept, int nAll, const std::function<void()>& body);
+long long graphIfPositive(xb_ctx* c, const int* v, int n, const std::function<void()>& body);
+void graphSetDouble(xb_ctx* c, double* p, double v);
+long long graphWhile(xb_ctx* c, const std::function<void(cudaGraphConditionalHandle)>& body);
+void graphKscContinue(xb_ctx* c, cudaGraphConditionalHandle h, const int* outs, int limit);
+int* graphRec(xb_ctx* c);
+// One frame pair, device to device (graph replay when c->graph is set).
+void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, float* dConv,
+                    float* dDiff);
+void destroyGraphs(xb_ctx* c);
+// cd and ksc as captured by a frame graph (xb_fit.cu): lCd gets the launches
+// of each set's conditional test fit; stageKscGraph returns the launches of
+// one refit pass.
+void stageCdGraph(xb_ctx* c, long long lCd[2]);
+long long stageKscGraph(xb_ctx* c);
 
 // Kernel image at normalised position (xf, yf) and its sum into *dOut
 // (device): tree = 1 sums in 32-wide groups (cl_kern/cd.cl:419-442), tree = 0

@@ -546,7 +546,11 @@ cudaError_t launchCluster(xb_ctx* c, Kern kernel, int CL, int threads, size_t sm
 int* deviceStatus(xb_ctx* c) {
   const bool fresh = c->pool.find("ldl_status") == c->pool.end();
   int* status = buf<int>(c, "ldl_status", 2);
-  if(fresh) XB_CUDA(cudaMemsetAsync(status, 0, 2 * sizeof(int), c->stream));
+  if(fresh) {
+    const int zero[2] = {0, 0};
+    if(c->capturing) uploadNow(c, status, zero, sizeof(zero));
+    else XB_CUDA(cudaMemsetAsync(status, 0, 2 * sizeof(int), c->stream));
+  }
   return status;
 }
 

@@ -42,12 +42,13 @@ __device__ __forceinline__ float floatNormF(int x, int w) {
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
     k_fill_w_f32(const T* __restrict__ img, int w, int h, const int* __restrict__ list,
-                 const int* __restrict__ count, const int* __restrict__ cur,
+                 const int* __restrict__ liveN, const int* __restrict__ count, const int* __restrict__ cur,
                  const int2* __restrict__ ssxy, int maxSS, const double* __restrict__ fX,
                  const double* __restrict__ fY, const int* __restrict__ gStart,
                  const int* __restrict__ gMembers, int hSS, int hK, int wRows, int ldW,
                  float* __restrict__ W) {
   extern __shared__ float fw_s[];
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int s = list[blockIdx.x], gi = blockIdx.y, tid = threadIdx.x;
   const int fK = 2 * hK + 1, fSS = 2 * hSS + 1, wCols = fSS * fSS;
   const int xHalf = hSS + hK, tw = 2 * xHalf + 1, th = fSS;
@@ -98,11 +99,13 @@ __global__ void __launch_bounds__(MX_THREADS)
 
 // convStampOdd and convStampBg in FP32; pads the background rows.
 __global__ void __launch_bounds__(MX_THREADS)
-    k_fill_finish_f32(const int* __restrict__ list, const int* __restrict__ count,
+    k_fill_finish_f32(const int* __restrict__ list, const int* __restrict__ liveN,
+                      const int* __restrict__ count,
                       const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                       const int* __restrict__ kx, const int* __restrict__ ky, int nPSF,
                       const int2* __restrict__ bgXY, int nBG, int hSS, int w, int h, int wRows,
                       int ldW, float* __restrict__ W) {
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int s = list[blockIdx.x], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS;
   float* Ws = W + (size_t)s * wRows * ldW;
@@ -139,10 +142,11 @@ constexpr int GM_KT = 32, GM_SPLIT = 6;
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
     k_gram_mixed(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
-                 const int* __restrict__ count, const int* __restrict__ cur,
+                 const int* __restrict__ liveN, const int* __restrict__ count, const int* __restrict__ cur,
                  const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int ldW,
                  const float* __restrict__ W, double* __restrict__ Gout) {
   extern __shared__ double gm_s[];
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS, R = wRows + 1;
   const int nEnt = R * (R + 1) / 2;
@@ -195,10 +199,12 @@ __global__ void __launch_bounds__(MX_THREADS)
 }
 
 __global__ void __launch_bounds__(MX_THREADS)
-    k_gram_scatter(const int* __restrict__ list, const int* __restrict__ count,
+    k_gram_scatter(const int* __restrict__ list, const int* __restrict__ liveN,
+                   const int* __restrict__ count,
                    const int* __restrict__ cur, int wRows, int nPSF, int nBG, int qc,
                    const double* __restrict__ Gin, double* __restrict__ Q,
                    double* __restrict__ B, double* __restrict__ dots, int stride) {
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x, R = wRows + 1;
   const double* G = Gin + (size_t)t * R * R;
   const bool live = cur[s] < count[s];
@@ -231,7 +237,8 @@ __global__ void __launch_bounds__(MX_THREADS)
 // ---------------------------------------------------- chi^2, FP32 model ---
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
-    k_sigs_f32(const int* __restrict__ list, const int* __restrict__ count,
+    k_sigs_f32(const int* __restrict__ list, const int* __restrict__ liveN,
+               const int* __restrict__ count,
                const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                const float* __restrict__ W, int wRows, int ldW, int hSS, int nPSF, int kOrder,
                int bgOrder, int nComp, const double* __restrict__ sol, const T* __restrict__ tImg,
@@ -241,6 +248,7 @@ __global__ void __launch_bounds__(MX_THREADS)
   __shared__ double sBg;
   __shared__ double rs[MX_THREADS / 32];
   __shared__ int rc[MX_THREADS / 32];
+  if(liveN && (int)blockIdx.x >= *liveN) return;
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, pix = fSS * fSS;
   const bool live = cur[s] < count[s];
@@ -765,7 +773,8 @@ constexpr int MXB_ROWS = 64, MXB_T = 32, MXB_MAXC = 32;
 __device__ __forceinline__ int mxPairRow(int qa, int qb) { return (qa - 1) * qa / 2 - 1 + (qb - 1); }
 
 __global__ void __launch_bounds__(256)
-    k_mx_build(const int* __restrict__ list, int nList, const int* __restrict__ count,
+    k_mx_build(const int* __restrict__ list, int nList, const int* __restrict__ liveN,
+               const int* __restrict__ count,
                const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                const double* __restrict__ Q, int qc, const double* __restrict__ dots, int stride,
                const double* __restrict__ B, const int2* __restrict__ monoExp, int nMono, int w,
@@ -773,7 +782,9 @@ __global__ void __launch_bounds__(256)
   __shared__ double Xs[MXB_ROWS][MXB_T + 1];
   __shared__ double Ys[MXB_T][MXB_MAXC];
   __shared__ int sS[MXB_T];
+  if(liveN) nList = min(nList, *liveN);
   const int tid = threadIdx.x, split = blockIdx.y, t0 = split * MXB_T;
+  if(t0 >= nList && split > 0) return;  // split 0 writes zeros for an empty list
   const int nt = min(MXB_T, nList - t0), row0 = blockIdx.x * MXB_ROWS, NC = nMono + 1;
   const int nQP = mxPairRow(nC1 + 2, 1);  // Q pairs
   if(tid < MXB_T) sS[tid] = tid < nt ? list[t0 + tid] : -1;
@@ -834,10 +845,13 @@ __global__ void __launch_bounds__(256)
 // Lower triangle of the global matrix (mirrored), row/column 0 zeroed, and
 // the RHS (nSol entries; bgBase selects the background projection form).
 __global__ void __launch_bounds__(256)
-    k_mx_scatter(const double* __restrict__ P, int nSplit, int nRows, int nMono,
-                 const int2* __restrict__ kp, const int* __restrict__ monoIdx, int monoDim,
-                 int nC1, int nC2, int nBG, int stride, int bgBase, int matSize, int nSol,
-                 double* __restrict__ M, double* __restrict__ rhs) {
+    k_mx_scatter(const double* __restrict__ P, int nSplit, const int* __restrict__ liveN,
+                 int nRows, int nMono, const int2* __restrict__ kp,
+                 const int* __restrict__ monoIdx, int monoDim, int nC1, int nC2, int nBG,
+                 int stride, int bgBase, int matSize, int nSol, double* __restrict__ M,
+                 double* __restrict__ rhs) {
+  // live stamps on the device: only their splits hold partial sums
+  if(liveN) nSplit = min(nSplit, (*liveN + MXB_T - 1) / MXB_T);
   const int ld = matSize + 1, nComp = nC1 * nC2, NC = nMono + 1;
   const int nQP = mxPairRow(nC1 + 2, 1), dotRow0 = nQP + 1, bRow0 = nQP + 1 + stride;
   const long long nTri = (long long)matSize * (matSize + 1) / 2;
@@ -907,7 +921,8 @@ int mixedLd(const Geo& g) { return (g.wCols + 31) / 32 * 32; }
 
 int mixedDotStride(const Geo& g) { return g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG + 2 * g.nBG; }
 
-void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv) {
+void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
+                     const int* liveN) {
   if(nList <= 0) return;
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
@@ -921,18 +936,18 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     dim3 grid(nList, nGroups);
     if(c->imgIsF64)
       k_fill_w_f32<double><<<grid, MX_THREADS, smemFill, c->stream>>>(
-          (const double*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS,
-          c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+          (const double*)c->img[imgConv], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy,
+          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
     else
       k_fill_w_f32<float><<<grid, MX_THREADS, smemFill, c->stream>>>(
-          (const float*)c->img[imgConv], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS,
-          c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+          (const float*)c->img[imgConv], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy,
+          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
     XB_LAUNCHED(c);
   }
   {
     KT_SCOPE(c, "fill_finish");
     k_fill_finish_f32<<<nList, MX_THREADS, 0, c->stream>>>(
-        dList, S.count, S.cur, S.ssxy, g.maxSS, c->dKx, c->dKy, g.nPSF, buf<int2>(c, "bgXY", g.nBG),
+        dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, c->dKx, c->dKy, g.nPSF, buf<int2>(c, "bgXY", g.nBG),
         g.nBG, g.hSS, c->w, c->h, g.wRows, ldW, S.Wf);
     XB_LAUNCHED(c);
   }
@@ -944,26 +959,26 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     const int split = std::max(GM_SPLIT, (R * (R + 1) / 2 + MX_THREADS - 1) / MX_THREADS);
     double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
     dim3 grid(nList, split);
-    if(gramTensorCores(c, si, dList, nList, other, G)) {
+    if(gramTensorCores(c, si, dList, nList, other, G, liveN)) {
       // exact tensor-core Gram (xb_gram_tc.cu)
     } else if(c->imgIsF64)
       k_gram_mixed<double><<<grid, MX_THREADS, smem, c->stream>>>(
-          (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-          g.wRows, ldW, S.Wf, G);
+          (const double*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
+          g.hSS, g.wRows, ldW, S.Wf, G);
     else
       k_gram_mixed<float><<<grid, MX_THREADS, smem, c->stream>>>(
-          (const float*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-          g.wRows, ldW, S.Wf, G);
+          (const float*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
+          g.hSS, g.wRows, ldW, S.Wf, G);
     XB_LAUNCHED(c);
-    k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, S.count, S.cur, g.wRows, g.nPSF,
-                                                        g.nBG, g.qCount, G, S.Q, S.B, S.dots,
-                                                        mixedDotStride(g));
+    k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, liveN, S.count, S.cur, g.wRows,
+                                                        g.nPSF, g.nBG, g.qCount, G, S.Q, S.B,
+                                                        S.dots, mixedDotStride(g));
     XB_LAUNCHED(c);
   }
 }
 
 void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSol, int convImg,
-               double* dSig) {
+               double* dSig, const int* liveN) {
   if(nList <= 0) return;
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
@@ -971,12 +986,12 @@ void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSo
   KT_SCOPE(c, "sigs");
   if(c->imgIsF64)
     k_sigs_f32<double><<<nList, MX_THREADS, 0, c->stream>>>(
-        dList, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
+        dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const double*)c->img[convImg],
         (const double*)c->img[other], c->mask, c->w, c->h, dSig);
   else
     k_sigs_f32<float><<<nList, MX_THREADS, 0, c->stream>>>(
-        dList, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
+        dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const float*)c->img[convImg],
         (const float*)c->img[other], c->mask, c->w, c->h, dSig);
   XB_LAUNCHED(c);
@@ -1034,28 +1049,33 @@ void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, 
 // Global matrix and RHS of the mixed path for the stamps list[0..nList) of
 // set si (weights from the current substamps, W dots per stamp).
 void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase, double* M,
-                      double* rhs) {
+                      double* rhs, const int* liveN) {
   const Geo& g = c->g;
   StampSetDev& S = c->set[si];
   const int K = c->p.kernelOrder, monoDim = 2 * K + 1;
   const int nMono = triNum(2 * K + 1);
   if(nMono + 1 > MXB_MAXC)
     throw XbError{XB_ERR_UNSUPPORTED, "kernel order too high for the mixed build"};
-  std::vector<int2> mexp;
-  std::vector<int> midx(monoDim * monoDim, 0);
-  for(int a = 0; a <= 2 * K; a++)
-    for(int b = 0; a + b <= 2 * K; b++) {
-      midx[a * monoDim + b] = (int)mexp.size();
-      mexp.push_back(make_int2(a, b));
-    }
-  std::vector<int2> kp(g.nComp2);
-  for(int k = 0; k < g.nComp2; k++) kp[k] = make_int2(c->basis.kpX[k], c->basis.kpY[k]);
-  int2* dExp = buf<int2>(c, "mx_exp", mexp.size());
-  int* dIdx = buf<int>(c, "mx_idx", midx.size());
-  int2* dKp = buf<int2>(c, "mx_kp", kp.size());
-  toDevice(c, dExp, mexp);
-  toDevice(c, dIdx, midx);
-  toDevice(c, dKp, kp);
+  // monomial exponents, their index table and the kernel powers: fixed by
+  // the parameters, uploaded once per context
+  int2* dExp = buf<int2>(c, "mx_exp", nMono);
+  int* dIdx = buf<int>(c, "mx_idx", (size_t)monoDim * monoDim);
+  int2* dKp = buf<int2>(c, "mx_kp", g.nComp2);
+  if(!c->mxTables) {
+    std::vector<int2> mexp;
+    std::vector<int> midx(monoDim * monoDim, 0);
+    for(int a = 0; a <= 2 * K; a++)
+      for(int b = 0; a + b <= 2 * K; b++) {
+        midx[a * monoDim + b] = (int)mexp.size();
+        mexp.push_back(make_int2(a, b));
+      }
+    std::vector<int2> kp(g.nComp2);
+    for(int k = 0; k < g.nComp2; k++) kp[k] = make_int2(c->basis.kpX[k], c->basis.kpY[k]);
+    toDevice(c, dExp, mexp);
+    toDevice(c, dIdx, midx);
+    toDevice(c, dKp, kp);
+    c->mxTables = 1;
+  }
   const int stride = mixedDotStride(g);
   const int nQP = (g.nComp1 + 1) * (g.nComp1 + 2) / 2 - 1;
   const int nRows = nQP + 1 + stride + g.nComp1 + 1;
@@ -1064,8 +1084,8 @@ void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase
   if(nSplit > 0) {
     KT_SCOPE(c, "mx_build");
     k_mx_build<<<dim3((nRows + MXB_ROWS - 1) / MXB_ROWS, nSplit), 256, 0, c->stream>>>(
-        dList, nList, S.count, S.cur, S.ssxy, g.maxSS, S.Q, g.qCount, S.dots, stride, S.B, dExp,
-        nMono, c->w, c->h, g.nComp1, nRows, P);
+        dList, nList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Q, g.qCount, S.dots, stride, S.B,
+        dExp, nMono, c->w, c->h, g.nComp1, nRows, P);
     XB_LAUNCHED(c);
   }
   {
@@ -1073,7 +1093,7 @@ void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase
     const long long nTri = (long long)g.matSize * (g.matSize + 1) / 2;
     const long long total = nTri + g.nSol + g.matSize + 1;
     k_mx_scatter<<<(int)std::min<long long>((total + 255) / 256, (long long)c->smCount * 4), 256,
-                   0, c->stream>>>(P, nSplit, nRows, nMono, dKp, dIdx, monoDim, g.nComp1,
+                   0, c->stream>>>(P, nSplit, liveN, nRows, nMono, dKp, dIdx, monoDim, g.nComp1,
                                    g.nComp2, g.nBG, stride, bgBase, g.matSize, g.nSol, M, rhs);
     XB_LAUNCHED(c);
   }

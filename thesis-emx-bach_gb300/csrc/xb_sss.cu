@@ -1111,6 +1111,18 @@ __global__ void __launch_bounds__(256)
   if(threadIdx.x == 0) *nOut = done;
 }
 
+// createStampBounds (sss.cl:86-105) on the device, for frame graphs: the
+// same integer expressions as the host table of stageSss.
+__global__ void k_stamp_geom(int4* __restrict__ geom, int nAll, int stampsx, int stampsy, int w,
+                             int h, int fSW) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if(id >= nAll) return;
+  const int sxI = id % stampsx, syI = id / stampsx;
+  const int startX = sxI * w / stampsx, startY = syI * h / stampsy;
+  const int stopX = min(startX + fSW, w), stopY = min(startY + fSW, h);
+  geom[id] = make_int4(startX, startY, stopX - startX, stopY - startY);
+}
+
 __global__ void k_reset_skip(uint16_t* mask, long long n) {
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (long long)gridDim.x * blockDim.x)
@@ -1196,6 +1208,7 @@ static void sssPass(xb_ctx* c, int* nKept) {
     XB_LAUNCHED(c);
     }
   }
+  if(c->capturing) return;  // frame graphs keep the counts on the device
   std::vector<int> n = toHost(c, c->dIWork, 2);
   nKept[0] = n[0];
   nKept[1] = n[1];
@@ -1254,8 +1267,32 @@ void stageSss(xb_ctx* c) {
   const size_t chunkDoubles = (size_t)nAll * 2 * ((fSW * fSW + 31) / 32);
   c->dWork = buf<double>(c, "chunkScratch", chunkDoubles);
   c->dIWork = buf<int>(c, "iwork", 64);
-  toDevice(c, c->geomAll, geom);
   int nKept[2];
+  if(c->capturing) {
+    // frame graph: the grid is computed on the device (the upload would be a
+    // per-shape constant), the retry is a conditional node on the counts
+    k_stamp_geom<<<(nAll + 255) / 256, 256, 0, c->stream>>>(c->geomAll, nAll, c->stampsx,
+                                                            c->stampsy, w, h, fSW);
+    XB_LAUNCHED(c);
+    sssPass(c, nKept);
+    graphSssRetry(c, c->dIWork, nAll, [&] {
+      const long long n = (long long)w * h;
+      k_reset_skip<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
+          c->mask, n);
+      XB_LAUNCHED(c);
+      sssPass(c, nKept);
+    });
+    for(int im = 0; im < 2; im++) {
+      c->set[im].n = nAll;  // bound; the kept count is dIWork[im]
+      c->set[im].dN = c->dIWork + im;
+    }
+    c->scalars["stampsx"] = c->stampsx;
+    c->scalars["stampsy"] = c->stampsy;
+    c->scalars["fStampWidth"] = c->fStampWidth;
+    return;
+  }
+  c->set[0].dN = c->set[1].dN = nullptr;
+  toDevice(c, c->geomAll, geom);
   sssPass(c, nKept);
   const int oldCount = nAll;
   const double fT = (double)nKept[0] / oldCount, fS = (double)nKept[1] / oldCount;
@@ -1272,11 +1309,6 @@ void stageSss(xb_ctx* c) {
   c->set[0].n = nKept[0];
   c->set[1].n = nKept[1];
   if(nKept[0] == 0 && nKept[1] == 0) throw XbError{XB_ERR_NO_SUBSTAMPS, "No substamps found"};
-  for(int im = 0; im < 2; im++) {
-    StampSetDev& S = c->set[im];
-    S.h_count = toHost(c, S.count, S.n);
-    S.h_cur.assign(S.n, 0);
-  }
   if(c->rank && c->rankW) rankSubstamps(c);  // learned order of each stamp's substamps
   if(c->trace) {
     for(int im = 0; im < 2; im++) {

@@ -55,6 +55,12 @@ int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
   if(!c->autotune || nVariants <= 1) return 0;
   const std::string key = std::string(kernel) + "@dev" + std::to_string(c->device) + ":" +
                           std::to_string(shape);
+  if(c->capturing) {  // a graph being captured cannot time: the table's choice or variant 0
+    std::lock_guard<std::mutex> lk(gMu);
+    loadCacheLocked();
+    auto it = gTable.find(key);
+    return it != gTable.end() && it->second >= 0 ? it->second : 0;
+  }
   {
     std::lock_guard<std::mutex> lk(gMu);
     loadCacheLocked();

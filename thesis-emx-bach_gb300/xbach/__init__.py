@@ -54,7 +54,7 @@ EXPORTS = [
     "xb_params_default", "xb_params_npsf", "xb_ctx_create", "xb_ctx_destroy",
     "xb_last_error", "xb_set_option", "xb_init", "xb_init_f32",
     "xb_init_device_f32", "xb_sss", "xb_cmv", "xb_cd", "xb_ksc", "xb_conv",
-    "xb_sub", "xb_run", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
+    "xb_sub", "xb_run", "xb_run_device", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
     "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
     "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc", "xb_batch_create",
@@ -89,6 +89,7 @@ def lib():
     L.xb_cd.argtypes = [vp, P(i)]
     L.xb_conv.argtypes = [vp, P(d)]
     L.xb_run.argtypes = [vp, vp, vp, i, i, vp, vp]
+    L.xb_run_device.argtypes = [vp, vp, vp, i, i, vp, vp]
     L.xb_get_image.argtypes = [vp, i, vp]
     L.xb_get_image_f64.argtypes = [vp, i, vp]
     L.xb_get_mask.argtypes = [vp, vp]
@@ -202,6 +203,24 @@ class Context:
     def sub(self):
         return self._check(self.L.xb_sub(self.h))
 
+    def run(self, T, S):
+        """init..sub through xb_run (FP32 (h, w) arrays; the frame-graph path
+        when option "graph" is on); results via image()."""
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        S = np.ascontiguousarray(S, dtype=np.float32)
+        if T.shape != S.shape:
+            raise ValueError("template and science differ in shape")
+        h, w = T.shape
+        return self._check(self.L.xb_run(self.h, T.ctypes.data, S.ctypes.data, w, h, None, None))
+
+    def run_device(self, dT, dS, w, h, dConv=None, dDiff=None):
+        """init..sub from device FP32 images (pointers as ints) into optional
+        device outputs, through xb_run_device."""
+        vp = ctypes.c_void_p
+        return self._check(self.L.xb_run_device(self.h, vp(dT), vp(dS), w, h,
+                                                vp(dConv) if dConv else None,
+                                                vp(dDiff) if dDiff else None))
+
     def run_all(self, T, S):
         self.init(T, S)
         self.sss()
@@ -312,6 +331,11 @@ class Batch:
         """Join a cudaStream_t handle (int) to later runs (0 detaches)."""
         if self.L.xb_batch_set_stream(self.h, ctypes.c_void_p(stream or None)):
             raise XbError(5, "xb_batch_set_stream failed")
+
+    def set_option(self, name, value):
+        """xb_set_option on every worker context (e.g. "graph")."""
+        for i in range(self.n_workers):
+            self.worker(i).set_option(name, value)
 
     def worker(self, i):
         c = ctypes.c_void_p()
