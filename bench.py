@@ -16,6 +16,12 @@ before every step, max over ranks.  e2e: the same through xb_run() with the
 host->device copy of both FP32 inputs from pinned memory and the
 device->host read of the conv and diff images inside the timed region.
 
+The headline runs 16 frame pairs per step on 16 worker contexts, each frame
+replayed as one captured CUDA graph (--graph 1).  The process asks for 32
+hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS, set before CUDA starts):
+with the default 8, the workers' streams share queues and their graphs
+serialise.
+
 N > 1 (torchrun): replicas - every rank runs its own frame pairs on its own
 GPU; the only cross-rank traffic is the barrier and the max of the timings.
 
@@ -34,6 +40,10 @@ import subprocess
 import sys
 import tempfile
 import time
+
+# concurrent frame graphs need their own hardware queues (read when the CUDA
+# context is created, so before torch touches the device)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 REPO = pathlib.Path(__file__).resolve().parent
 PKG = REPO / "thesis-emx-bach_gb300"
@@ -211,11 +221,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"],
                     help="mixed = the chosen pipeline (headline); plain = the FP64 path alone")
-    ap.add_argument("--batch", type=int, default=8,
+    ap.add_argument("--batch", type=int, default=16,
                     help="frame pairs per step, run concurrently (1 = one pair per step)")
-    ap.add_argument("--workers", type=int, default=8, help="concurrent frames of a batch")
+    ap.add_argument("--workers", type=int, default=16, help="concurrent frames of a batch")
     ap.add_argument("--cpu-runs", type=int, default=2)
+    ap.add_argument("--graph", type=int, default=1,
+                    help="mixed mode: replay every frame as one captured CUDA graph (1) or run "
+                         "the stages host-driven (0)")
     args = ap.parse_args()
+    use_graph = bool(args.graph) and args.mode == "mixed"
     if args.impl == "reference":
         return run_reference(args)
 
@@ -303,6 +317,26 @@ def main():
             kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}
     ctx.set_option("time_kernels", 0)
     single_value = world * args.steps / (single_ms / 1000.0)
+    single_graph = None
+    if use_graph:
+        # the same frame as a replayed graph (one launch, one synchronisation)
+        gctx = xbach.Context(params, device=local)
+        gctx.set_option("graph", 1)
+        gC = torch.empty((h, w), dtype=torch.float32, device="cuda")
+        gD = torch.empty((h, w), dtype=torch.float32, device="cuda")
+
+        def single_g():
+            gctx.run_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h, gC.data_ptr(),
+                            gD.data_ptr())
+        for _ in range(max(args.warmup, 2)):
+            single_g()
+        torch.cuda.synchronize()
+        gl0 = gctx.launches()
+        g_ms = max_over_ranks(timed(single_g, torch.cuda.ExternalStream(gctx.stream()),
+                                    args.steps))
+        single_graph = {"value": world * args.steps / (g_ms / 1000.0), "unit": UNIT,
+                        "ms_per_step": g_ms / args.steps,
+                        "gpu_launches": (gctx.launches() - gl0) / args.steps}
 
     # ---- the headline: B frame pairs per step through the batch API ----
     jst = torch.cuda.Stream()
@@ -311,6 +345,13 @@ def main():
         batch.set_stream(jst.cuda_stream)
         dC = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
         dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
+        if use_graph:
+            # every worker captures its graph before the timed steps
+            batch.set_option("graph", 1)
+            for i in range(batch.n_workers):
+                batch.worker(i).run_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h,
+                                           dC[0].data_ptr(), dD[0].data_ptr())
+            torch.cuda.synchronize()
 
         def run_batch():
             batch.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], [w] * B,
@@ -379,10 +420,14 @@ def main():
                    "frames_per_step": B, "concurrent_frames": min(args.workers, B) if B > 1 else 1,
                    "parallelism": f"replicas x{world}",
                    "l2": "flushed before every step (256 MB write); each step's inputs exceed L2",
-                   "inputs": "device-resident FP32 T,S"},
+                   "inputs": "device-resident FP32 T,S",
+                   "frame_graphs": use_graph,
+                   "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
         "single_frame": {"value": single_value, "unit": UNIT,
-                         "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single},
+                         "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single,
+                         "path": "stages, host-driven (per-kernel timers on)"},
+        "single_frame_graph": single_graph,
         "dominant_kernel": dominant, "kernels": kernels,
     }
     oracle_res = None

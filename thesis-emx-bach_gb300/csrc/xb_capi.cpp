@@ -288,26 +288,19 @@ int xb_run_device(xb_ctx* c, const float* dT, const float* dS, int w, int h, flo
                   float* dDiff) {
   return guarded(c, [&] {
     if(!dT || !dS || w <= 0 || h <= 0) throw XbError{XB_ERR_ARG, "bad image"};
-    runFrameDevice(c, dT, dS, w, h, dConv, dDiff);
+    runFrame(c, dT, dS, w, h, dConv, dDiff, false);
   });
 }
 
 int xb_run(xb_ctx* c, const float* T, const float* S, int w, int h, float* convOut,
            float* diffOut) {
   if(c && c->graph && mixedMode(c)) {
-    // frame graph: inputs to the device, one replay, outputs back
-    int rc = guarded(c, [&] {
+    // frame graph: inputs straight into the graph's images, one replay,
+    // outputs straight back
+    return guarded(c, [&] {
       if(!T || !S || w <= 0 || h <= 0) throw XbError{XB_ERR_ARG, "bad image"};
-      const size_t n = (size_t)w * h;
-      float* dT = buf<float>(c, "run_in0", n);
-      float* dS = buf<float>(c, "run_in1", n);
-      XB_CUDA(cudaMemcpyAsync(dT, T, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-      XB_CUDA(cudaMemcpyAsync(dS, S, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-      runFrameDevice(c, dT, dS, w, h, nullptr, nullptr);
+      runFrame(c, T, S, w, h, convOut, diffOut, true);
     });
-    if(rc == XB_OK && convOut) rc = xb_get_image(c, XB_IMG_CONV, convOut);
-    if(rc == XB_OK && diffOut) rc = xb_get_image(c, XB_IMG_DIFF, diffOut);
-    return rc;
   }
   int rc = xb_init_f32(c, T, w, h, S, w, h);
   if(rc == XB_OK) rc = xb_sss(c);

@@ -415,12 +415,26 @@ static void captureFrame(xb_ctx* c, FrameGraph& fg) {
   (void)g;
 }
 
-// Frame pair from device buffers to device buffers; with c->graph set the
-// frame goes through the graph of its shape (captured on first use).
-void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, float* dConv,
-                    float* dDiff) {
+// One frame pair from T,S to conv,diff (device buffers, or host buffers
+// when host is set; conv/diff may be null).  With c->graph set the frame
+// goes through the graph of its shape (captured on first use), its inputs
+// copied straight into the graph's input images.
+void runFrame(xb_ctx* c, const float* T, const float* S, int w, int h, float* conv, float* diff,
+              bool host) {
   const size_t n = (size_t)w * h, bytes = n * sizeof(float);
   const bool useGraph = c->graph && mixedMode(c) && !c->trace && !c->rank && !c->timeKernels;
+  const cudaMemcpyKind kIn = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind kOut = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  const float *dT = T, *dS = S;
+  if(host && (!useGraph || !c->graphs || !c->graphs->byShape.count(shapeKey(c, w, h)))) {
+    // stage by stage (or the capturing first frame) reads device images
+    float* uT = buf<float>(c, "run_in0", n);
+    float* uS = buf<float>(c, "run_in1", n);
+    XB_CUDA(cudaMemcpyAsync(uT, T, bytes, kIn, c->stream));
+    XB_CUDA(cudaMemcpyAsync(uS, S, bytes, kIn, c->stream));
+    dT = uT;
+    dS = uS;
+  }
   if(!useGraph) {
     // stage by stage
     int rc = xb_init_device_f32(c, dT, dS, w, h);
@@ -431,8 +445,8 @@ void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, f
     if(rc == XB_OK) rc = xb_conv(c, nullptr);
     if(rc == XB_OK) rc = xb_sub(c);
     if(rc != XB_OK) throw XbError{rc, c->lastError};
-    if(dConv) XB_CUDA(cudaMemcpyAsync(dConv, c->convF, bytes, cudaMemcpyDeviceToDevice, c->stream));
-    if(dDiff) XB_CUDA(cudaMemcpyAsync(dDiff, c->diffF, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if(conv) XB_CUDA(cudaMemcpyAsync(conv, c->convF, bytes, kOut, c->stream));
+    if(diff) XB_CUDA(cudaMemcpyAsync(diff, c->diffF, bytes, kOut, c->stream));
     XB_CUDA(cudaStreamSynchronize(c->stream));
     return;
   }
@@ -445,12 +459,15 @@ void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, f
     // stage-by-stage results stay the frame's results
     c->graph = 0;
     try {
-      runFrameDevice(c, dT, dS, w, h, dConv, dDiff);
+      runFrame(c, dT, dS, w, h, nullptr, nullptr, false);
     } catch(...) {
       c->graph = 1;
       throw;
     }
     c->graph = 1;
+    if(conv) XB_CUDA(cudaMemcpyAsync(conv, c->convF, bytes, kOut, c->stream));
+    if(diff) XB_CUDA(cudaMemcpyAsync(diff, c->diffF, bytes, kOut, c->stream));
+    XB_CUDA(cudaStreamSynchronize(c->stream));
     CtxView keep = saveView(c);
     FrameGraph fg;
     fg.in[0] = buf<float>(c, "graph_in0", n);
@@ -471,11 +488,11 @@ void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, f
     return;
   }
   FrameGraph& fg = it->second;
-  XB_CUDA(cudaMemcpyAsync(fg.in[0], dT, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  XB_CUDA(cudaMemcpyAsync(fg.in[1], dS, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  XB_CUDA(cudaMemcpyAsync(fg.in[0], T, bytes, kIn, c->stream));
+  XB_CUDA(cudaMemcpyAsync(fg.in[1], S, bytes, kIn, c->stream));
   XB_CUDA(cudaGraphLaunch(fg.exec, c->stream));
-  if(dConv) XB_CUDA(cudaMemcpyAsync(dConv, fg.conv, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  if(dDiff) XB_CUDA(cudaMemcpyAsync(dDiff, fg.diff, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  if(conv) XB_CUDA(cudaMemcpyAsync(conv, fg.conv, bytes, kOut, c->stream));
+  if(diff) XB_CUDA(cudaMemcpyAsync(diff, fg.diff, bytes, kOut, c->stream));
   XB_CUDA(cudaStreamSynchronize(c->stream));
   const FrameRec& r = *fg.rec;
   c->w = w;

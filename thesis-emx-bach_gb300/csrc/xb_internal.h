@@ -329,9 +329,10 @@ void graphSetDouble(xb_ctx* c, double* p, double v);
 long long graphWhile(xb_ctx* c, const std::function<void(cudaGraphConditionalHandle)>& body);
 void graphKscContinue(xb_ctx* c, cudaGraphConditionalHandle h, const int* outs, int limit);
 int* graphRec(xb_ctx* c);
-// One frame pair, device to device (graph replay when c->graph is set).
-void runFrameDevice(xb_ctx* c, const float* dT, const float* dS, int w, int h, float* dConv,
-                    float* dDiff);
+// One frame pair, device or host buffers in and out (graph replay when
+// c->graph is set).
+void runFrame(xb_ctx* c, const float* T, const float* S, int w, int h, float* conv, float* diff,
+              bool host);
 void destroyGraphs(xb_ctx* c);
 // cd and ksc as captured by a frame graph (xb_fit.cu): lCd gets the launches
 // of each set's conditional test fit; stageKscGraph returns the launches of
