@@ -213,6 +213,112 @@ def accuracy(xbach, ctx, pctx, oracle_res, T, S, params):
     return out
 
 
+def _make_pair4(frame):
+    sys.path.insert(0, str(PKG))
+    from xbach.synth import make_pair4
+    return make_pair4(frame)
+
+
+def run_config4(args):
+    """64 pairs of sizes 512^2..4096^2, each with its own stamp grid, source
+    density and FWHM ratio (preset 4), in one batch per step: frame graphs on
+    `workers` contexts, per-pair parameters, fixed schedule."""
+    import concurrent.futures
+    import multiprocessing
+    n_pairs = args.pairs
+    # host generation in a spawned pool, before CUDA starts in this process
+    with concurrent.futures.ProcessPoolExecutor(
+            max_workers=min(16, os.cpu_count() or 1),
+            mp_context=multiprocessing.get_context("spawn")) as ex:
+        frames = list(ex.map(_make_pair4, range(n_pairs)))
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    import xbach
+    mode = xbach.XB_MODE_PLAIN if args.mode == "plain" else xbach.XB_MODE_MIXED
+    params = [frame_params(xbach, f[2], mode) for f in frames]
+    dT = [torch.from_numpy(f[0]).cuda() for f in frames]
+    dS = [torch.from_numpy(f[1]).cuda() for f in frames]
+    dC = [torch.empty_like(t) for t in dT]
+    dD = [torch.empty_like(t) for t in dT]
+    ws = [t.shape[1] for t in dT]
+    hs = [t.shape[0] for t in dT]
+    pix = sum(w * h for w, h in zip(ws, hs))
+    batch = xbach.Batch(params[0], workers=args.workers)
+    batch.set_params(params)
+    use_graph = bool(args.graph) and args.mode == "mixed"
+    if use_graph:
+        batch.set_option("graph", 1)
+    st = torch.cuda.Stream()
+    batch.set_stream(st.cuda_stream)
+
+    def run():
+        batch.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], ws, hs,
+                       [t.data_ptr() for t in dC], [t.data_ptr() for t in dD], device=True)
+    t0 = time.time()
+    run()  # first pass: every worker captures the graphs of its pairs
+    torch.cuda.synchronize()
+    capture_s = time.time() - t0
+    for _ in range(max(args.warmup - 1, 1)):
+        run()
+    torch.cuda.synchronize()
+    workers = [batch.worker(i) for i in range(batch.n_workers)]
+    l0 = sum(wk.launches() for wk in workers)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ms = 0.0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            run()
+            e1.record(st)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+    launches = sum(wk.launches() for wk in workers) - l0
+    # a sample of pairs against single contexts run stage by stage
+    check = sorted(range(n_pairs), key=lambda i: ws[i] * hs[i])
+    check = check[:2] + check[-1:]
+    same = []
+    for i in check:
+        ctx = xbach.Context(params[i])
+        ctx.init_device(dT[i].data_ptr(), dS[i].data_ptr(), ws[i], hs[i])
+        for stage in (ctx.sss, ctx.cmv, ctx.cd, ctx.ksc, ctx.conv, ctx.sub):
+            stage()
+        ref = torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))
+        same.append(bool(torch.equal(ref, dD[i].cpu())))
+        ctx.close()
+    sizes = {}
+    for w in ws:
+        sizes[f"{w}^2"] = sizes.get(f"{w}^2", 0) + 1
+    line = {
+        "metric": "difference-images/s, 64 pairs of mixed size (preset 4)",
+        "value": n_pairs * args.steps / (ms / 1000.0), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.mode == "plain" else "f32",
+        "data": "synthetic (preset 4: size, stamp grid, density, FWHM ratio per pair from its seed)",
+        "config": {"workload": f"{n_pairs} pairs, sizes {sizes}, stamp grids "
+                               f"{min(p.stampsx for p in params)}-{max(p.stampsx for p in params)}, "
+                               "49 basis functions, kernel order 2, background order 1",
+                   "mode": args.mode, "frames_per_step": n_pairs, "workers": args.workers,
+                   "frame_graphs": use_graph, "schedule": "fixed, largest first" if use_graph
+                   else "shared queue",
+                   "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+                   "l2": "flushed before every step; inputs exceed L2",
+                   "inputs": "device-resident FP32 T,S"},
+        "megapixels_per_s": pix * args.steps / (ms / 1000.0) / 1e6,
+        "gpu_launches": launches, "clocks": clk.summary(), "roofline": None, "e2e": None,
+        "first_pass_s": capture_s,
+        "check_vs_stage_by_stage": {"pairs": check, "identical": same},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,6 +331,9 @@ def main():
                     help="frame pairs per step, run concurrently (1 = one pair per step)")
     ap.add_argument("--workers", type=int, default=16, help="concurrent frames of a batch")
     ap.add_argument("--cpu-runs", type=int, default=2)
+    ap.add_argument("--config", type=int, default=2, choices=[2, 4],
+                    help="2: the headline 2048^2 workload; 4: 64 pairs of mixed size")
+    ap.add_argument("--pairs", type=int, default=64, help="--config 4: pairs per step")
     ap.add_argument("--graph", type=int, default=1,
                     help="mixed mode: replay every frame as one captured CUDA graph (1) or run "
                          "the stages host-driven (0)")
@@ -232,6 +341,8 @@ def main():
     use_graph = bool(args.graph) and args.mode == "mixed"
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 4:
+        return run_config4(args)
 
     rank, world, local = dist_env()
     import numpy as np

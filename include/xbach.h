@@ -120,6 +120,10 @@ int xb_ctx_create(const xb_params* p, int device, xb_ctx** out);
 int xb_ctx_destroy(xb_ctx* ctx);
 /* Human-readable message for the last failing call on this context. */
 const char* xb_last_error(const xb_ctx* ctx);
+/* Switches a context to other parameters that keep its basis, widths,
+ * orders and mode (stamp grid, thresholds, clipping may change; XB_ERR_ARG
+ * otherwise).  The next frame starts at init. */
+int xb_ctx_set_params(xb_ctx* ctx, const xb_params* p);
 /* Context options.  "trace" (0/1): keep host copies of the intermediate
  * results of every stage for xb_get_array (parity checks; costs copies).
  * "time_kernels" (0/1): time the main kernels with CUDA events on the
@@ -271,6 +275,13 @@ int xb_batch_run_device(xb_batch* b, int nFrames, const float* const* dT,
                         double* kernSum);
 /* Worker context i (options such as "time_kernels", timers, launch counts). */
 int xb_batch_worker(xb_batch* b, int i, xb_ctx** ctx);
+/* Parameters per frame for later runs: params[i] applies to frame i (stamp
+ * grid, thresholds, clipping); every set must keep the batch's basis,
+ * widths, orders and mode (XB_ERR_ARG otherwise).  nFrames = 0 returns to
+ * the batch's parameters.  With option "graph" on every worker, frames are
+ * dealt to workers by a fixed schedule (largest first to the least-loaded
+ * worker), so a repeated list of frames replays captured graphs. */
+int xb_batch_set_params(xb_batch* b, int nFrames, const xb_params* params);
 /* Joins a caller's cudaStream_t to every later run: the workers' first
  * launches wait for the work already queued on `stream`, and work queued on
  * `stream` after the run waits for every worker, so CUDA events recorded on

@@ -78,3 +78,54 @@ def test_batch_reports_failing_frame():
     rc = L.xb_batch_run(batch.h, 1, None, None, None, None, None, None, st, None)
     assert rc == 1  # XB_ERR_ARG: null frame arrays
     del good
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_batch_per_frame_parameters(test01, graph):
+    """Pairs with their own stamp grids and thresholds in one batch (preset-4
+    style); every result equals a single context run with that pair's
+    parameters, stage by stage."""
+    import xbach
+    from xbach.synth import make_pair
+    pairs = [(test01["T"].astype(np.float32), test01["S"].astype(np.float32),
+              dict(stampsx=10, stampsy=10))]
+    for f, grid in enumerate((6, 13, 8)):
+        T, S, info = make_pair(1, frame=f)
+        pairs.append((T, S, dict(stampsx=grid, stampsy=grid + 1, threshHigh=info["threshHigh"])))
+    mode = xbach.XB_MODE_MIXED
+    params = [xbach.default_params(mode=mode, **kw) for _, _, kw in pairs]
+    batch = xbach.Batch(params[0], workers=3)
+    batch.set_params(params)
+    if graph:
+        batch.set_option("graph", 1)
+    refs = []
+    for (T, S, _), p in zip(pairs, params):
+        ctx = xbach.Context(p)
+        ctx.run_all(T, S)
+        refs.append((ctx.image(xbach.XB_IMG_DIFF, f64=False), ctx.scalar("kernSum"),
+                     ctx.scalar("stampsx")))
+    for rep in range(2 if graph else 1):
+        diffs = [np.empty_like(T) for T, _, _ in pairs]
+        st, ks = batch.run([T for T, _, _ in pairs], [S for _, S, _ in pairs], None, diffs)
+        assert st == [0] * len(pairs)
+        for i, (d, k, _) in enumerate(refs):
+            assert np.array_equal(diffs[i], d), (rep, i)
+            assert ks[i] == k, (rep, i)
+    # back to the batch's own parameters
+    batch.set_params([])
+    st, _ = batch.run([pairs[1][0]], [pairs[1][1]])
+    assert st == [0]
+
+
+def test_batch_parameters_must_keep_the_fit():
+    import xbach
+    base = xbach.default_params(mode=xbach.XB_MODE_MIXED)
+    batch = xbach.Batch(base, workers=1)
+    with pytest.raises(xbach.XbError):
+        batch.set_params([xbach.default_params(mode=xbach.XB_MODE_MIXED, kernelOrder=1)])
+    with pytest.raises(xbach.XbError):
+        batch.set_params([xbach.default_params(mode=xbach.XB_MODE_PLAIN)])
+    ctx = xbach.Context(base)
+    with pytest.raises(xbach.XbError):
+        ctx.set_params(xbach.default_params(mode=xbach.XB_MODE_MIXED, hKernelWidth=8))
+    ctx.set_params(xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=7, threshHigh=3e4))

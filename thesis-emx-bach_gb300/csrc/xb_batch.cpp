@@ -9,8 +9,17 @@
 // so the GPU interleaves the kernels of up to nWorkers frames.  Contexts keep
 // their device buffers between frames (the buffer pool only grows), so a
 // steady stream of frames allocates nothing.
+//
+// Frames may carry their own parameters (xb_batch_set_params): the stamp
+// grid, thresholds and clipping of each pair, within the batch's basis and
+// sizes.  When the workers replay frame graphs, frames are dealt to workers
+// by a fixed schedule (largest first, to the least-loaded worker) instead of
+// a shared queue, so the same list of frames meets the same worker, whose
+// graph for that shape and parameter set is already captured.
 
+#include <algorithm>
 #include <atomic>
+#include <numeric>
 #include <string>
 #include <thread>
 #include <vector>
@@ -19,6 +28,8 @@
 
 struct xb_batch {
   std::vector<xb_ctx*> workers;
+  xb_params base{};                        // the batch's parameters
+  std::vector<xb_params> frameParams;      // per frame (xb_batch_set_params), or empty
   std::string lastError;
   int device = 0;
   cudaStream_t join = nullptr;             // caller's stream (xb_batch_set_stream)
@@ -35,18 +46,47 @@ int runDeviceFrame(xb_ctx* c, const float* dT, const float* dS, int w, int h, fl
   return xb_run_device(c, dT, dS, w, h, dConv, dDiff);
 }
 
+// Frames per worker for graph replays: largest first, each to the worker
+// with the fewest pixels so far (lowest index on ties).
+std::vector<std::vector<int>> fixedSchedule(int nFrames, int nW, const int* w, const int* h) {
+  std::vector<int> order(nFrames);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (long long)w[a] * h[a] > (long long)w[b] * h[b];
+  });
+  std::vector<long long> load(nW, 0);
+  std::vector<std::vector<int>> per(nW);
+  for(int i : order) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    per[k].push_back(i);
+    load[k] += (long long)w[i] * h[i];
+  }
+  return per;
+}
+
 template <class F>
-int runQueue(xb_batch* b, int nFrames, int* frameStatus, double* kernSum, F&& frame) {
+int runQueue(xb_batch* b, int nFrames, const int* fw, const int* fh, int* frameStatus,
+             double* kernSum, F&& frame) {
   if(!b) return XB_ERR_ARG;
   if(nFrames < 0) {
     b->lastError = "negative frame count";
+    return XB_ERR_ARG;
+  }
+  if(!b->frameParams.empty() && (int)b->frameParams.size() < nFrames) {
+    b->lastError = "fewer frame parameter sets than frames";
     return XB_ERR_ARG;
   }
   std::vector<int> st(nFrames, XB_OK);
   std::vector<std::string> msg(nFrames);
   std::atomic<int> next{0};
   std::vector<std::thread> th;
-  const int nW = std::min<int>((int)b->workers.size(), std::max(nFrames, 1));
+  bool graphs = nFrames > 0;
+  for(xb_ctx* c : b->workers) graphs = graphs && c->graph;
+  // graph replays: every worker runs, on its fixed share of the frames
+  const int nW = graphs ? (int)b->workers.size()
+                        : std::min<int>((int)b->workers.size(), std::max(nFrames, 1));
+  std::vector<std::vector<int>> fixed;
+  if(graphs) fixed = fixedSchedule(nFrames, nW, fw, fh);
   if(b->join) {
     cudaSetDevice(b->device);
     const cudaError_t e = cudaEventRecord(b->start, b->join);
@@ -60,10 +100,17 @@ int runQueue(xb_batch* b, int nFrames, int* frameStatus, double* kernSum, F&& fr
       cudaSetDevice(b->device);
       xb_ctx* c = b->workers[wi];
       if(b->join) cudaStreamWaitEvent(c->stream, b->start, 0);
-      for(;;) {
-        const int i = next.fetch_add(1);
-        if(i >= nFrames) break;
-        st[i] = frame(c, i);
+      for(size_t k = 0;; k++) {
+        int i;
+        if(graphs) {
+          if(k >= fixed[wi].size()) break;
+          i = fixed[wi][k];
+        } else {
+          i = next.fetch_add(1);
+          if(i >= nFrames) break;
+        }
+        st[i] = xb_ctx_set_params(c, b->frameParams.empty() ? &b->base : &b->frameParams[i]);
+        if(st[i] == XB_OK) st[i] = frame(c, i);
         if(st[i] != XB_OK) msg[i] = c->lastError;
         if(kernSum) kernSum[i] = st[i] == XB_OK ? c->kernSum : 0.0;
       }
@@ -92,6 +139,7 @@ int xb_batch_create(const xb_params* p, int device, int nWorkers, xb_batch** out
   *out = nullptr;
   xb_batch* b = new xb_batch;
   b->device = device;
+  b->base = *p;
   for(int i = 0; i < nWorkers; i++) {
     xb_ctx* c = nullptr;
     const int rc = xb_ctx_create(p, device, &c);
@@ -146,7 +194,7 @@ int xb_batch_run(xb_batch* b, int nFrames, const float* const* T, const float* c
     b->lastError = "null frame arrays";
     return XB_ERR_ARG;
   }
-  return runQueue(b, nFrames, frameStatus, kernSum, [&](xb_ctx* c, int i) {
+  return runQueue(b, nFrames, w, h, frameStatus, kernSum, [&](xb_ctx* c, int i) {
     return xb_run(c, T[i], S[i], w[i], h[i], conv ? conv[i] : nullptr, diff ? diff[i] : nullptr);
   });
 }
@@ -159,10 +207,22 @@ int xb_batch_run_device(xb_batch* b, int nFrames, const float* const* dT,
     b->lastError = "null frame arrays";
     return XB_ERR_ARG;
   }
-  return runQueue(b, nFrames, frameStatus, kernSum, [&](xb_ctx* c, int i) {
+  return runQueue(b, nFrames, w, h, frameStatus, kernSum, [&](xb_ctx* c, int i) {
     return runDeviceFrame(c, dT[i], dS[i], w[i], h[i], dConv ? dConv[i] : nullptr,
                           dDiff ? dDiff[i] : nullptr);
   });
+}
+
+int xb_batch_set_params(xb_batch* b, int nFrames, const xb_params* params) {
+  if(!b || nFrames < 0 || (nFrames > 0 && !params)) return XB_ERR_ARG;
+  for(int i = 0; i < nFrames; i++)
+    if(!xb::sameFit(b->base, params[i])) {
+      b->lastError = "frame " + std::to_string(i) +
+                     ": parameters change the basis or the fit's sizes of the batch";
+      return XB_ERR_ARG;
+    }
+  b->frameParams.assign(params, params + nFrames);
+  return XB_OK;
 }
 
 int xb_batch_worker(xb_batch* b, int i, xb_ctx** ctx) {

@@ -48,6 +48,23 @@ int validate(const xb_params& p, std::string& why) {
   return XB_OK;
 }
 
+}  // namespace
+
+namespace xb {
+// Parameters that size the fit or build its basis: a context keeps them for
+// its lifetime (its basis tables and launch shapes depend on them).
+bool sameFit(const xb_params& a, const xb_params& b) {
+  const Geo ga = makeGeo(a), gb = makeGeo(b);
+  if(std::memcmp(&ga, &gb, sizeof(Geo)) != 0) return false;
+  if(a.mode != b.mode || a.nGauss != b.nGauss) return false;
+  for(int i = 0; i < a.nGauss; i++)
+    if(a.dg[i] != b.dg[i] || a.bg[i] != b.bg[i]) return false;
+  return true;
+}
+}  // namespace xb
+
+namespace {
+
 template <class T>
 void uploadImages(xb_ctx* c, const T* t, const T* s, int w, int h, bool f64) {
   const size_t n = (size_t)w * h;
@@ -169,6 +186,19 @@ int xb_ctx_destroy(xb_ctx* c) {
 }
 
 const char* xb_last_error(const xb_ctx* c) { return c ? c->lastError.c_str() : "null context"; }
+
+int xb_ctx_set_params(xb_ctx* c, const xb_params* p) {
+  return guarded(c, [&] {
+    if(!p) throw XbError{XB_ERR_ARG, "null parameters"};
+    std::string why;
+    const int rc = validate(*p, why);
+    if(rc != XB_OK) throw XbError{rc, why};
+    if(!sameFit(c->p, *p))
+      throw XbError{XB_ERR_ARG, "the parameters change the basis or the fit's sizes (new context)"};
+    c->p = *p;
+    c->stage = 0;
+  });
+}
 
 int xb_set_option(xb_ctx* c, const char* name, long long value) {
   if(!c || !name) return XB_ERR_ARG;

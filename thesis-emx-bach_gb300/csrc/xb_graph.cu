@@ -230,11 +230,36 @@ int* graphRec(xb_ctx* c) { return buf<int>(c, "graph_rec", 8); }
 
 namespace {
 
+// Frame size plus every parameter a capture bakes in (field by field: the
+// struct's padding bytes are not part of the key).
 std::string shapeKey(const xb_ctx* c, int w, int h) {
-  std::string k(reinterpret_cast<const char*>(&c->p), sizeof(xb_params));
-  k.append(reinterpret_cast<const char*>(&w), sizeof(w));
-  k.append(reinterpret_cast<const char*>(&h), sizeof(h));
-  k.append(1, (char)c->gramFp64);
+  std::string k;
+  auto put = [&](const auto& v) { k.append(reinterpret_cast<const char*>(&v), sizeof(v)); };
+  const xb_params& p = c->p;
+  put(w);
+  put(h);
+  put(p.stampsx);
+  put(p.stampsy);
+  put(p.threshLow);
+  put(p.threshHigh);
+  put(p.threshKernFit);
+  put(p.sigKernFit);
+  put(p.sigClipAlpha);
+  put(p.iqRange);
+  put(p.maxKSStamps);
+  put(p.hSStampWidth);
+  put(p.hKernelWidth);
+  put(p.inSpreadMaskFactor);
+  put(p.normalizeTemplate);
+  put(p.backgroundOrder);
+  put(p.kernelOrder);
+  put(p.nGauss);
+  for(int i = 0; i < p.nGauss; i++) {
+    put(p.dg[i]);
+    put(p.bg[i]);
+  }
+  put(p.mode);
+  put(c->gramFp64);
   return k;
 }
 

@@ -49,6 +49,9 @@ struct Geo {
 inline int triNum(int t) { return t * (t + 1) / 2; }
 
 Geo makeGeo(const xb_params& p);
+// a and b give the same basis, widths, orders and mode (a context can switch
+// between them; stamp grid, thresholds and clipping may differ)
+bool sameFit(const xb_params& a, const xb_params& b);
 
 // Basis tables built once on the host (createKernelFilter/createKernelVector,
 // cl_kern/cmv.cl:1-68; the host Kernel struct of include/datatypeUtil.h).

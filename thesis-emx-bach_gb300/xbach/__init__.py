@@ -52,14 +52,14 @@ _lib = None
 
 EXPORTS = [
     "xb_params_default", "xb_params_npsf", "xb_ctx_create", "xb_ctx_destroy",
-    "xb_last_error", "xb_set_option", "xb_init", "xb_init_f32",
+    "xb_last_error", "xb_ctx_set_params", "xb_set_option", "xb_init", "xb_init_f32",
     "xb_init_device_f32", "xb_sss", "xb_cmv", "xb_cd", "xb_ksc", "xb_conv",
     "xb_sub", "xb_run", "xb_run_device", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
     "xb_get_scalar", "xb_kernel_launches", "xb_get_stream", "xb_fits_read",
     "xb_fits_write", "xb_free", "xb_stamp_stats_noalloc", "xb_batch_create",
     "xb_batch_destroy", "xb_batch_last_error", "xb_batch_run", "xb_batch_run_device",
-    "xb_batch_worker", "xb_batch_set_stream", "xb_ranker_param_count", "xb_ranker_set",
+    "xb_batch_worker", "xb_batch_set_stream", "xb_batch_set_params", "xb_ranker_param_count", "xb_ranker_set",
     "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
 ]
 
@@ -113,6 +113,8 @@ def lib():
                                       P(d)]
     L.xb_batch_worker.argtypes = [vp, i, P(vp)]
     L.xb_batch_set_stream.argtypes = [vp, vp]
+    L.xb_batch_set_params.argtypes = [vp, i, vp]
+    L.xb_ctx_set_params.argtypes = [vp, vp]
     L.xb_ranker_param_count.argtypes = []
     L.xb_ranker_set.argtypes = [vp, vp, i]
     L.xb_ranker_features.argtypes = [vp, i, vp, vp, vp, vp, i, P(i)]
@@ -276,6 +278,11 @@ class Context:
     def set_option(self, name, value):
         return self._check(self.L.xb_set_option(self.h, name.encode(), int(value)))
 
+    def set_params(self, params):
+        """Other parameters with the same basis, widths, orders and mode."""
+        self._check(self.L.xb_ctx_set_params(self.h, ctypes.byref(params)))
+        self.params = params
+
     def kernel_time(self, name):
         """(total ms, launches) of a timed kernel (option time_kernels)."""
         try:
@@ -331,6 +338,16 @@ class Batch:
         """Join a cudaStream_t handle (int) to later runs (0 detaches)."""
         if self.L.xb_batch_set_stream(self.h, ctypes.c_void_p(stream or None)):
             raise XbError(5, "xb_batch_set_stream failed")
+
+    def set_params(self, params_list):
+        """Parameters per frame for later runs (a list of xb_params; [] or
+        None returns to the batch's own)."""
+        params_list = list(params_list or [])
+        arr = (XbParams * max(len(params_list), 1))(*params_list)
+        rc = self.L.xb_batch_set_params(self.h, len(params_list), arr)
+        if rc:
+            raise XbError(rc, self.L.xb_batch_last_error(self.h).decode())
+        self._keep_params = arr
 
     def set_option(self, name, value):
         """xb_set_option on every worker context (e.g. "graph")."""

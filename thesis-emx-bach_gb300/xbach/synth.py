@@ -37,10 +37,21 @@ PARAMS_3 = dict(nGauss=4, dg=[6, 4, 3, 2],
                 kernelOrder=3, backgroundOrder=2)
 
 
-def _render(img, xs, ys, fluxes, sigmas):
-    """Adds pixel-integrated Gaussians (one sigma per source) into img."""
+def _render(img, xs, ys, fluxes, sigmas, chunk=None, r=None):
+    """Adds pixel-integrated Gaussians (one sigma per source) into img.
+
+    chunk: sources per pass (bounds the temporary arrays); every pass uses
+    the radius of the widest source, so the image does not depend on it."""
+    if len(xs) == 0:
+        return
+    if r is None:
+        r = int(np.ceil(4.0 * sigmas.max())) + 1
+    if chunk and len(xs) > chunk:
+        for i in range(0, len(xs), chunk):
+            _render(img, xs[i:i + chunk], ys[i:i + chunk], fluxes[i:i + chunk],
+                    sigmas[i:i + chunk], None, r)
+        return
     h, w = img.shape
-    r = int(np.ceil(4.0 * sigmas.max())) + 1
     off = np.arange(-r, r + 1)
     cx = np.floor(xs).astype(np.int64)
     cy = np.floor(ys).astype(np.int64)
@@ -67,8 +78,9 @@ def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over
         cfg["size"] = size
     if n_src is not None:
         cfg["n_src"] = n_src
+    seed = over.pop("seed", config)
     cfg.update(over)
-    rng = np.random.Generator(np.random.Philox(key=config * 1000003 + frame))
+    rng = np.random.Generator(np.random.Philox(key=seed * 1000003 + frame))
     n = cfg["size"]
     sky, rn, scale = 1000.0, 5.0, 1.1
     ns = cfg["n_src"]
@@ -94,8 +106,8 @@ def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over
     sig_s = fwhm_at(cfg["fwhm_s"]) * c
     T = np.zeros((n, n))
     S = np.zeros((n, n))
-    _render(T, xs, ys, flux, sig_t)
-    _render(S, xs, ys, flux_s, sig_s)
+    _render(T, xs, ys, flux, sig_t, cfg.get("chunk"))
+    _render(S, xs, ys, flux_s, sig_s, cfg.get("chunk"))
     xx = np.arange(n)[None, :].repeat(n, 0)
     S += 50.0 + 0.01 * xx
     T = rng.poisson(T + sky).astype(np.float64) + rng.normal(0.0, rn, T.shape)
@@ -110,3 +122,34 @@ def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over
     info = dict(config=config, frame=frame, stamps=cfg["stamps"], size=n, n_src=ns,
                 threshHigh=cfg["saturation"] or 25000.0)
     return T.astype(dtype), S.astype(dtype), info
+
+
+# Batched preset 4: pairs whose size, stamp grid, source density and
+# science/template FWHM ratio are drawn from the frame's seed; otherwise
+# preset 2 (FWHM 2.2-3.2 px across the template field, 1 % cosmic-ray
+# pixels, 40 saturated stars, saturation 6e4).
+SIZES_4 = (512, 1024, 2048, 3072, 4096)
+
+
+def config4_draw(frame):
+    """Size, stamp grid, density (sources per px^2) and FWHM ratio of pair
+    `frame` of preset 4."""
+    rng = np.random.Generator(np.random.Philox(key=4 * 1000003 + 104729 * (frame + 1)))
+    size = int(SIZES_4[int(rng.integers(0, len(SIZES_4)))])
+    stamps = int(rng.integers(5, 21))
+    density = float(rng.uniform(0.002, 0.01))
+    ratio = float(rng.uniform(1.1, 1.8))
+    return dict(size=size, stamps=stamps, density=density, ratio=ratio,
+                n_src=int(round(density * size * size)))
+
+
+def make_pair4(frame, dtype=np.float32):
+    """Pair `frame` of preset 4: (template, science, info); info carries the
+    pair's stamp grid and threshHigh."""
+    d = config4_draw(frame)
+    lo, hi = CONFIGS[2]["fwhm_t"]
+    T, S, info = make_pair(2, frame=frame, size=d["size"], n_src=d["n_src"], dtype=dtype,
+                           seed=4, stamps=d["stamps"], chunk=16384,
+                           fwhm_s=(lo * d["ratio"], hi * d["ratio"]))
+    info.update(config=4, density=d["density"], fwhm_ratio=d["ratio"])
+    return T, S, info
