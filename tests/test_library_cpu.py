@@ -103,3 +103,23 @@ def test_context_creation_rejects_bad_params(xb):
     assert xb.lib().xb_ctx_create(ctypes.byref(p), 0, ctypes.byref(h)) == 1
     p = xb.default_params(nGauss=0)
     assert xb.lib().xb_ctx_create(ctypes.byref(p), 0, ctypes.byref(h)) == 1
+
+
+def test_histogram_density_compare_is_exact():
+    """The mode search of the stamp statistics compares S/D > S'/D' (FP64
+    quotients of integer counts S < 2^31 and widths D <= 254) as
+    S*D' > S'*D; distinct fractions of that form are more than 2^-47 apart
+    relatively, so the correctly rounded quotients order the same way."""
+    rng = np.random.default_rng(7)
+    n = 2_000_000
+    S = rng.integers(0, 2**31 - 1, n, dtype=np.int64)
+    D = rng.integers(1, 255, n, dtype=np.int64)
+    S2 = rng.integers(0, 2**31 - 1, n, dtype=np.int64)
+    D2 = rng.integers(1, 255, n, dtype=np.int64)
+    # nearby fractions too: S2/D2 close to S/D
+    k = n // 2
+    S2[:k] = (S[:k] * D2[:k]) // D[:k] + rng.integers(-2, 3, k)
+    S2 = np.clip(S2, 0, 2**31 - 1)
+    by_float = (S.astype(np.float64) / D) > (S2.astype(np.float64) / D2)
+    by_int = S * D2 > S2 * D
+    assert np.array_equal(by_float, by_int)

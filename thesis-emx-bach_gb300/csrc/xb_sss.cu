@@ -464,12 +464,24 @@ __global__ void __launch_bounds__(ST_THREADS)
       if(ok == 0 || binSize == 0.0) {
         hState = 2;
       } else {
-        double sumBins = 0.0, maxDens = 0.0;
+        // densest run of bins holding a tenth of the pixels.  The reference
+        // compares the FP64 quotients sumBins / (upper - lower); both are
+        // integer over integer (sums of counts < 2^31, widths 1..254), and two
+        // different such fractions differ by more than 2^-47 relative, so
+        // their correctly rounded quotients compare like the fractions:
+        // S / D > S' / D'  <=>  S * D' > S' * D, exact in 64-bit integers.
+        // The width is never 0: the window is empty only at the top of the
+        // loop, and then the inner loop adds a bin (upper < 255 there).
+        double sumBins = 0.0;
+        long long maxNum = 0, maxDen = 1;  // maxDens = 0 at first
+        const double okTenth = ok / 10.0;
         int lowerIndex = 1, upperIndex = 1, maxIndex = -1;
         while(upperIndex < 255) {
-          while(sumBins < ok / 10.0 && upperIndex < 255) sumBins += bins[upperIndex++];
-          if(sumBins / (upperIndex - lowerIndex) > maxDens) {
-            maxDens = sumBins / (upperIndex - lowerIndex);
+          while(sumBins < okTenth && upperIndex < 255) sumBins += bins[upperIndex++];
+          const long long S = (long long)sumBins, D = upperIndex - lowerIndex;
+          if(S * maxDen > maxNum * D) {
+            maxNum = S;
+            maxDen = D;
             maxIndex = lowerIndex;
           }
           sumBins -= bins[lowerIndex++];
@@ -908,15 +920,22 @@ __global__ void __launch_bounds__(FS_T, 1)
     flags[p] = fl;
   }
   __syncthreads();
-  // maps of the current bad state (keys, window argmax, window ORs)
-  auto build = [&]() {
-    for(int p = tid; p < N; p += FS_T) {
+  // maps of the current bad state (keys, window argmax, window ORs) over the
+  // columns [x0, x1] of the rows [k0, k1] (keys and row maps) and [r0, r1]
+  // (column maps); the full build covers the stamp.  After an acceptance
+  // only the accepted window's bad bits change, so only keys inside it, row
+  // maps within hSS of it in x and column maps within hSS of it in x and y
+  // can change: rebuilding that region gives the maps of a full rebuild.
+  auto build = [&](int x0, int x1, int k0, int k1, int r0, int r1) {
+    const int kw = x1 - x0 + 1;
+    for(int i = tid; i < kw * (k1 - k0 + 1); i += FS_T) {
+      const int p = (k0 + i / kw) * n + x0 + i % kw;
       const uint8_t fl = flags[p];
       key[p] = (!bad[p] && (fl & FL_KFQ) && (fl & FL_VPOS)) ? __float_as_uint(V[p]) : 0u;
     }
     __syncthreads();
-    for(int ly = warp; ly < n; ly += NW)
-      for(int lx = lane; lx < n; lx += 32) {
+    for(int ly = k0 + warp; ly <= k1; ly += NW)
+      for(int lx = x0 + lane; lx <= x1; lx += 32) {
         const int row = ly * n;
         uint32_t bk = 0;
         int bi = 0xFF;
@@ -938,8 +957,8 @@ __global__ void __launch_bounds__(FS_T, 1)
         rowf[row + lx] = o;
       }
     __syncthreads();
-    for(int ly = warp; ly < n; ly += NW)
-      for(int lx = lane; lx < n; lx += 32) {
+    for(int ly = r0 + warp; ly <= r1; ly += NW)
+      for(int lx = x0 + lane; lx <= x1; lx += 32) {
         uint32_t bk = 0;
         int bi = 0xFFFF;
         for(int y = max(ly - hSS, 0); y <= min(ly + hSS, n - 1); y++) {
@@ -958,7 +977,7 @@ __global__ void __launch_bounds__(FS_T, 1)
       }
     __syncthreads();
   };
-  build();
+  build(0, n - 1, 0, n - 1, 0, n - 1);
   const double floorV = sky + tKF * fwhm;
   double dfrac = 0.9;
   int cnt = 0, passes = 0;
@@ -1057,7 +1076,12 @@ __global__ void __launch_bounds__(FS_T, 1)
         bad[(gy - cy) * n + (gx - cx)] = 1;  // skipMask is part of badMask
       }
       __syncthreads();
-      if(cnt < maxSS) build();
+      if(cnt < maxSS) {
+        // keys change inside the window only; maps within hSS of it
+        const int a0 = u0 - cx, a1 = u1 - cx, b0 = v0 - cy, b1 = v1 - cy;
+        build(max(a0 - hSS, 0), min(a1 + hSS, n - 1), b0, b1, max(b0 - hSS, 0),
+              min(b1 + hSS, n - 1));
+      }
     }
     if(cnt >= maxSS || lim == floorV) break;
     dfrac -= 0.2;
