@@ -162,7 +162,7 @@ template <class T>
 __global__ void __launch_bounds__(ST_THREADS)
     k_stamp_stats(const T* __restrict__ img, uint16_t* __restrict__ mask,
                   const int4* __restrict__ geom, int w, int h, int fSW,
-                  double* __restrict__ good, uint8_t* __restrict__ clip,
+                  T* __restrict__ good, uint8_t* __restrict__ clip,
                   double* __restrict__ chunkBuf, int maxChunks,
                   double sigClipAlpha, double iqRange, double* __restrict__ skyOut,
                   double* __restrict__ fwhmOut, const double* __restrict__ draws) {
@@ -257,37 +257,61 @@ __global__ void __launch_bounds__(ST_THREADS)
   __syncthreads();
 
   // ---- phase B: ordered compaction of good pixels (maskStamp) ----
-  // each thread owns a contiguous run of the stamp's pixel indices, so one
-  // block scan keeps the ascending order
-  double* gd = good + (size_t)s * fSW * fSW;
+  // warp w owns a contiguous range of the stamp's pixel indices and reads it
+  // 32 consecutive pixels at a time; ballots keep the ascending order inside
+  // the warp and one block scan over the warp totals orders the warps.  The
+  // good pixels are kept as read (FP32 pixels stay FP32).
+  T* gd = good + (size_t)s * fSW * fSW;
   uint8_t* cl = clip + (size_t)s * fSW * fSW;
-  const int nPixS = fSW * fSW, per = (nPixS + ST_THREADS - 1) / ST_THREADS;
-  const int i0 = min(tid * per, nPixS), i1 = min(i0 + per, nPixS);
-  int myGood = 0;
-  for(int idxS = i0; idxS < i1; idxS++) {
+  const int nPixS = fSW * fSW;
+  constexpr int NWARP = ST_THREADS / 32;
+  const int perW = ((nPixS + NWARP - 1) / NWARP + 31) & ~31;
+  const int w0 = min(warp * perW, nPixS), w1 = min(w0 + perW, nPixS);
+  // v <= 1e-10 of the reference: for an FP32 pixel the same test as f <= fTiny,
+  // the largest float not above 1e-10
+  const float fTiny = __double2float_rd(1e-10);
+  auto tiny = [&](T v) -> bool {
+    if(F32) return (float)v <= fTiny;
+    return (double)v <= 1e-10;
+  };
+  auto pixelAt = [&](int idxS, size_t* id) -> bool {
     const int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
-    if(xI < w && yI < h) {
-      const size_t id = (size_t)xI + (size_t)yI * w;
-      const double pix = (double)img[id];
-      if(!(mask[id] > 0 || pix <= 1e-10)) {
+    *id = (size_t)xI + (size_t)yI * w;
+    return xI < w && yI < h;
+  };
+  int wGood = 0;
+  for(int b = w0; b < w1; b += 32) {
+    const int idxS = b + lane;
+    bool g = false;
+    size_t id;
+    if(idxS < w1 && pixelAt(idxS, &id)) {
+      const T pix = img[id];
+      if(!(mask[id] > 0 || tiny(pix))) {
         if(isnan(pix)) mask[id] |= NAN_PIXEL | BAD_INPUT;
-        else myGood++;
+        else g = true;
       }
     }
+    wGood += __popc(__ballot_sync(0xffffffffu, g));
   }
-  int pos = blockExclusiveScan(myGood, warpTot, &sTotal);
+  const int wBase = blockExclusiveScan(lane == 0 ? wGood : 0, warpTot, &sTotal);
   const int nGood = sTotal;
-  for(int idxS = i0; idxS < i1 && myGood > 0; idxS++) {
-    const int xI = idxS % fSW + gm.x, yI = idxS / fSW + gm.y;
-    if(xI < w && yI < h) {
-      const size_t id = (size_t)xI + (size_t)yI * w;
-      const double pix = (double)img[id];
-      if(!(mask[id] > 0 || pix <= 1e-10)) {
-        gd[pos] = pix;
-        cl[pos] = 0;
-        pos++;
-      }
+  int pos = __shfl_sync(0xffffffffu, wBase, 0);
+  for(int b = w0; b < w1; b += 32) {
+    const int idxS = b + lane;
+    bool g = false;
+    T pix = 0;
+    size_t id;
+    if(idxS < w1 && pixelAt(idxS, &id)) {
+      pix = img[id];
+      g = !(mask[id] > 0 || tiny(pix));  // NaN pixels carry their mask bits now
     }
+    const unsigned bal = __ballot_sync(0xffffffffu, g);
+    if(g) {
+      const int q = pos + __popc(bal & ((1u << lane) - 1u));
+      gd[q] = pix;
+      cl[q] = 0;
+    }
+    pos += __popc(bal);
   }
 
   // ---- phase C: sigma clip, maxIter 3 (bachUtil.cpp:34-128) ----
@@ -304,23 +328,27 @@ __global__ void __launch_bounds__(ST_THREADS)
   __syncthreads();
   const int nChunks = (nGood + 31) / 32;
   // exact clip thresholds for (m, inv) into tLo/tHi (warp 0; all threads call)
+  // (warp 0 searches the upper edge, warp 1 the lower one)
   auto thresholds = [&](double m, double inv) {
-    if(warp == 0) {
+    if(warp < 2) {
       const bool direct = !isfinite(m) || isnan(inv);
       if(!direct) {
-        bool noHi, noLo;
-        const unsigned long long kh = clipEdge(m, inv, sigClipAlpha, true, &noHi);
-        const unsigned long long kl = clipEdge(m, inv, sigClipAlpha, false, &noLo);
+        bool none;
+        const unsigned long long k = clipEdge(m, inv, sigClipAlpha, warp == 0, &none);
         if(lane == 0) {
-          tHi = keyD(kh);
-          tLo = keyD(kl);
-          fHi = __double2float_ru(tHi);  // f >= tHi  <=>  f >= fHi for a float f
-          fLo = __double2float_rd(tLo);
-          tNoHi = noHi;
-          tNoLo = noLo;
+          const double t = keyD(k);
+          if(warp == 0) {
+            tHi = t;
+            fHi = __double2float_ru(t);  // f >= tHi  <=>  f >= fHi for a float f
+            tNoHi = none;
+          } else {
+            tLo = t;
+            fLo = __double2float_rd(t);
+            tNoLo = none;
+          }
         }
       }
-      if(lane == 0) tDirect = direct;
+      if(warp == 0 && lane == 0) tDirect = direct;
     }
     __syncthreads();
   };
@@ -332,6 +360,29 @@ __global__ void __launch_bounds__(ST_THREADS)
     }
     return (!tNoHi && v >= tHi) || (!tNoLo && v <= tLo);
   };
+  // the same for a pixel as read (no FP64 conversion for FP32 pixels)
+  auto isClippedPix = [&](T pv, double m, double inv) -> bool {
+    if(tDirect) return clipOut((double)pv, m, inv, sigClipAlpha);
+    if(F32) {
+      const float f = (float)pv;
+      return (!tNoHi && f >= fHi) || (!tNoLo && f <= fLo);
+    }
+    return isClipped((double)pv, m, inv);
+  };
+  // chunk sums of the unclipped pixels: 32 consecutive good pixels each, in
+  // order (all pixels at first; then fused with each round's clip pass, for
+  // the next round)
+  for(int c = tid; c < nChunks; c += ST_THREADS) {
+    double a = 0.0, a2 = 0.0;
+    const int lc = min(32, nGood - c * 32);
+    for(int l = 0; l < lc; l++) {
+      const double d = (double)gd[c * 32 + l];
+      a += d;
+      a2 += d * d;
+    }
+    cS[c] = a;
+    cS2[c] = a2;
+  }
   for(int it = 0; it < 3; it++) {
     if(sDone || sCurr == sPrev) break;
     if(sPrev <= 1) {
@@ -343,18 +394,6 @@ __global__ void __launch_bounds__(ST_THREADS)
     }
     __syncthreads();
     if(tid == 0) sCurr = sPrev;
-    for(int c = tid; c < nChunks; c += ST_THREADS) {
-      double a = 0.0, a2 = 0.0;
-      int lc = min(32, nGood - c * 32);
-      for(int l = 0; l < lc; l++) {
-        int k = c * 32 + l;
-        double d = cl[k] == 0 ? gd[k] : 0.0;
-        a += d;
-        a2 += d * d;
-      }
-      cS[c] = a;
-      cS2[c] = a2;
-    }
     __syncthreads();
     // the two sequential chunk sums run on two warps
     if(tid == 0) {
@@ -381,11 +420,25 @@ __global__ void __launch_bounds__(ST_THREADS)
     const double m = sMean, inv = sInv;
     thresholds(m, inv);
     int myClip = 0;
-    for(int k = tid; k < nGood; k += ST_THREADS)
-      if(cl[k] == 0 && isClipped(gd[k], m, inv)) {
-        cl[k] = 1;
-        myClip++;
+    for(int c = tid; c < nChunks; c += ST_THREADS) {
+      double a = 0.0, a2 = 0.0;
+      const int lc = min(32, nGood - c * 32);
+      for(int l = 0; l < lc; l++) {
+        const int k = c * 32 + l;
+        const T v = gd[k];
+        uint8_t f = cl[k];
+        if(f == 0 && isClippedPix(v, m, inv)) {
+          f = 1;
+          cl[k] = 1;
+          myClip++;
+        }
+        const double d = f == 0 ? (double)v : 0.0;
+        a += d;
+        a2 += d * d;
       }
+      cS[c] = a;
+      cS2[c] = a2;
+    }
     if(myClip) atomicAdd(&sClip, myClip);
     __syncthreads();
     if(tid == 0) sPrev = sCurr - sClip;
@@ -430,31 +483,41 @@ __global__ void __launch_bounds__(ST_THREADS)
     const bool exactAll = bExact != 0;
     const float fl = bLbv, fi = bInv, fd = bDelta;
     int myOk = 0;
-    for(int i = tid; i < gm.z * gm.w; i += ST_THREADS) {
-      int x = i % gm.z, y = i / gm.z;
-      size_t id = (size_t)(gm.x + x) + (size_t)(gm.y + y) * w;
-      double v = (double)img[id];
-      if(mask[id] != 0 || v <= 1e-10) continue;
-      if(isClipped(v, mean, invStd)) continue;
+    // the pixels of createHistogram (mask 0, above 1e-10, not clipped) are
+    // the good list of phase B (the kernel changes no other mask bit of the
+    // stamp) less the final clip; a warp-uniform trip count lets the lanes of
+    // a warp that land in the same bin (most pixels sit in a few sky bins)
+    // add to it with one atomic
+    for(int base = 0; base < nGood; base += ST_THREADS) {
+      const int k = base + tid;
       int index = -1;
-      if(!exactAll) {
-        const float q = ((float)v - fl) * fi;
-        if(q > 300.f) {
-          index = 255;
-        } else if(q < -50.f) {
-          index = 0;
-        } else {
-          const float f0 = floorf(q), fr = q - f0;
-          if(fr > fd && fr < 1.f - fd) index = min(max((int)f0 + 1, 0), 255);
+      if(k < nGood) {
+        const T pv = gd[k];
+        if(!isClippedPix(pv, mean, invStd)) {
+          if(!exactAll) {
+            const float q = ((float)pv - fl) * fi;
+            if(q > 300.f) {
+              index = 255;
+            } else if(q < -50.f) {
+              index = 0;
+            } else {
+              const float f0 = floorf(q), fr = q - f0;
+              if(fr > fd && fr < 1.f - fd) index = min(max((int)f0 + 1, 0), 255);
+            }
+          }
+          if(index < 0) {
+            const double v = (double)pv;
+            index = satFloorToInt((v - lbv) / bs);
+            index = index == INT_MAX ? INT_MAX : index + 1;
+            index = min(max(index, 0), 255);
+          }
         }
       }
-      if(index < 0) {
-        index = satFloorToInt((v - lbv) / bs);
-        index = index == INT_MAX ? INT_MAX : index + 1;
-        index = min(max(index, 0), 255);
+      const unsigned grp = __match_any_sync(0xffffffffu, index);
+      if(index >= 0) {
+        myOk++;
+        if(lane == __ffs(grp) - 1) atomicAdd(&bins[index], __popc(grp));
       }
-      atomicAdd(&bins[index], 1);
-      myOk++;
     }
     if(myOk) atomicAdd(&okCount, myOk);
     __syncthreads();
@@ -472,36 +535,41 @@ __global__ void __launch_bounds__(ST_THREADS)
         // S / D > S' / D'  <=>  S * D' > S' * D, exact in 64-bit integers.
         // The width is never 0: the window is empty only at the top of the
         // loop, and then the inner loop adds a bin (upper < 255 there).
-        double sumBins = 0.0;
+        // The running sums of bin counts (sumBins, sumExpect) are FP64 in the
+        // reference but hold integers below 2^53, so they are kept in int64
+        // here (no serial FP64 add chain); S < x for an integer S and a double
+        // x is S < ceil(x).
+        long long S = 0;
         long long maxNum = 0, maxDen = 1;  // maxDens = 0 at first
-        const double okTenth = ok / 10.0;
+        const long long tenth = (long long)ceil(ok / 10.0);
         int lowerIndex = 1, upperIndex = 1, maxIndex = -1;
         while(upperIndex < 255) {
-          while(sumBins < okTenth && upperIndex < 255) sumBins += bins[upperIndex++];
-          const long long S = (long long)sumBins, D = upperIndex - lowerIndex;
+          while(S < tenth && upperIndex < 255) S += bins[upperIndex++];
+          const long long D = upperIndex - lowerIndex;
           if(S * maxDen > maxNum * D) {
             maxNum = S;
             maxDen = D;
             maxIndex = lowerIndex;
           }
-          sumBins -= bins[lowerIndex++];
+          S -= bins[lowerIndex++];
         }
         if(maxIndex < 0 || maxIndex > 255) maxIndex = 0;
-        sumBins = 0.0;
-        double sumExpect = 0.0;
-        for(int i = maxIndex; sumBins < ok / 10.0 && i < 255; i++) {
-          sumBins += bins[i];
-          sumExpect += i * bins[i];
+        S = 0;
+        long long E = 0;
+        for(int i = maxIndex; S < tenth && i < 255; i++) {
+          S += bins[i];
+          E += (long long)(i * bins[i]);
         }
-        double modeBin = sumExpect / sumBins + 0.5;
+        double modeBin = (double)E / (double)S + 0.5;
         double skyEst = lowerBinVal + binSize * (modeBin - 1.0);
         double lower = ok * 0.25, upper = ok * 0.75;
-        sumBins = 0.0;
+        const long long lowerCeil = (long long)ceil(lower), upperCeil = (long long)ceil(upper);
+        S = 0;
         int i = 0;
-        while(sumBins < lower) sumBins += bins[i++];
-        lower = i - (sumBins - lower) / bins[i - 1];
-        while(sumBins < upper) sumBins += bins[i++];
-        upper = i - (sumBins - upper) / bins[i - 1];
+        while(S < lowerCeil) S += bins[i++];
+        lower = i - ((double)S - lower) / bins[i - 1];
+        while(S < upperCeil) S += bins[i++];
+        upper = i - ((double)S - upper) / bins[i - 1];
         hSky = skyEst;
         hLower = lower;
         hUpper = upper;
@@ -1191,7 +1259,7 @@ static void sssPass(xb_ctx* c, int* nKept) {
     else
       k_stamp_stats<float><<<nAll, ST_THREADS, 0, c->stream>>>(
           (const float*)c->img[im], c->mask, c->geomAll, c->w, c->h, fSW,
-          c->goodScratch, c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
+          reinterpret_cast<float*>(c->goodScratch), c->clipScratch, chunkBuf, maxChunks, c->p.sigClipAlpha,
           c->p.iqRange, c->skyAll[im], c->fwhmAll[im], draws);
     XB_LAUNCHED(c);
     }
@@ -1441,7 +1509,8 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
   // reads is written first (clip flags and good pixels during the
   // compaction, chunk sums before they are summed).
   xb::k_stamp_stats<float><<<nStamps, xb::ST_THREADS, 0, (cudaStream_t)stream>>>(
-      dImg, dMask, reinterpret_cast<const int4*>(dGeom), w, h, fStampWidth, good, clip, chunks,
+      dImg, dMask, reinterpret_cast<const int4*>(dGeom), w, h, fStampWidth,
+      reinterpret_cast<float*>(good), clip, chunks,
       maxChunks, sigClipAlpha, iqRange, dSky, dFwhm, nullptr);
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
