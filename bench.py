@@ -17,7 +17,8 @@ host->device copy of both FP32 inputs from pinned memory and the
 device->host read of the conv and diff images inside the timed region.
 
 The headline runs 16 frame pairs per step on 16 worker contexts, each frame
-replayed as one captured CUDA graph (--graph 1).  The process asks for 32
+replayed as one captured CUDA graph (--graph 1), with the learned substamp
+order (--rank 1: policy 1 with the shipped weights, xbach/ranker_preset5.npy).  The process asks for 32
 hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS, set before CUDA starts):
 with the default 8, the workers' streams share queues and their graphs
 serialise.
@@ -195,20 +196,36 @@ def run_result(xbach, cx):
             "convTemplate": cx.scalar("convTemplate")}
 
 
-def accuracy(xbach, ctx, pctx, oracle_res, T, S, params):
-    """Chosen vs plain GPU (acceptance: diff within 1e-3 sigma) and both
-    against the FP64 oracle on the same frame pair."""
+def accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx=None, uctx=None):
+    """Chosen vs plain GPU (acceptance: diff within 1e-3 sigma) and against
+    the FP64 oracle on the same frame pair.
+
+    With the learned ranking on, the chosen result is compared with the plain
+    FP64 GPU pipeline running the same ranking (prctx: the same substamp
+    order, so the figures are the precision error alone); the oracle has no
+    ranking, so the mixed pipeline without it (uctx) is compared with the
+    oracle, and ranking_effect gives what the ranking itself changes."""
     from xbach import accuracy as acc
     n_comp, n_bg = acc.layout(params)
     chosen, plain = run_result(xbach, ctx), run_result(xbach, pctx)
-    out = {"chosen_vs_plain": acc.compare(chosen, plain, T, S, n_comp, n_bg),
+    plain_same = run_result(xbach, prctx) if prctx is not None else plain
+    unranked = run_result(xbach, uctx) if uctx is not None else chosen
+    out = {"chosen_vs_plain": acc.compare(chosen, plain_same, T, S, n_comp, n_bg),
            "sigma_definition": "sqrt(|target| + |conv| + 2*5^2) ADU, gain 1"}
+    if uctx is not None:
+        out["chosen_vs_plain"]["reference"] = "plain FP64 GPU pipeline with the same ranking"
+        out["ranking_effect"] = acc.compare(chosen, unranked, T, S, n_comp, n_bg)
+        out["ranking_effect"]["ksc_refills"] = [int(uctx.scalar("ksc_refills")),
+                                                int(ctx.scalar("ksc_refills"))]
+        out["ranking_effect"]["ksc_iterations"] = [int(uctx.scalar("ksc_iterations")),
+                                                   int(ctx.scalar("ksc_iterations"))]
     if oracle_res is not None:
         ref = {"diff": oracle_res.image("diff"), "conv": oracle_res.image("conv"),
                "solution": oracle_res.array("solution", "float64"),
                "kernSum": oracle_res.scalar("kernSum"),
                "convTemplate": oracle_res.scalar("convTemplate")}
-        out["chosen_vs_fp64_oracle"] = acc.compare(chosen, ref, T, S, n_comp, n_bg)
+        key = "mixed_unranked_vs_fp64_oracle" if uctx is not None else "chosen_vs_fp64_oracle"
+        out[key] = acc.compare(unranked, ref, T, S, n_comp, n_bg)
         out["plain_vs_fp64_oracle"] = acc.compare(plain, ref, T, S, n_comp, n_bg)
     return out
 
@@ -334,11 +351,15 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[2, 4],
                     help="2: the headline 2048^2 workload; 4: 64 pairs of mixed size")
     ap.add_argument("--pairs", type=int, default=64, help="--config 4: pairs per step")
+    ap.add_argument("--rank", type=int, default=1,
+                    help="mixed mode: learned substamp order (policy 1, shipped weights) on (1) "
+                         "or off (0)")
     ap.add_argument("--graph", type=int, default=1,
                     help="mixed mode: replay every frame as one captured CUDA graph (1) or run "
                          "the stages host-driven (0)")
     args = ap.parse_args()
     use_graph = bool(args.graph) and args.mode == "mixed"
+    use_rank = bool(args.rank) and args.mode == "mixed"
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 4:
@@ -358,7 +379,14 @@ def main():
         dist.barrier()
         __graft_entry__._paths()
     import xbach
+    from xbach import ranker
     from xbach.synth import make_pair
+    rank_w = ranker.preset5_weights() if use_rank else None
+
+    def with_rank(cx):
+        if use_rank:
+            ranker.enable(cx, rank_w, policy=1, tau=0.5)
+        return cx
 
     B = max(1, args.batch)
     frames = [make_pair(2, frame=rank * B + i) for i in range(B)]
@@ -407,7 +435,7 @@ def main():
         return float(t.item())
 
     # ---- one frame pair per step: per-kernel breakdown ----
-    ctx = xbach.Context(params, device=local)
+    ctx = with_rank(xbach.Context(params, device=local))
     cst = torch.cuda.ExternalStream(ctx.stream())
     single = make_pipeline(ctx)
     for _ in range(args.warmup):
@@ -422,7 +450,8 @@ def main():
                  "fill_w", "fill_finish", "gram_qb", "stamp_test_fit", "cd_select", "weights",
                  "stamp_dots", "build_matrix", "build_rhs", "global_lu", "global_lubksb",
                  "kernel_sum", "sigs", "cd_merit", "ksc_check", "conv_sub", "gram",
-                 "global_ldl", "lu_fallback", "global_solve", "mx_build", "mx_scatter"):
+                 "global_ldl", "lu_fallback", "global_solve", "mx_build", "mx_scatter",
+                 "rank_score"):
         ms, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}
@@ -431,7 +460,7 @@ def main():
     single_graph = None
     if use_graph:
         # the same frame as a replayed graph (one launch, one synchronisation)
-        gctx = xbach.Context(params, device=local)
+        gctx = with_rank(xbach.Context(params, device=local))
         gctx.set_option("graph", 1)
         gC = torch.empty((h, w), dtype=torch.float32, device="cuda")
         gD = torch.empty((h, w), dtype=torch.float32, device="cuda")
@@ -456,6 +485,8 @@ def main():
         batch.set_stream(jst.cuda_stream)
         dC = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
         dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
+        for i in range(batch.n_workers):
+            with_rank(batch.worker(i))
         if use_graph:
             # every worker captures its graph before the timed steps
             batch.set_option("graph", 1)
@@ -533,6 +564,8 @@ def main():
                    "l2": "flushed before every step (256 MB write); each step's inputs exceed L2",
                    "inputs": "device-resident FP32 T,S",
                    "frame_graphs": use_graph,
+                   "learned_ranking": "policy 1, tau 0.5, xbach/ranker_preset5.npy" if use_rank
+                   else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
         "single_frame": {"value": single_value, "unit": UNIT,
@@ -557,8 +590,15 @@ def main():
                              "ms_per_step": p_ms / p_steps, "steps": p_steps}
         line["chosen_over_plain"] = value / line["plain_gpu"]["value"]
         make_pipeline(ctx)()
+        prctx = uctx = None
+        if use_rank:
+            prctx = with_rank(xbach.Context(frame_params(xbach, info, xbach.XB_MODE_PLAIN),
+                                            device=local))
+            make_pipeline(prctx)()
+            uctx = xbach.Context(params, device=local)
+            make_pipeline(uctx)()
         torch.cuda.synchronize()
-        line["accuracy"] = accuracy(xbach, ctx, pctx, oracle_res, T, S, params)
+        line["accuracy"] = accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx, uctx)
         if B > 1:
             same = bool(torch.equal(dD[0].cpu(), torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))))
             line["accuracy"]["batch_frame0_equals_single"] = same

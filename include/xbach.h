@@ -149,8 +149,8 @@ int xb_ctx_set_params(xb_ctx* ctx, const xb_params* p);
  * refit loop) run on the device as conditional nodes; the first frame of a
  * shape (size and parameters) runs stage by stage and is captured, later
  * frames of that shape replay it with one synchronisation.  Results are the
- * stage-by-stage results bit for bit.  Ignored while "trace", "rank" or
- * "time_kernels" is on. */
+ * stage-by-stage results bit for bit (the learned ranking included).
+ * Ignored while "trace" or "time_kernels" is on. */
 int xb_set_option(xb_ctx* ctx, const char* name, long long value);
 
 /* ---- stage API (include/bach.h:66-87) ------------------------------------ */

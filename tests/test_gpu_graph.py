@@ -7,7 +7,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-DECISIONS = ("convTemplate", "ksc_iterations", "sss_retry", "merit0", "merit1", "kernSum",
+DECISIONS = ("convTemplate", "ksc_iterations", "ksc_refills", "sss_retry", "merit0", "merit1", "kernSum",
              "singular")
 
 

@@ -1091,6 +1091,7 @@ void stageKsc(xb_ctx* c) {
   c->dSol = buf<double>(c, "solution", std::max(g.nSol, g.matSize + 1));
   std::vector<int> rejects;
   int iteration = 0;
+  long long refills = 0;  // substamps replaced over the loop
   bool check;
   do {
     solveGlobal(c, si, f, allList, n, nullptr, 1 - si, true, c->dSol);
@@ -1105,6 +1106,7 @@ void stageKsc(xb_ctx* c) {
     }
     std::vector<int> o = toHost(c, outs, 3);
     const int nRefill = o[0];
+    refills += nRefill;
     check = nRefill > 0;
     if(c->trace && nRefill > 0) {
       std::vector<int> po = toHost(c, passOf, n);
@@ -1123,6 +1125,7 @@ void stageKsc(xb_ctx* c) {
   c->singular = toHost(c, f.singular, 1)[0];
   if(mixedMode(c)) checkSolveTimeout(c);
   c->scalars["ksc_iterations"] = iteration;
+  c->scalars["ksc_refills"] = (double)refills;
   c->scalars["singular"] = c->singular;
   if(c->trace) {
     c->put("ksc_rejects", rejects);
@@ -1193,7 +1196,7 @@ long long stageKscGraph(xb_ctx* c) {
   int* outs = buf<int>(c, "ksc_out", 4);
   double* chi2 = buf<double>(c, "ksc_chi2", n);
   c->dSol = buf<double>(c, "solution", std::max(g.nSol, g.matSize + 1));
-  k_zero_ints<<<1, 32, 0, c->stream>>>(graphRec(c) + 2, 2);  // iteration count, overflow
+  k_zero_ints<<<1, 32, 0, c->stream>>>(graphRec(c) + 2, 3);  // iterations, overflow, refills
   XB_LAUNCHED(c);
   const int limit = 4 * n * g.maxSS + 8;
   return graphWhile(c, [&](cudaGraphConditionalHandle h) {

@@ -36,6 +36,7 @@ struct FrameRec {
   int convTemplate;
   int kscIterations;
   int kscOverflow;
+  int kscRefills;
   int singular;
   int timeout;
   double merit[2];
@@ -61,7 +62,7 @@ struct FrameGraphs {
 
 namespace {
 
-constexpr int REC_RETRY = 0, REC_CONVT = 1, REC_KSC_IT = 2, REC_KSC_OVER = 3;
+constexpr int REC_RETRY = 0, REC_CONVT = 1, REC_KSC_IT = 2, REC_KSC_OVER = 3, REC_REFILLS = 4;
 
 __global__ void k_cond_sss_retry(const int* __restrict__ nKept, int nAll,
                                  cudaGraphConditionalHandle h, int* __restrict__ rec) {
@@ -93,6 +94,7 @@ __global__ void k_cond_direction(const double* __restrict__ merit, cudaGraphCond
 __global__ void k_cond_ksc(const int* __restrict__ outs, int limit, int* __restrict__ rec,
                            cudaGraphConditionalHandle h) {
   const int it = ++rec[REC_KSC_IT];
+  rec[REC_REFILLS] += outs[0];
   int more = outs[0] > 0 ? 1 : 0;
   if(more && it > limit) {  // indices only grow, so this cannot happen
     rec[REC_KSC_OVER] = 1;
@@ -114,6 +116,7 @@ __global__ void k_frame_record(const int* __restrict__ nKept, const int* __restr
   out->convTemplate = rec[REC_CONVT];
   out->kscIterations = rec[REC_KSC_IT];
   out->kscOverflow = rec[REC_KSC_OVER];
+  out->kscRefills = rec[REC_REFILLS];
   out->singular = *singular;
   out->timeout = status[1];
   status[1] = 0;  // reported once, as checkSolveTimeout does
@@ -260,6 +263,9 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
   }
   put(p.mode);
   put(c->gramFp64);
+  const int rank = c->rankW ? c->rank : 0;  // the weights are read from the device at replay
+  put(rank);
+  put(c->rankTau);
   return k;
 }
 
@@ -447,7 +453,7 @@ static void captureFrame(xb_ctx* c, FrameGraph& fg) {
 void runFrame(xb_ctx* c, const float* T, const float* S, int w, int h, float* conv, float* diff,
               bool host) {
   const size_t n = (size_t)w * h, bytes = n * sizeof(float);
-  const bool useGraph = c->graph && mixedMode(c) && !c->trace && !c->rank && !c->timeKernels;
+  const bool useGraph = c->graph && mixedMode(c) && !c->trace && !c->timeKernels;
   const cudaMemcpyKind kIn = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const cudaMemcpyKind kOut = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   const float *dT = T, *dS = S;
@@ -558,6 +564,7 @@ void runFrame(xb_ctx* c, const float* T, const float* S, int w, int h, float* co
   c->scalars["merit1"] = c->merit[1];
   c->scalars["convTemplate"] = c->convTemplate;
   c->scalars["ksc_iterations"] = c->kscIterations = r.kscIterations;
+  c->scalars["ksc_refills"] = r.kscRefills;
   c->scalars["singular"] = c->singular = r.singular;
   c->scalars["kernSum"] = c->kernSum = r.kernSum;
   c->scalars["graph_replay"] = 1;

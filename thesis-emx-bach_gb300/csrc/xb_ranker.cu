@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(RK_T)
     k_rank_features(const T* __restrict__ imT, const T* __restrict__ imS,
                     const uint16_t* __restrict__ mask, int w, int h, const int* __restrict__ orig,
                     const int2* __restrict__ ssxy, int maxSS, const int2* __restrict__ cand,
-                    int nCand,
+                    int nCand, const int* __restrict__ liveN,
                     const double* __restrict__ skyT, const double* __restrict__ sigT,
                     const double* __restrict__ skyS, const double* __restrict__ sigS,
                     float threshHigh, float* __restrict__ stats, float* __restrict__ pix) {
@@ -308,7 +308,22 @@ __global__ void __launch_bounds__(RK_T)
   __shared__ float sh[16];
   const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if(i >= nCand) return;
-  const int s = cand[i].x, k = cand[i].y, o = orig[s];
+  // candidates from the list, or (no list) slot i % maxSS of stamp i / maxSS,
+  // whose features are zero when the slot is empty or the stamp not kept
+  int s, k;
+  if(cand) {
+    s = cand[i].x;
+    k = cand[i].y;
+  } else {
+    s = i / maxSS;
+    k = i % maxSS;
+    if((liveN && s >= *liveN) || ssxy[(size_t)s * maxSS + k].x == INT_MAX) {
+      for(int q = tid; q < RK_NS; q += RK_T) stats[(size_t)i * RK_NS + q] = 0.f;
+      for(int q = tid; q < RK_PIX; q += RK_T) pix[(size_t)i * RK_PIX + q] = 0.f;
+      return;
+    }
+  }
+  const int o = orig[s];
   const int2 c = ssxy[(size_t)s * maxSS + k];
   int nValid = 0;
   for(int q = 0; q < maxSS; q++) nValid += ssxy[(size_t)s * maxSS + q].x != INT_MAX;
@@ -422,6 +437,54 @@ __global__ void __launch_bounds__(RK_T)
   }
 }
 
+// The learned order of each kept stamp's candidates (one thread per stamp):
+// the valid slots (a prefix of the stamp's maxSS slots) are reordered by
+// their scores z, policy 1 moving those below zTau behind the others (each
+// group in the reference's order), policy 2 sorting all by descending score
+// (ties in the reference's order).
+__global__ void k_rank_order(int2* __restrict__ ssxy, double* __restrict__ ssval,
+                             const float* __restrict__ z, int nBound,
+                             const int* __restrict__ liveN, int maxSS, int policy, float zTau) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = liveN ? min(*liveN, nBound) : nBound;
+  if(s >= n) return;
+  int2 xy[MAX_MAXSS];
+  double v[MAX_MAXSS];
+  float sc[MAX_MAXSS];
+  int order[MAX_MAXSS];
+  int cnt = 0;
+  for(int k = 0; k < maxSS; k++) {
+    xy[k] = ssxy[(size_t)s * maxSS + k];
+    v[k] = ssval[(size_t)s * maxSS + k];
+    if(xy[k].x != INT_MAX) {
+      sc[cnt] = z[(size_t)s * maxSS + k];
+      order[cnt++] = k;
+    }
+  }
+  if(policy == 2) {
+    for(int a = 1; a < cnt; a++)  // stable insertion sort, descending
+      for(int b = a; b > 0 && sc[b - 1] < sc[b]; b--) {
+        const float t = sc[b - 1];
+        sc[b - 1] = sc[b];
+        sc[b] = t;
+        const int u = order[b - 1];
+        order[b - 1] = order[b];
+        order[b] = u;
+      }
+  } else {
+    int tmp[MAX_MAXSS], m = 0;
+    for(int a = 0; a < cnt; a++)
+      if(sc[a] >= zTau) tmp[m++] = order[a];
+    for(int a = 0; a < cnt; a++)
+      if(!(sc[a] >= zTau)) tmp[m++] = order[a];
+    for(int a = 0; a < cnt; a++) order[a] = tmp[a];
+  }
+  for(int r = 0; r < cnt; r++) {
+    ssxy[(size_t)s * maxSS + r] = xy[order[r]];
+    ssval[(size_t)s * maxSS + r] = v[order[r]];
+  }
+}
+
 }  // namespace
 
 constexpr int kRankParams = RK_NP;
@@ -451,12 +514,12 @@ static void rankFeatures(xb_ctx* c, int si, const std::vector<int2>& cand, float
   if(c->imgIsF64)
     k_rank_features<double><<<n, RK_T, 0, c->stream>>>(
         (const double*)c->img[0], (const double*)c->img[1], c->mask, c->w, c->h, S.orig, S.ssxy,
-        g.maxSS, dCand, n, c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1],
+        g.maxSS, dCand, n, nullptr, c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1],
         (float)c->p.threshHigh, dStats, dPix);
   else
     k_rank_features<float><<<n, RK_T, 0, c->stream>>>(
         (const float*)c->img[0], (const float*)c->img[1], c->mask, c->w, c->h, S.orig, S.ssxy,
-        g.maxSS, dCand, n, c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1],
+        g.maxSS, dCand, n, nullptr, c->skyAll[0], c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1],
         (float)c->p.threshHigh, dStats, dPix);
   XB_LAUNCHED(c);
 }
@@ -466,54 +529,40 @@ static void rankFeatures(xb_ctx* c, int si, const std::vector<int2>& cand, float
 // is on.  rank = 1: candidates whose accept probability is below the
 // threshold (option "rank_tau", in thousandths) move behind the others, each
 // group keeping the reference's order; rank = 2: all by descending score.
+// Everything runs on the device (features of every slot, scores, the
+// per-stamp reorder), so a frame graph captures it; S.dN, when set, holds the
+// kept count and S.n bounds it.
 void rankSubstamps(xb_ctx* c) {
   const float tau = c->rankTau / 1000.f;
   const float zTau = logf(tau / (1.f - tau));  // logit of the threshold
   const Geo& g = c->g;
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
-    std::vector<int2> cand;
-    const int n = rankCandidates(c, si, cand);
-    if(n == 0) continue;
+    if(S.n <= 0) continue;
+    const int n = S.n * g.maxSS;
     float* dStats = buf<float>(c, "rank_stats", (size_t)n * RK_NS);
     float* dPix = buf<float>(c, "rank_pix", (size_t)n * RK_PIX);
     float* dLogit = buf<float>(c, "rank_logit", n);
-    rankFeatures(c, si, cand, dStats, dPix);
+    if(c->imgIsF64)
+      k_rank_features<double><<<n, RK_T, 0, c->stream>>>(
+          (const double*)c->img[0], (const double*)c->img[1], c->mask, c->w, c->h, S.orig,
+          S.ssxy, g.maxSS, nullptr, n, S.dN, c->skyAll[0], c->fwhmAll[0], c->skyAll[1],
+          c->fwhmAll[1], (float)c->p.threshHigh, dStats, dPix);
+    else
+      k_rank_features<float><<<n, RK_T, 0, c->stream>>>(
+          (const float*)c->img[0], (const float*)c->img[1], c->mask, c->w, c->h, S.orig,
+          S.ssxy, g.maxSS, nullptr, n, S.dN, c->skyAll[0], c->fwhmAll[0], c->skyAll[1],
+          c->fwhmAll[1], (float)c->p.threshHigh, dStats, dPix);
+    XB_LAUNCHED(c);
     {
       KT_SCOPE(c, "rank_score");
       k_rank_forward<<<std::min(n, c->smCount * 8), RK_T, 0, c->stream>>>(c->rankW, dStats, dPix,
                                                                           n, dLogit);
       XB_LAUNCHED(c);
     }
-    std::vector<float> z = toHost(c, dLogit, n);
-    std::vector<int2> xy = toHost(c, S.ssxy, (size_t)S.n * g.maxSS);
-    std::vector<double> val = toHost(c, S.ssval, (size_t)S.n * g.maxSS);
-    size_t q = 0;
-    for(int s = 0; s < S.n; s++) {
-      std::vector<std::pair<float, int>> order;
-      while(q < cand.size() && cand[q].x == s) {
-        order.push_back({z[q], cand[q].y});
-        q++;
-      }
-      if(c->rank == 2)
-        std::stable_sort(order.begin(), order.end(),
-                         [](const std::pair<float, int>& a, const std::pair<float, int>& b) {
-                           return a.first > b.first;
-                         });
-      else
-        std::stable_partition(order.begin(), order.end(),
-                              [zTau](const std::pair<float, int>& a) { return a.first >= zTau; });
-      std::vector<int2> nx(xy.begin() + (size_t)s * g.maxSS, xy.begin() + (size_t)(s + 1) * g.maxSS);
-      std::vector<double> nv(val.begin() + (size_t)s * g.maxSS, val.begin() + (size_t)(s + 1) * g.maxSS);
-      for(size_t r = 0; r < order.size(); r++) {
-        nx[r] = xy[(size_t)s * g.maxSS + order[r].second];
-        nv[r] = val[(size_t)s * g.maxSS + order[r].second];
-      }
-      std::copy(nx.begin(), nx.end(), xy.begin() + (size_t)s * g.maxSS);
-      std::copy(nv.begin(), nv.end(), val.begin() + (size_t)s * g.maxSS);
-    }
-    toDevice(c, S.ssxy, xy);
-    toDevice(c, S.ssval, val);
+    k_rank_order<<<(S.n + 127) / 128, 128, 0, c->stream>>>(S.ssxy, S.ssval, dLogit, S.n, S.dN,
+                                                           g.maxSS, c->rank, zTau);
+    XB_LAUNCHED(c);
   }
 }
 

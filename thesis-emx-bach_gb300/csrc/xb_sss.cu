@@ -1378,6 +1378,7 @@ void stageSss(xb_ctx* c) {
       c->set[im].n = nAll;  // bound; the kept count is dIWork[im]
       c->set[im].dN = c->dIWork + im;
     }
+    if(c->rank && c->rankW) rankSubstamps(c);  // learned order, on the device
     c->scalars["stampsx"] = c->stampsx;
     c->scalars["stampsy"] = c->stampsy;
     c->scalars["fStampWidth"] = c->fStampWidth;

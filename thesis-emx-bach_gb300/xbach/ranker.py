@@ -167,3 +167,10 @@ def enable(ctx, weights, policy=1, tau=0.5):
         raise XbError(rc, L.xb_last_error(ctx.h).decode())
     ctx.set_option("rank", policy)
     ctx.set_option("rank_tau", int(round(tau * 1000)))
+
+
+def preset5_weights():
+    """The shipped weights (xbach/ranker_preset5.npy, made by
+    `python -m xbach.train_ranker`): trained on preset-5 defect fields."""
+    import pathlib
+    return np.load(pathlib.Path(__file__).resolve().parent / "ranker_preset5.npy")

@@ -31,6 +31,15 @@ CONFIGS = {
             saturation=None),
 }
 
+# Ranker field, preset 5: preset 2 at 4096^2 with 120k sources and 20x20
+# stamps, plus defects on the substamps the fit would try first: in 2 % of
+# the stamps a hot column of the science image (+300..3000 ADU over the
+# stamp's rows) passes within 3 px of the stamp's brightest unsaturated star,
+# in 5 % that star gets a variable companion 1.5-3 px away (flux 0.3-1 of the
+# primary, science flux off by 20-40 %).
+CONFIGS[5] = dict(CONFIGS[2], size=4096, n_src=120000, stamps=20, bad_col_frac=0.02,
+                  binary_frac=0.05, chunk=16384)
+
 # Basis and orders of preset 3 (keyword arguments of xbach.default_params).
 PARAMS_3 = dict(nGauss=4, dg=[6, 4, 3, 2],
                 bg=[1 / (2 * 0.6 ** 2), 1 / (2 * 1.2 ** 2), 1 / (2 * 2.4 ** 2), 1 / (2 * 4.8 ** 2)],
@@ -96,6 +105,39 @@ def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over
     var = rng.choice(ns, min(15, ns), replace=False)
     flux_s = flux * scale
     flux_s[var] *= 1.0 + rng.uniform(-0.2, 0.2, len(var))
+    # defects on the brightest unsaturated star of chosen stamp cells
+    bad_cols, binaries = [], []
+    if cfg.get("bad_col_frac") or cfg.get("binary_frac"):
+        g = cfg["stamps"]
+        cell = np.minimum((xs * g / n).astype(int), g - 1) + g * np.minimum((ys * g / n).astype(int), g - 1)
+        usable = (flux < 3e5) & ~sat
+        add_x, add_y, add_f, add_fs = [], [], [], []
+        for c in range(g * g):
+            want_col = rng.random() < cfg.get("bad_col_frac", 0.0)
+            want_bin = rng.random() < cfg.get("binary_frac", 0.0)
+            if not (want_col or want_bin):
+                continue
+            idx = np.flatnonzero((cell == c) & usable)
+            if len(idx) == 0:
+                continue
+            k = idx[np.argmax(flux[idx])]
+            if want_bin:
+                r, a = rng.uniform(1.5, 3.0), rng.uniform(0, 2 * np.pi)
+                f2 = flux[k] * rng.uniform(0.3, 1.0)
+                add_x.append(xs[k] + r * np.cos(a))
+                add_y.append(ys[k] + r * np.sin(a))
+                add_f.append(f2)
+                add_fs.append(f2 * scale * (1.0 + rng.choice([-1, 1]) * rng.uniform(0.2, 0.4)))
+                binaries.append((float(xs[k]), float(ys[k])))
+            if want_col:
+                x0 = int(np.clip(round(xs[k]) + rng.integers(-3, 4), 0, n - 1))
+                cy0, cy1 = (c // g) * n // g, ((c // g) + 1) * n // g
+                bad_cols.append((x0, cy0, cy1, float(rng.uniform(300.0, 3000.0))))
+        if add_x:
+            xs = np.concatenate([xs, np.clip(add_x, 0, n - 1)])
+            ys = np.concatenate([ys, np.clip(add_y, 0, n - 1)])
+            flux = np.concatenate([flux, add_f])
+            flux_s = np.concatenate([flux_s, add_fs])
 
     def fwhm_at(rng_fwhm):
         a, b = rng_fwhm
@@ -116,11 +158,13 @@ def make_pair(config=1, frame=0, size=None, n_src=None, dtype=np.float32, **over
         for img in (T, S):
             m = rng.random(img.shape) < cfg["cr_frac"]
             img[m] += rng.uniform(5e3, 5e4, int(m.sum()))
+    for x0, y0, y1, off in bad_cols:
+        S[y0:y1, x0] += off
     if cfg["saturation"]:
         np.minimum(T, cfg["saturation"], out=T)
         np.minimum(S, cfg["saturation"], out=S)
     info = dict(config=config, frame=frame, stamps=cfg["stamps"], size=n, n_src=ns,
-                threshHigh=cfg["saturation"] or 25000.0)
+                threshHigh=cfg["saturation"] or 25000.0, bad_cols=bad_cols, binaries=binaries)
     return T.astype(dtype), S.astype(dtype), info
 
 
