@@ -219,6 +219,8 @@ def accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx=None, uctx=None):
                                                 int(ctx.scalar("ksc_refills"))]
         out["ranking_effect"]["ksc_iterations"] = [int(uctx.scalar("ksc_iterations")),
                                                    int(ctx.scalar("ksc_iterations"))]
+        q = acc.residual_noise([unranked, chosen], T, S)
+        out["ranking_effect"]["residual_noise"] = {"unranked": q[0], "ranked": q[1]}
     if oracle_res is not None:
         ref = {"diff": oracle_res.image("diff"), "conv": oracle_res.image("conv"),
                "solution": oracle_res.array("solution", "float64"),

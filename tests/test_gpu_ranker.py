@@ -188,11 +188,13 @@ def test_ranker_cuts_refits_on_defect_fields():
     import xbach
     from xbach import ranker
     from xbach.synth import make_pair
+    from xbach import accuracy as acc
     w = ranker.preset5_weights()
     tot = {0: [0, 0], 1: [0, 0]}
+    noise = {0: [], 1: []}
     for f in range(1000, 1004):
         T, S, info = make_pair(5, frame=f)
-        ks = {}
+        ks, res = {}, {}
         for rk in (0, 1):
             ctx = xbach.Context(_ranker_params(info))
             if rk:
@@ -201,11 +203,19 @@ def test_ranker_cuts_refits_on_defect_fields():
             tot[rk][0] += int(ctx.scalar("ksc_iterations"))
             tot[rk][1] += int(ctx.scalar("ksc_refills"))
             ks[rk] = ctx.scalar("kernSum")
+            res[rk] = {"diff": ctx.image(xbach.XB_IMG_DIFF), "conv": ctx.image(xbach.XB_IMG_CONV),
+                       "convTemplate": ctx.scalar("convTemplate")}
         assert abs(ks[1] / ks[0] - 1) < 0.02
+        q = acc.residual_noise([res[0], res[1]], T, S)
+        noise[0].append(q[0]["robust_sigma"])
+        noise[1].append(q[1]["robust_sigma"])
     print(f"preset 5, 4 frames: ksc rounds {tot[0][0]} -> {tot[1][0]}, "
-          f"refills {tot[0][1]} -> {tot[1][1]}")
+          f"refills {tot[0][1]} -> {tot[1][1]}, residual robust sigma "
+          f"{np.mean(noise[0]):.4f} -> {np.mean(noise[1]):.4f} sigma")
     assert tot[1][1] <= 0.8 * tot[0][1]
     assert tot[1][0] <= tot[0][0]
+    # the fit is no worse: residual noise of the difference images
+    assert np.mean(noise[1]) <= 1.02 * np.mean(noise[0])
 
 
 def test_ranked_graph_equals_stage_by_stage():

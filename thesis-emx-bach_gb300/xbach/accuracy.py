@@ -61,3 +61,28 @@ def compare(run, ref, T, S, n_comp, n_bg, sigma_rn=SIGMA_RN):
     out.update(fit_error(run["solution"], ref["solution"], n_comp, n_bg))
     out["diff"] = diff_error(run["diff"], ref["diff"], ref["conv"], target, sigma_rn)
     return out
+
+
+def residual_noise(runs, T, S, sigma_rn=SIGMA_RN):
+    """Fit quality of difference images without a ground truth: diff in
+    units of sigma_pix (above), over the pixels every run kept.  A perfect
+    kernel leaves noise; a poorer one leaves residuals around the stars,
+    which widen the bulk of the distribution (robust_sigma = 1.4826 x the
+    median absolute deviation, 1 for pure noise; p90 of |diff|/sigma).  The
+    rms is dominated by cosmic rays, variable stars and defects, which no
+    kernel removes.  runs: dicts with diff, conv, convTemplate."""
+    ok = np.ones(np.shape(T), bool)
+    for r in runs:
+        ok &= np.asarray(r["diff"]) != 1e-30
+    out = []
+    for r in runs:
+        target = S if r["convTemplate"] else T
+        sigma = np.sqrt(np.abs(np.asarray(target, np.float64)) +
+                        np.abs(np.asarray(r["conv"], np.float64)) + 2 * sigma_rn ** 2)
+        e = np.asarray(r["diff"], np.float64)[ok] / sigma[ok]
+        med = np.median(e)
+        a = np.abs(e)
+        out.append({"robust_sigma": float(1.4826 * np.median(np.abs(e - med))),
+                    "p90_sigma": float(np.quantile(a, 0.9)),
+                    "rms_sigma": float(np.sqrt(np.mean(e * e))), "pixels": int(ok.sum())})
+    return out
