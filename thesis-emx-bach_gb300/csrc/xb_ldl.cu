@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(LDL_THREADS)
 // ------------------------------------------------------------------ solve --
 namespace {
 
-constexpr int SV_THREADS = 1024;
+constexpr int SV_THREADS = 512;
 constexpr int SV_NB = 32;  // diagonal block size
 constexpr int SV_AW = 4;   // warps of a 32x32 block product (8 terms each)
 
@@ -335,7 +335,31 @@ __device__ void invertDiagBlock(const double* __restrict__ F, int n, int q, doub
 // the diagonal blocks in Li (shared, nB x 32 x 32).  Per block: the 32x32
 // product with the inverse (warps 0-3, eight terms each), then the next
 // block's rows (warps 0-3) and, at the same time, the rows beyond it
-// (warps 4-31, one row per thread).  part: SV_AW x 32 doubles.
+// (warps 4-15, one row per thread; each loads its row's 32 entries of L at
+// once, since the chain is bound by L2 latency).  part: SV_AW x 32 doubles.
+// sum_t F[s + t][i] x[s + t] over the nb (<= 32) rows of a block: four
+// accumulators over t in steps of four, the remainder into the first; the 32
+// loads are issued before the products.
+__device__ __forceinline__ double rowDot(const double* __restrict__ F, int ld, int s, int nb,
+                                         int i, const double* x) {
+  double f[SV_NB];
+#pragma unroll
+  for(int t = 0; t < SV_NB; t++) f[t] = t < nb ? F[(size_t)(s + t) * ld + i] : 0.0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+  for(int t = 0; t < SV_NB; t += 4)
+    if(t + 4 <= nb) {
+      a0 = fma(f[t], x[s + t], a0);
+      a1 = fma(f[t + 1], x[s + t + 1], a1);
+      a2 = fma(f[t + 2], x[s + t + 2], a2);
+      a3 = fma(f[t + 3], x[s + t + 3], a3);
+    }
+#pragma unroll
+  for(int t = 0; t < SV_NB; t++)
+    if(t >= (nb & ~3) && t < nb) a0 = fma(f[t], x[s + t], a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
 __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restrict__ rinv, int n,
                             const double* Li, double* x, double* part) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, ld = n + 1;
@@ -369,17 +393,8 @@ __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restri
         part[warp * 32 + lane] = acc;
       }
     } else {
-      for(int i = s2 + SV_NB + (tid - SV_AW * 32); i <= n; i += SV_THREADS - SV_AW * 32) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        for(int t = 0; t + 4 <= nb; t += 4) {
-          a0 = fma(F[(size_t)(s + t) * ld + i], x[s + t], a0);
-          a1 = fma(F[(size_t)(s + t + 1) * ld + i], x[s + t + 1], a1);
-          a2 = fma(F[(size_t)(s + t + 2) * ld + i], x[s + t + 2], a2);
-          a3 = fma(F[(size_t)(s + t + 3) * ld + i], x[s + t + 3], a3);
-        }
-        for(int t = nb & ~3; t < nb; t++) a0 = fma(F[(size_t)(s + t) * ld + i], x[s + t], a0);
-        x[i] -= (a0 + a1) + (a2 + a3);
-      }
+      for(int i = s2 + SV_NB + (tid - SV_AW * 32); i <= n; i += SV_THREADS - SV_AW * 32)
+        x[i] -= rowDot(F, ld, s, nb, i, x);
     }
     __syncthreads();
     if(warp == 0 && nb2 > 0 && lane < nb2)
@@ -417,17 +432,8 @@ __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restri
         part[warp * 32 + lane] = acc;
       }
     } else {
-      for(int k = 1 + (tid - SV_AW * 32); k < s2; k += SV_THREADS - SV_AW * 32) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        for(int t = 0; t + 4 <= nb; t += 4) {
-          a0 = fma(F[(size_t)(s + t) * ld + k], x[s + t], a0);
-          a1 = fma(F[(size_t)(s + t + 1) * ld + k], x[s + t + 1], a1);
-          a2 = fma(F[(size_t)(s + t + 2) * ld + k], x[s + t + 2], a2);
-          a3 = fma(F[(size_t)(s + t + 3) * ld + k], x[s + t + 3], a3);
-        }
-        for(int t = nb & ~3; t < nb; t++) a0 = fma(F[(size_t)(s + t) * ld + k], x[s + t], a0);
-        x[k] -= (a0 + a1) + (a2 + a3);
-      }
+      for(int k = 1 + (tid - SV_AW * 32); k < s2; k += SV_THREADS - SV_AW * 32)
+        x[k] -= rowDot(F, ld, s, nb, k, x);
     }
     __syncthreads();
     if(warp == 0 && K > 0)

@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(MX_THREADS)
                const T* __restrict__ sImg, uint16_t* __restrict__ mask, int w, int h,
                double* __restrict__ sig) {
   __shared__ double coeff[MAX_NPSF];
+  __shared__ float cHi[MAX_NPSF], cLo[MAX_NPSF];
   __shared__ double sBg;
   __shared__ double rs[MX_THREADS / 32];
   __shared__ int rc[MX_THREADS / 32];
@@ -274,6 +275,9 @@ __global__ void __launch_bounds__(MX_THREADS)
         }
       }
       coeff[i] = cc;
+      const float hi = (float)cc;
+      cHi[i] = hi;
+      cLo[i] = (float)(cc - (double)hi);
     }
     if(tid == 0) {
       double bg = 0.0, ax = 1.0;
@@ -291,29 +295,44 @@ __global__ void __launch_bounds__(MX_THREADS)
   }
   __syncthreads();
   // The coefficients of an ill-conditioned fit cancel strongly, so the model
-  // is summed in FP64 and stored in FP32 as the reference does.
+  // keeps about 48 bits: each coefficient is hi + lo in FP32, every product
+  // with the (FP32) basis value is split exactly by an FMA, and the sum runs
+  // in double-float (two-sum with a running error term), all on the FP32
+  // pipe.  The model is then stored in FP32 as the reference does, and the
+  // chi^2 terms (which only rank stamps against each other) are FP32.
   const float* Ws = W + (size_t)s * wRows * ldW;
   double acc = 0.0;
   int cnt = 0;
   if(live) {
-    const double bg = sBg;
+    const float bgF = (float)sBg;
+    float part = 0.f;
     for(int j = tid; j < pix; j += MX_THREADS) {
-      double md = 0.0;
-      for(int i = 0; i < nPSF; i++) md = fma(coeff[i], (double)Ws[(size_t)i * ldW + j], md);
-      const float m0 = (float)md;
+      float sh = 0.f, sl = 0.f;
+      for(int i = 0; i < nPSF; i++) {
+        const float wv = Ws[(size_t)i * ldW + j];
+        const float ph = cHi[i] * wv;
+        const float pe = fmaf(cHi[i], wv, -ph) + cLo[i] * wv;  // exact low part + lo term
+        const float ts = sh + ph;                             // two-sum of sh and ph
+        const float bp = ts - sh;
+        const float er = (sh - (ts - bp)) + (ph - bp);
+        sh = ts;
+        sl += er + pe;
+      }
+      const float m0 = (float)((double)sh + (double)sl);
       const int ax = j % fSS - fSS / 2 + c.x, ay = j / fSS - fSS / 2 + c.y;
       const size_t ai = (size_t)min(max(ax, 0), w - 1) + (size_t)min(max(ay, 0), h - 1) * w;
-      const double sD = (double)sImg[ai];
-      if((mask[ai] & BAD_INPUT) == 0 && fabs(sD) > 1e-10) {
-        if(isnan(m0) || isnan(sD)) {
+      const float sF = (float)sImg[ai];
+      if((mask[ai] & BAD_INPUT) == 0 && fabsf(sF) > __double2float_rd(1e-10)) {
+        if(isnan(m0) || isnan(sF)) {
           maskOr(mask, ai, NAN_PIXEL);
         } else {
-          const double diff = (double)m0 - sD + bg;
-          acc += diff * diff / (fabs((double)tImg[ai]) + fabs(sD));
+          const float d = (m0 - sF) + bgF;
+          part += d * d / (fabsf((float)tImg[ai]) + fabsf(sF));
           cnt++;
         }
       }
     }
+    acc = (double)part;
   }
 #pragma unroll
   for(int o = 16; o > 0; o >>= 1) {
