@@ -210,6 +210,8 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->kt.total.clear();
   } else if(n == "gram_fp64") {
     c->gramFp64 = value != 0;
+  } else if(n == "ldl_panel") {
+    c->ldlPanel = value != 0;
   } else if(n == "graph") {
     if(value != 0 && !mixedMode(c)) {
       c->lastError = "frame graphs are built for the mixed mode";

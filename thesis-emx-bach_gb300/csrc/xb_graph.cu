@@ -263,6 +263,7 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
   }
   put(p.mode);
   put(c->gramFp64);
+  put(c->ldlPanel);
   const int rank = c->rankW ? c->rank : 0;  // the weights are read from the device at replay
   put(rank);
   put(c->rankTau);

@@ -165,6 +165,7 @@ struct xb_ctx {
   int tuneForce = -1;    // >= 0: launch this variant of every tunable kernel
   float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
   int mxTables = 0;        // the mixed build's monomial tables are on the device
+  int ldlPanel = 1;        // option "ldl_panel": panel LDL^T kernel (0: the column kernel)
   // frame graphs (xb_graph.cu)
   int graph = 0;           // option "graph": whole frames replay as captured CUDA graphs
   int capturing = 0;       // stage code is being captured: no host reads, no timers

@@ -282,6 +282,185 @@ __global__ void __launch_bounds__(LDL_THREADS)
   cluster.sync();  // no CTA leaves while another may still address its shared memory
 }
 
+// Panel variant (same factors, bit for bit): panels of P columns, panel p
+// owned by CTA p % CL, which applies every earlier panel to it, factors it
+// locally (pivot, then the updates inside the panel, in column order) and
+// copies the P columns to ring slot p % ring of every other CTA with one
+// bulk copy per receiver.  Every column receives the same updates, in the same
+// order, with the same FMAs as in the column kernel above; only the number
+// of cluster-wide exchanges drops (n/P instead of n).  Receivers arm a slot
+// before its copy can come and release it to the sender of panel p + ring
+// (ring <= CL keeps the empty-barrier phases in order).  The protocol is
+// modelled on the CPU in tests/test_ldl_panel_protocol.py.
+template <int CL, int P>
+__global__ void __launch_bounds__(LDL_THREADS)
+    k_global_ldl_panel(const double* __restrict__ M, double* __restrict__ F,
+                       double* __restrict__ rinv, int n, int ring, int* __restrict__ status) {
+  extern __shared__ __align__(16) double ldl_s[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank(), tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = LDL_THREADS / 32;
+  const int ld = n + 1;
+  const int LC = (n + 3) & ~1;
+  const int nP = (n + P - 1) / P, lpn = (nP + CL - 1) / CL, lastSent = nP - 2;
+  double* col = ldl_s;                                // lpn * P x LC (panel lp = p / CL)
+  double* slot = col + (size_t)lpn * P * LC;          // ring x P x LC
+  double* rvec = slot + (size_t)ring * P * LC;        // LC
+  unsigned long long* bars = (unsigned long long*)(rvec + LC);  // ring full + 1 empty
+  __shared__ int sErr;
+  const unsigned long long deadline = globalTimer() + LDL_WAIT_NS;
+  const uint32_t panelBytes = (uint32_t)P * (uint32_t)LC * 8u;
+  auto ownerOf = [](int p) { return p % CL; };
+  auto localCol = [&](int k) {  // column k (1-based) of a panel owned here
+    const int p = (k - 1) / P;
+    return col + (size_t)((p / CL) * P + (k - 1) % P) * LC;
+  };
+
+  for(int lp = 0; lp < lpn; lp++) {
+    const int p = lp * CL + rank;
+    for(int q = 0; q < P; q++) {
+      const int k = 1 + p * P + q;
+      double* ck = col + (size_t)(lp * P + q) * LC;
+      for(int i = tid; i < LC; i += LDL_THREADS)
+        ck[i] = (p < nP && k <= n && i <= n) ? M[(size_t)k * ld + i] : 0.0;
+    }
+  }
+  for(int i = tid; i < LC; i += LDL_THREADS) rvec[i] = 0.0;
+  if(tid == 0) {
+    sErr = 0;
+    for(int r = 0; r < ring; r++) mbarInit(smemAddr(&bars[r]), 1);
+    mbarInit(smemAddr(&bars[ring]), CL - 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for(int r = 0; r < ring; r++)
+      for(int p = r; p <= lastSent; p += ring)
+        if(ownerOf(p) != rank) {
+          mbarArriveExpect(smemAddr(&bars[r]), panelBytes);
+          break;
+        }
+  }
+  __syncthreads();
+  cluster.sync();
+
+  uint32_t phaseBits = 0, emptyPhase = 0;
+  volatile int* vErr = &sErr;
+
+  // pivots and in-panel updates of panel p (owned, earlier panels applied)
+  auto factorPanel = [&](int p) {
+    const int first = 1 + p * P, last = min(n, first + P - 1);
+    for(int j = first; j <= last; j++) {
+      double* cj = localCol(j);
+      if(tid == 0) {
+        const double d = cj[j];
+        double r = recipFast(d);
+        if(!(d > 0.0) || !isfinite(r)) {
+          atomicOr(status, 1);
+          r = 0.0;
+        }
+        rvec[j] = r;
+        cj[((j + 1) & ~1) - 2] = r;  // travels with the column, above its diagonal
+      }
+      __syncthreads();
+      const double r = rvec[j];
+      for(int k = j + 1 + warp; k <= last; k += NW) {
+        double* ck = localCol(k);
+        const double cf = cj[k] * r;
+        for(int i = k + lane; i <= n; i += 32) ck[i] = fma(-cj[i], cf, ck[i]);
+      }
+      __syncthreads();
+    }
+  };
+  // panel p (base: its P columns) applied to the local columns of the panels
+  // [pFrom, pTo]: per entry, the panel's columns in order
+  auto applyPanel = [&](const double* base, int p, int pFrom, int pTo) {
+    const int first = 1 + p * P, w = min(P, n - first + 1);
+    double rq[P];
+#pragma unroll
+    for(int q = 0; q < P; q++) rq[q] = q < w ? base[(size_t)q * LC + ((first + q + 1) & ~1) - 2] : 0.0;
+    const int lp0 = (pFrom - rank + CL - 1) / CL;  // first local panel >= pFrom
+    for(int e = warp; ; e += NW) {
+      const int lp = lp0 + e / P, q = e % P, pk = lp * CL + rank, k = 1 + pk * P + q;
+      if(pk > pTo || pk >= nP || k > n) break;
+      double* ck = col + (size_t)(lp * P + q) * LC;
+      double cf[P];
+#pragma unroll
+      for(int u = 0; u < P; u++) cf[u] = u < w ? base[(size_t)u * LC + k] * rq[u] : 0.0;
+      for(int i = k + lane; i <= n; i += 32) {
+        double v = ck[i];
+#pragma unroll
+        for(int u = 0; u < P; u++)
+          if(u < w) v = fma(-base[(size_t)u * LC + i], cf[u], v);
+        ck[i] = v;
+      }
+    }
+  };
+  auto sendPanel = [&](int p) {
+    if(tid == 0) {
+      if(p >= ring) waitPhase(smemAddr(&bars[ring]), emptyPhase, deadline, vErr, status);
+      const int sl = p % ring;
+      const uint32_t src = smemAddr(localCol(1 + p * P));
+      const uint32_t dst = smemAddr(slot + (size_t)sl * P * LC);
+      const uint32_t fullA = smemAddr(&bars[sl]);
+      for(int q = 0; q < CL; q++)
+        if(q != rank) bulkCopyCluster(mapaRank(dst, q), src, panelBytes, mapaRank(fullA, q));
+    }
+    if(p >= ring) emptyPhase ^= 1u;
+  };
+
+  if(ownerOf(0) == rank) {
+    factorPanel(0);
+    fenceProxyAsync();
+    __syncthreads();
+    if(0 <= lastSent) sendPanel(0);
+  }
+  for(int p = 0; p < nP - 1; p++) {
+    const int sl = p % ring;
+    const bool own = ownerOf(p) == rank;
+    const double* base;
+    if(own) {
+      base = localCol(1 + p * P);
+    } else {
+      base = slot + (size_t)sl * P * LC;
+      waitPhase(smemAddr(&bars[sl]), (phaseBits >> sl) & 1u, deadline, vErr, status);
+      phaseBits ^= 1u << sl;
+    }
+    const bool ahead = ownerOf(p + 1) == rank;
+    if(ahead) {  // look-ahead: the next panel first, factored and sent
+      applyPanel(base, p, p + 1, p + 1);
+      __syncthreads();
+      factorPanel(p + 1);
+      fenceProxyAsync();
+      __syncthreads();
+      if(p + 1 <= lastSent) sendPanel(p + 1);
+    }
+    applyPanel(base, p, ahead ? p + 2 : p + 1, nP - 1);
+    __syncthreads();
+    if(!own && tid == 0) {
+      for(int pn = p + ring; pn <= lastSent; pn += ring)
+        if(ownerOf(pn) != rank) {
+          mbarArriveExpect(smemAddr(&bars[sl]), panelBytes);
+          break;
+        }
+      if(p + ring <= lastSent) mbarArriveCluster(mapaRank(smemAddr(&bars[ring]), ownerOf(p + ring)));
+    }
+  }
+  __syncthreads();
+  for(int lp = 0; lp < lpn; lp++)
+    for(int q = 0; q < P; q++) {
+      const int k = 1 + (lp * CL + rank) * P + q;
+      if(k > n) break;
+      const double* ck = col + (size_t)(lp * P + q) * LC;
+      const double rk = rvec[k];
+      for(int i = k + tid; i <= n; i += LDL_THREADS) {
+        const double v = i == k ? ck[k] : ck[i] * rk;
+        F[(size_t)k * ld + i] = v;
+        F[(size_t)i * ld + k] = v;
+      }
+      if(tid == 0) rinv[k] = rk;
+    }
+  cluster.sync();  // no CTA leaves while another may still address its shared memory
+}
+
 // ------------------------------------------------------------------ solve --
 namespace {
 
@@ -508,6 +687,12 @@ __global__ void __launch_bounds__(SV_THREADS)
 }
 
 template __global__ void k_global_ldl<8>(const double*, double*, double*, int, int*);
+template __global__ void k_global_ldl_panel<16, 2>(const double*, double*, double*, int, int, int*);
+template __global__ void k_global_ldl_panel<16, 4>(const double*, double*, double*, int, int, int*);
+template __global__ void k_global_ldl_panel<16, 8>(const double*, double*, double*, int, int, int*);
+template __global__ void k_global_ldl_panel<8, 2>(const double*, double*, double*, int, int, int*);
+template __global__ void k_global_ldl_panel<8, 4>(const double*, double*, double*, int, int, int*);
+template __global__ void k_global_ldl_panel<8, 8>(const double*, double*, double*, int, int, int*);
 template __global__ void k_global_ldl<16>(const double*, double*, double*, int, int*);
 template __global__ void k_ldl_solve<8>(const double*, const double*, const double*, int, double*,
                                         const int*, double*);
@@ -520,6 +705,14 @@ size_t ldlSmemBytes(int n, int CL) {
   const int LC = (n + 3) & ~1, ncol = (n + CL - 1) / CL;
   return ((size_t)ncol * LC + (size_t)LDL_RING * LC + LC) * sizeof(double) +
          (LDL_RING + 1) * sizeof(unsigned long long);
+}
+
+// Shared memory of the panel kernel: the owned panels, the receive ring, the
+// pivots and the barriers.
+size_t ldlPanelSmemBytes(int n, int CL, int P, int ring) {
+  const int LC = (n + 3) & ~1, nP = (n + P - 1) / P, lpn = (nP + CL - 1) / CL;
+  return ((size_t)lpn * P * LC + (size_t)ring * P * LC + LC) * sizeof(double) +
+         (size_t)(ring + 1) * sizeof(unsigned long long);
 }
 
 template <class Kern, class... Args>
@@ -569,20 +762,58 @@ void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, 
   // 16-CTA clusters where the device allows them, else 8
   static std::atomic<int> clusterSize{0};
   {
+    // Variants with the same factors bit for bit: the column kernel (0) and
+    // panels of 2, 4 or 8 columns (1-3), where shared memory holds a receive
+    // ring of at least two panels.  Wider panels need fewer cluster-wide
+    // exchanges but put more FP64 work on the owner of the next panel (the
+    // look-ahead), so the autotuner times them.
+    int maxSmem = 0;
+    XB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    auto ringFor = [&](int CL, int P) {
+      for(int rg = std::min(4, CL); rg >= 2; rg--)
+        if(ldlPanelSmemBytes(n, CL, P, rg) <= (size_t)maxSmem) return rg;
+      return 0;
+    };
+    auto launchVariant = [&](int v, int CL) -> cudaError_t {
+      const int P = v == 1 ? 2 : v == 2 ? 4 : 8;
+      const int rg = v > 0 ? ringFor(CL, P) : 0;
+      if(v == 0 || rg == 0)
+        return CL == 16 ? launchCluster(c, k_global_ldl<16>, 16, LDL_THREADS, ldlSmemBytes(n, 16),
+                                        M, F, rinv, n, status)
+                        : launchCluster(c, k_global_ldl<8>, 8, LDL_THREADS, ldlSmemBytes(n, 8), M,
+                                        F, rinv, n, status);
+      const size_t sm = ldlPanelSmemBytes(n, CL, P, rg);
+      if(CL == 16)
+        return P == 2 ? launchCluster(c, k_global_ldl_panel<16, 2>, 16, LDL_THREADS, sm, M, F, rinv,
+                                      n, rg, status)
+             : P == 4 ? launchCluster(c, k_global_ldl_panel<16, 4>, 16, LDL_THREADS, sm, M, F, rinv,
+                                      n, rg, status)
+                      : launchCluster(c, k_global_ldl_panel<16, 8>, 16, LDL_THREADS, sm, M, F, rinv,
+                                      n, rg, status);
+      return P == 2 ? launchCluster(c, k_global_ldl_panel<8, 2>, 8, LDL_THREADS, sm, M, F, rinv, n,
+                                    rg, status)
+           : P == 4 ? launchCluster(c, k_global_ldl_panel<8, 4>, 8, LDL_THREADS, sm, M, F, rinv, n,
+                                    rg, status)
+                    : launchCluster(c, k_global_ldl_panel<8, 8>, 8, LDL_THREADS, sm, M, F, rinv, n,
+                                    rg, status);
+    };
+    // 16-CTA clusters where the device allows them, else 8
+    auto launch = [&](int v) {
+      cudaError_t e = cudaErrorUnknown;
+      if(clusterSize.load() != 8) {
+        e = launchVariant(v, 16);
+        if(e == cudaSuccess) clusterSize = 16;
+        else cudaGetLastError();
+      }
+      if(e != cudaSuccess) {
+        XB_CUDA(launchVariant(v, 8));
+        clusterSize = 8;
+      }
+      XB_LAUNCHED(c);
+    };
+    const int v = c->ldlPanel ? tunedVariant(c, "global_ldl", n, 4, launch) : 0;
     KT_SCOPE(c, "global_ldl");
-    cudaError_t e = cudaErrorUnknown;
-    if(clusterSize.load() != 8) {
-      e = launchCluster(c, k_global_ldl<16>, 16, LDL_THREADS, ldlSmemBytes(n, 16), M, F, rinv, n,
-                        status);
-      if(e == cudaSuccess) clusterSize = 16;
-      else cudaGetLastError();
-    }
-    if(e != cudaSuccess) {
-      XB_CUDA(launchCluster(c, k_global_ldl<8>, 8, LDL_THREADS, ldlSmemBytes(n, 8), M, F, rinv, n,
-                            status));
-      clusterSize = 8;
-    }
-    XB_LAUNCHED(c);
+    launch(v);
   }
   luFallbackSolve(c, M, F, n, rhs, piv, singular, status);
   {
