@@ -110,9 +110,22 @@ __global__ void __launch_bounds__(MX_THREADS)
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS;
   float* Ws = W + (size_t)s * wRows * ldW;
   const bool live = cur[s] < count[s];
-  for(int n = 1; n < nPSF; n++) {
-    if(kx[n] % 2 != 0 || ky[n] % 2 != 0) continue;
-    for(int p = tid; p < wCols; p += MX_THREADS) Ws[(size_t)n * ldW + p] -= Ws[p];
+  // W[n] -= W[0] for the even/even rows: each thread takes its pixels
+  // through all such rows (independent loads in flight, not one pass per row)
+  __shared__ short evenRows[MAX_NPSF];
+  __shared__ int nEven;
+  if(tid == 0) {
+    int m = 0;
+    for(int n = 1; n < nPSF; n++)
+      if(kx[n] % 2 == 0 && ky[n] % 2 == 0) evenRows[m++] = (short)n;
+    nEven = m;
+  }
+  __syncthreads();
+  const int ne = nEven;
+  for(int p = tid; p < wCols; p += MX_THREADS) {
+    const float w0 = Ws[p];
+#pragma unroll 8
+    for(int e = 0; e < ne; e++) Ws[(size_t)evenRows[e] * ldW + p] -= w0;
   }
   int2 c = make_int2(0, 0);
   if(live) c = ssxy[(size_t)s * maxSS + cur[s]];

@@ -928,13 +928,19 @@ __global__ void __launch_bounds__(FS_T, 1)
   const int cx = gm.x, cy = gm.y, sx = gm.z, sy = gm.w, n = fSW, N = n * n;
   const double invFwhm = 1.0 / fwhm;
   float* V = (float*)fs_s;                 // N pixel values
-  uint32_t* key = (uint32_t*)(V + N);      // N (0: not a local-maximum candidate)
-  uint16_t* arg = (uint16_t*)(key + N);    // N (0xFFFF: none)
+  uint16_t* arg = (uint16_t*)(V + N);      // N (0xFFFF: none)
   uint8_t* flags = (uint8_t*)(arg + N);    // N
   uint8_t* bad = flags + N;                // N
   uint8_t* hx = bad + N;                   // N (0xFF: none)
   uint8_t* rowf = hx + N;                  // N
   uint8_t* okw = rowf + N;                 // N
+  // block scans of the map build: prefix / suffix argmax (index in the row
+  // or column, 0xFF: none) and prefix / suffix OR within blocks of the window
+  // width
+  uint8_t* tPA = okw + N;                  // N
+  uint8_t* tSA = tPA + N;                  // N
+  uint8_t* tPO = tSA + N;                  // N
+  uint8_t* tSO = tPO + N;                  // N
   __shared__ int2 locXY[MAX_MAXSS];
   __shared__ double locVal[MAX_MAXSS];
   __shared__ int sBest;
@@ -988,61 +994,146 @@ __global__ void __launch_bounds__(FS_T, 1)
     flags[p] = fl;
   }
   __syncthreads();
-  // maps of the current bad state (keys, window argmax, window ORs) over the
-  // columns [x0, x1] of the rows [k0, k1] (keys and row maps) and [r0, r1]
+  // maps of the current bad state (window argmax of the keys, window ORs)
+  // over the columns [x0, x1] of the rows [k0, k1] (row maps) and [r0, r1]
   // (column maps); the full build covers the stamp.  After an acceptance
-  // only the accepted window's bad bits change, so only keys inside it, row
-  // maps within hSS of it in x and column maps within hSS of it in x and y
-  // can change: rebuilding that region gives the maps of a full rebuild.
+  // only the accepted window's bad bits change, so only row maps within hSS
+  // of it in x and column maps within hSS of it in x and y can change:
+  // rebuilding that region gives the maps of a full rebuild.
+  // A key is the float bit pattern of a qualifying pixel (0: none).  Window
+  // argmax and OR use the van Herk / Gil-Werman scheme: split the line into
+  // blocks of the window width W, scan each block forwards (prefix) and
+  // backwards (suffix); the window [a, b] is then suffix(a) with prefix(b)
+  // when they lie in different blocks, prefix(b) when a starts its block,
+  // suffix(a) otherwise (b is then the line's end).  Ties keep the smaller
+  // index: the prefix updates on a larger key, the suffix on a larger or
+  // equal one, and prefix(b) wins only with a larger key.
+  const int W = 2 * hSS + 1;
+  auto keyAt = [&](int p) -> uint32_t {
+    const uint8_t fl = flags[p];
+    return (!bad[p] && (fl & FL_KFQ) && (fl & FL_VPOS)) ? __float_as_uint(V[p]) : 0u;
+  };
+  auto orAt = [&](int p) -> uint8_t {
+    const uint8_t fl = flags[p];
+    return (bad[p] ? OK_BAD : 0) | ((fl & FL_PRED) ? OK_PRED : 0) | ((fl & FL_NONPOS) ? OK_NONPOS : 0);
+  };
   auto build = [&](int x0, int x1, int k0, int k1, int r0, int r1) {
-    const int kw = x1 - x0 + 1;
-    for(int i = tid; i < kw * (k1 - k0 + 1); i += FS_T) {
-      const int p = (k0 + i / kw) * n + x0 + i % kw;
-      const uint8_t fl = flags[p];
-      key[p] = (!bad[p] && (fl & FL_KFQ) && (fl & FL_VPOS)) ? __float_as_uint(V[p]) : 0u;
-    }
-    __syncthreads();
-    for(int ly = k0 + warp; ly <= k1; ly += NW)
-      for(int lx = x0 + lane; lx <= x1; lx += 32) {
-        const int row = ly * n;
+    // ---- rows [k0, k1]: block scans along x over the blocks under the windows
+    {
+      const int ba = max(x0 - hSS, 0) / W, bb = min(x1 + hSS, n - 1) / W;
+      const int nr = k1 - k0 + 1, nTask = nr * (bb - ba + 1);
+      for(int t = tid; t < nTask; t += FS_T) {
+        const int ly = k0 + t % nr, blk = ba + t / nr, row = ly * n;
+        const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
         uint32_t bk = 0;
         int bi = 0xFF;
-        for(int x = max(lx - hSS, 0); x <= min(lx + hSS, n - 1); x++) {
-          const uint32_t k = key[row + x];
-          if(k > bk) {  // ascending x: ties keep the smallest x
+        uint8_t o = 0;
+        for(int x = b0; x <= b1; x++) {
+          const int p = row + x;
+          const uint32_t k = keyAt(p);
+          if(k > bk) {
             bk = k;
             bi = x;
           }
+          if(x < sx) o |= orAt(p);
+          tPA[p] = (uint8_t)bi;
+          tPO[p] = o;
         }
-        hx[row + lx] = bk ? (uint8_t)bi : (uint8_t)0xFF;
-        uint8_t o = 0;
-        for(int x = max(lx - hSS, 0); x <= min(lx + hSS, sx - 1); x++) {
-          const uint8_t f = flags[row + x];
-          o |= bad[row + x] ? OK_BAD : 0;
-          o |= (f & FL_PRED) ? OK_PRED : 0;
-          o |= (f & FL_NONPOS) ? OK_NONPOS : 0;
-        }
-        rowf[row + lx] = o;
-      }
-    __syncthreads();
-    for(int ly = r0 + warp; ly <= r1; ly += NW)
-      for(int lx = x0 + lane; lx <= x1; lx += 32) {
-        uint32_t bk = 0;
-        int bi = 0xFFFF;
-        for(int y = max(ly - hSS, 0); y <= min(ly + hSS, n - 1); y++) {
-          const uint8_t xx = hx[y * n + lx];
-          if(xx == 0xFF) continue;
-          const uint32_t k = key[y * n + xx];
-          if(k > bk) {  // ascending y: the first row keeps ties
+        bk = 0;
+        bi = 0xFF;
+        o = 0;
+        for(int x = b1; x >= b0; x--) {
+          const int p = row + x;
+          const uint32_t k = keyAt(p);
+          if(k != 0 && k >= bk) {
             bk = k;
-            bi = y * n + xx;
+            bi = x;
           }
+          if(x < sx) o |= orAt(p);
+          tSA[p] = (uint8_t)bi;
+          tSO[p] = o;
         }
-        arg[ly * n + lx] = (uint16_t)bi;
+      }
+    }
+    __syncthreads();
+    const int kw = x1 - x0 + 1;
+    for(int i = tid; i < (k1 - k0 + 1) * kw; i += FS_T) {
+      const int ly = k0 + i / kw, lx = x0 + i % kw, row = ly * n;
+      const int a = max(lx - hSS, 0), b = min(lx + hSS, n - 1);
+      uint8_t h, o;
+      if(a / W != b / W) {
+        const uint8_t L = tSA[row + a], R = tPA[row + b];
+        h = L == 0xFF ? R : R == 0xFF ? L : (keyAt(row + R) > keyAt(row + L) ? R : L);
+        o = tSO[row + a] | tPO[row + b];
+      } else if(a % W == 0) {
+        h = tPA[row + b];
+        o = tPO[row + b];
+      } else {
+        h = tSA[row + a];
+        o = tSO[row + a];
+      }
+      hx[row + lx] = h;
+      rowf[row + lx] = o;
+    }
+    __syncthreads();
+    // ---- columns [x0, x1]: block scans along y of the row winners
+    {
+      const int ba = max(r0 - hSS, 0) / W, bb = min(r1 + hSS, n - 1) / W;
+      const int nTask = kw * (bb - ba + 1);
+      auto candKey = [&](int y, int lx) -> uint32_t {
+        const uint8_t xx = hx[y * n + lx];
+        return xx == 0xFF ? 0u : keyAt(y * n + xx);
+      };
+      for(int t = tid; t < nTask; t += FS_T) {
+        const int lx = x0 + t % kw, blk = ba + t / kw;
+        const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
+        uint32_t bk = 0;
+        int bi = 0xFF;
         uint8_t o = 0;
-        for(int y = max(ly - hSS, 0); y <= min(ly + hSS, sy - 1); y++) o |= rowf[y * n + lx];
+        for(int y = b0; y <= b1; y++) {
+          const uint32_t k = candKey(y, lx);
+          if(k > bk) {
+            bk = k;
+            bi = y;
+          }
+          if(y < sy) o |= rowf[y * n + lx];
+          tPA[y * n + lx] = (uint8_t)bi;
+          tPO[y * n + lx] = o;
+        }
+        bk = 0;
+        bi = 0xFF;
+        o = 0;
+        for(int y = b1; y >= b0; y--) {
+          const uint32_t k = candKey(y, lx);
+          if(k != 0 && k >= bk) {
+            bk = k;
+            bi = y;
+          }
+          if(y < sy) o |= rowf[y * n + lx];
+          tSA[y * n + lx] = (uint8_t)bi;
+          tSO[y * n + lx] = o;
+        }
+      }
+      __syncthreads();
+      for(int i = tid; i < (r1 - r0 + 1) * kw; i += FS_T) {
+        const int ly = r0 + i / kw, lx = x0 + i % kw;
+        const int a = max(ly - hSS, 0), b = min(ly + hSS, n - 1);
+        uint8_t yb, o;
+        if(a / W != b / W) {
+          const uint8_t L = tSA[a * n + lx], R = tPA[b * n + lx];
+          yb = L == 0xFF ? R : R == 0xFF ? L : (candKey(R, lx) > candKey(L, lx) ? R : L);
+          o = tSO[a * n + lx] | tPO[b * n + lx];
+        } else if(a % W == 0) {
+          yb = tPA[b * n + lx];
+          o = tPO[b * n + lx];
+        } else {
+          yb = tSA[a * n + lx];
+          o = tSO[a * n + lx];
+        }
+        arg[ly * n + lx] = yb == 0xFF ? (uint16_t)0xFFFF : (uint16_t)(yb * n + hx[yb * n + lx]);
         okw[ly * n + lx] = o;
       }
+    }
     __syncthreads();
   };
   build(0, n - 1, 0, n - 1, 0, n - 1);
