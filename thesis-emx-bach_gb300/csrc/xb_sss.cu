@@ -955,22 +955,23 @@ __global__ void __launch_bounds__(FS_T, 1)
       V[ly * n + lx] = img[a];
       bad[ly * n + lx] = (ldMask(mask, a) & badMask) ? 1 : 0;
     }
-  // exact thresholds of the two static predicates
-  if(warp == 0) {
+  // exact thresholds of the two static predicates (one warp each)
+  if(warp < 2) {
     auto pr = [&](double v) { return (v - sky) / fwhm > tKF; };
     auto kq = [&](double v) { return !((v - sky) * invFwhm < tKF); };
     const bool direct = !(fwhm > 0.0 && isfinite(fwhm) && isfinite(sky) && isfinite(invFwhm) &&
                           pr(INFINITY) && !pr(-INFINITY) && kq(INFINITY) && !kq(-INFINITY));
     if(!direct) {
       const unsigned long long kLo = dKey(-INFINITY), kHi = dKey(INFINITY);
-      const unsigned long long kP = warpFirstTrue(kLo, kHi, pr);
-      const unsigned long long kK = warpFirstTrue(kLo, kHi, kq);
-      if(lane == 0) {
-        sfP = __double2float_ru(keyD(kP));  // pr(v) <=> v >= sfP for a float v
-        sfK = __double2float_ru(keyD(kK));
+      if(warp == 0) {
+        const unsigned long long kP = warpFirstTrue(kLo, kHi, pr);
+        if(lane == 0) sfP = __double2float_ru(keyD(kP));  // pr(v) <=> v >= sfP for a float v
+      } else {
+        const unsigned long long kK = warpFirstTrue(kLo, kHi, kq);
+        if(lane == 0) sfK = __double2float_ru(keyD(kK));
       }
     }
-    if(lane == 0) sDirect = direct;
+    if(warp == 0 && lane == 0) sDirect = direct;
   }
   __syncthreads();
   const bool direct = sDirect != 0;
@@ -1022,36 +1023,38 @@ __global__ void __launch_bounds__(FS_T, 1)
     {
       const int ba = max(x0 - hSS, 0) / W, bb = min(x1 + hSS, n - 1) / W;
       const int nr = k1 - k0 + 1, nTask = nr * (bb - ba + 1);
-      for(int t = tid; t < nTask; t += FS_T) {
-        const int ly = k0 + t % nr, blk = ba + t / nr, row = ly * n;
+      for(int t = tid; t < 2 * nTask; t += FS_T) {  // prefix and suffix on separate threads
+        const bool suffix = t >= nTask;
+        const int tt = suffix ? t - nTask : t;
+        const int ly = k0 + tt % nr, blk = ba + tt / nr, row = ly * n;
         const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
         uint32_t bk = 0;
         int bi = 0xFF;
         uint8_t o = 0;
-        for(int x = b0; x <= b1; x++) {
-          const int p = row + x;
-          const uint32_t k = keyAt(p);
-          if(k > bk) {
-            bk = k;
-            bi = x;
+        if(!suffix) {
+          for(int x = b0; x <= b1; x++) {
+            const int p = row + x;
+            const uint32_t k = keyAt(p);
+            if(k > bk) {
+              bk = k;
+              bi = x;
+            }
+            if(x < sx) o |= orAt(p);
+            tPA[p] = (uint8_t)bi;
+            tPO[p] = o;
           }
-          if(x < sx) o |= orAt(p);
-          tPA[p] = (uint8_t)bi;
-          tPO[p] = o;
-        }
-        bk = 0;
-        bi = 0xFF;
-        o = 0;
-        for(int x = b1; x >= b0; x--) {
-          const int p = row + x;
-          const uint32_t k = keyAt(p);
-          if(k != 0 && k >= bk) {
-            bk = k;
-            bi = x;
+        } else {
+          for(int x = b1; x >= b0; x--) {
+            const int p = row + x;
+            const uint32_t k = keyAt(p);
+            if(k != 0 && k >= bk) {
+              bk = k;
+              bi = x;
+            }
+            if(x < sx) o |= orAt(p);
+            tSA[p] = (uint8_t)bi;
+            tSO[p] = o;
           }
-          if(x < sx) o |= orAt(p);
-          tSA[p] = (uint8_t)bi;
-          tSO[p] = o;
         }
       }
     }
@@ -1084,34 +1087,36 @@ __global__ void __launch_bounds__(FS_T, 1)
         const uint8_t xx = hx[y * n + lx];
         return xx == 0xFF ? 0u : keyAt(y * n + xx);
       };
-      for(int t = tid; t < nTask; t += FS_T) {
-        const int lx = x0 + t % kw, blk = ba + t / kw;
+      for(int t = tid; t < 2 * nTask; t += FS_T) {
+        const bool suffix = t >= nTask;
+        const int tt = suffix ? t - nTask : t;
+        const int lx = x0 + tt % kw, blk = ba + tt / kw;
         const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
         uint32_t bk = 0;
         int bi = 0xFF;
         uint8_t o = 0;
-        for(int y = b0; y <= b1; y++) {
-          const uint32_t k = candKey(y, lx);
-          if(k > bk) {
-            bk = k;
-            bi = y;
+        if(!suffix) {
+          for(int y = b0; y <= b1; y++) {
+            const uint32_t k = candKey(y, lx);
+            if(k > bk) {
+              bk = k;
+              bi = y;
+            }
+            if(y < sy) o |= rowf[y * n + lx];
+            tPA[y * n + lx] = (uint8_t)bi;
+            tPO[y * n + lx] = o;
           }
-          if(y < sy) o |= rowf[y * n + lx];
-          tPA[y * n + lx] = (uint8_t)bi;
-          tPO[y * n + lx] = o;
-        }
-        bk = 0;
-        bi = 0xFF;
-        o = 0;
-        for(int y = b1; y >= b0; y--) {
-          const uint32_t k = candKey(y, lx);
-          if(k != 0 && k >= bk) {
-            bk = k;
-            bi = y;
+        } else {
+          for(int y = b1; y >= b0; y--) {
+            const uint32_t k = candKey(y, lx);
+            if(k != 0 && k >= bk) {
+              bk = k;
+              bi = y;
+            }
+            if(y < sy) o |= rowf[y * n + lx];
+            tSA[y * n + lx] = (uint8_t)bi;
+            tSO[y * n + lx] = o;
           }
-          if(y < sy) o |= rowf[y * n + lx];
-          tSA[y * n + lx] = (uint8_t)bi;
-          tSO[y * n + lx] = o;
         }
       }
       __syncthreads();
