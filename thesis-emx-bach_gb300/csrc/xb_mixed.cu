@@ -811,15 +811,40 @@ __global__ void __launch_bounds__(256)
                const double* __restrict__ Q, int qc, const double* __restrict__ dots, int stride,
                const double* __restrict__ B, const int2* __restrict__ monoExp, int nMono, int w,
                int h, int nC1, int nRows, double* __restrict__ P) {
-  __shared__ double Xs[MXB_ROWS][MXB_T + 1];
-  __shared__ double Ys[MXB_T][MXB_MAXC];
+  // X and Y as double-float pairs (hi + lo in FP32): the products and sums
+  // run on the FP32 pipe with about 48 bits (two-product by FMA, two-sum
+  // with a running error term), far below the 2^-36 of the Gram entries
+  // they come from; the partial sums are stored in FP64.
+  __shared__ float XsH[MXB_ROWS][MXB_T + 1], XsL[MXB_ROWS][MXB_T + 1];
+  __shared__ float YsH[MXB_T][MXB_MAXC], YsL[MXB_T][MXB_MAXC];
   __shared__ int sS[MXB_T];
+  __shared__ int rowSrc[MXB_ROWS];  // source of each row: type << 24 | offset in the stamp
   if(liveN) nList = min(nList, *liveN);
   const int tid = threadIdx.x, split = blockIdx.y, t0 = split * MXB_T;
   if(t0 >= nList && split > 0) return;  // split 0 writes zeros for an empty list
   const int nt = min(MXB_T, nList - t0), row0 = blockIdx.x * MXB_ROWS, NC = nMono + 1;
   const int nQP = mxPairRow(nC1 + 2, 1);  // Q pairs
   if(tid < MXB_T) sS[tid] = tid < nt ? list[t0 + tid] : -1;
+  if(tid >= 64 && tid < 64 + MXB_ROWS) {
+    const int r = tid - 64, row = row0 + r;
+    int code = -1;
+    if(row < nRows) {
+      if(row < nQP) {
+        int qa = (int)((sqrtf(8.f * (float)(row + 1) + 1.f) - 1.f) * 0.5f) + 1;  // first guess
+        while(mxPairRow(qa + 1, 1) <= row) qa++;
+        while(qa > 1 && mxPairRow(qa, 1) > row) qa--;
+        const int qb = row - mxPairRow(qa, 1) + 1;
+        code = qa * qc + qb;
+      } else if(row == nQP) {
+        code = qc + 1;
+      } else if(row < nQP + 1 + stride) {
+        code = (1 << 24) | (row - nQP - 1);
+      } else {
+        code = (2 << 24) | (1 + row - nQP - 1 - stride);
+      }
+    }
+    rowSrc[r] = code;
+  }
   __syncthreads();
   for(int e = tid; e < MXB_T * NC; e += 256) {
     const int tt = e / NC, cI = e % NC, st = sS[tt];
@@ -833,44 +858,46 @@ __global__ void __launch_bounds__(256)
         v = ipowD(floatNormD(c.x, w), ex.x) * ipowD(floatNormD(c.y, h), ex.y);
       }
     }
-    Ys[tt][cI] = v;
+    const float hi = (float)v;
+    YsH[tt][cI] = hi;
+    YsL[tt][cI] = (float)(v - (double)hi);
   }
   for(int e = tid; e < MXB_ROWS * MXB_T; e += 256) {
-    const int r = e / MXB_T, tt = e % MXB_T, row = row0 + r, st = sS[tt];
+    const int r = e / MXB_T, tt = e % MXB_T, st = sS[tt], code = rowSrc[r];
     double v = 0.0;
-    if(st >= 0 && row < nRows) {
-      if(row < nQP) {
-        int qa = (int)((sqrt(8.0 * (double)(row + 1) + 1.0) - 1.0) * 0.5) + 1;  // first guess
-        while(mxPairRow(qa + 1, 1) <= row) qa++;
-        while(mxPairRow(qa, 1) > row) qa--;
-        const int qb = row - mxPairRow(qa, 1) + 1;
-        v = Q[(size_t)st * qc * qc + (size_t)qa * qc + qb];
-      } else if(row == nQP) {
-        v = Q[(size_t)st * qc * qc + qc + 1];
-      } else if(row < nQP + 1 + stride) {
-        v = dots[(size_t)st * stride + (row - nQP - 1)];
-      } else {
-        v = B[(size_t)st * qc + 1 + (row - nQP - 1 - stride)];
-      }
+    if(st >= 0 && code >= 0) {
+      const int type = code >> 24, off = code & 0xFFFFFF;
+      v = type == 0 ? Q[(size_t)st * qc * qc + off]
+        : type == 1 ? dots[(size_t)st * stride + off]
+                    : B[(size_t)st * qc + off];
     }
-    Xs[r][tt] = v;
+    const float hi = (float)v;
+    XsH[r][tt] = hi;
+    XsL[r][tt] = (float)(v - (double)hi);
   }
   __syncthreads();
   const int r = tid >> 2, cg0 = tid & 3;
-  double acc[MXB_MAXC / 4];
+  float aH[MXB_MAXC / 4], aL[MXB_MAXC / 4];
 #pragma unroll
-  for(int u = 0; u < MXB_MAXC / 4; u++) acc[u] = 0.0;
+  for(int u = 0; u < MXB_MAXC / 4; u++) aH[u] = aL[u] = 0.f;
   for(int tt = 0; tt < nt; tt++) {
-    const double x = Xs[r][tt];
+    const float xh = XsH[r][tt], xl = XsL[r][tt];
 #pragma unroll
     for(int u = 0; u < MXB_MAXC / 4; u++)
-      if(cg0 + 4 * u < NC) acc[u] = fma(x, Ys[tt][cg0 + 4 * u], acc[u]);
+      if(cg0 + 4 * u < NC) {
+        const float yh = YsH[tt][cg0 + 4 * u], yl = YsL[tt][cg0 + 4 * u];
+        const float ph = xh * yh;
+        const float pe = fmaf(xl, yh, fmaf(xh, yl, fmaf(xh, yh, -ph)));
+        const float sm = aH[u] + ph, bp = sm - aH[u];
+        aL[u] += ((aH[u] - (sm - bp)) + (ph - bp)) + pe;
+        aH[u] = sm;
+      }
   }
   if(row0 + r < nRows) {
     double* out = P + ((size_t)split * nRows + row0 + r) * NC;
 #pragma unroll
     for(int u = 0; u < MXB_MAXC / 4; u++)
-      if(cg0 + 4 * u < NC) out[cg0 + 4 * u] = acc[u];
+      if(cg0 + 4 * u < NC) out[cg0 + 4 * u] = (double)aH[u] + (double)aL[u];
   }
 }
 
