@@ -177,8 +177,20 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
   // per-row exponents: |x| < 2^e for the whole row
   for(int r = warp; r < GT_RB; r += GT_THREADS / 32) {
     float m = 0.f;
-    if(r < R)
-      for(int k = lane; k < K; k += 32) m = fmaxf(m, fabsf(r < wRows ? Ws[(size_t)r * ldW + k] : imgRow[k]));
+    if(r < R) {
+      // four running maxima keep four loads in flight (max is exact in any order)
+      const float* src = r < wRows ? Ws + (size_t)r * ldW : imgRow;
+      float m1 = 0.f, m2 = 0.f, m3 = 0.f;
+      int k = lane;
+      for(; k + 96 < K; k += 128) {
+        m = fmaxf(m, fabsf(src[k]));
+        m1 = fmaxf(m1, fabsf(src[k + 32]));
+        m2 = fmaxf(m2, fabsf(src[k + 64]));
+        m3 = fmaxf(m3, fabsf(src[k + 96]));
+      }
+      for(; k < K; k += 32) m = fmaxf(m, fabsf(src[k]));
+      m = fmaxf(fmaxf(m, m1), fmaxf(m2, m3));
+    }
 #pragma unroll
     for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if(lane == 0) {
