@@ -20,13 +20,21 @@ def bit_equal(a, b):
     return a.shape == b.shape and np.array_equal(_u64(a), _u64(b))
 
 
-CASES = ["test01", "config1", "config2"]
+# test01_f64 (FP64 frames) and config1_s3 (149-px stamps) take the substamp
+# search through the global-memory map kernel; the others through the
+# shared-memory one.
+CASES = ["test01", "config1", "config2", "test01_f64", "config1_s3"]
 
 
 def case_inputs(name, test01):
     from xbach.synth import make_pair
     if name == "test01":
         return test01["T"].astype(np.float32), test01["S"].astype(np.float32), {}
+    if name == "test01_f64":
+        return test01["T"].astype(np.float64), test01["S"].astype(np.float64), {}
+    if name == "config1_s3":
+        T, S, info = make_pair(1)
+        return T, S, dict(stampsx=3, stampsy=3, threshHigh=info["threshHigh"])
     cfg = int(name[-1])
     T, S, info = make_pair(cfg)
     return T, S, dict(stampsx=info["stamps"], stampsy=info["stamps"],

@@ -632,15 +632,12 @@ constexpr int FM_THREADS = 256;
 enum : uint8_t { FL_PRED = 1, FL_NONPOS = 2, FL_KFQ = 4, FL_VPOS = 8 };
 enum : uint8_t { OK_BAD = 1, OK_PRED = 2, OK_NONPOS = 4 };
 
-__device__ __forceinline__ bool keyBetter(unsigned long long k, int i, unsigned long long bk, int bi) {
-  return k > bk || (k == bk && k != 0 && i < bi);
-}
 
+// Bad map and keys of the whole stamp from the mask (the search's start).
 template <class T>
-__device__ void fmBuild(const T* img, const uint16_t* mask, int w, int cx, int cy, int n, int sx,
-                        int sy, int hSS, uint16_t badMask, const uint8_t* flags, uint8_t* bad,
-                        unsigned long long* key, unsigned short* hx, uint8_t* rowf, int* arg,
-                        uint8_t* okw) {
+__device__ void fmInit(const T* img, const uint16_t* mask, int w, int cx, int cy, int n,
+                       uint16_t badMask, const uint8_t* flags, uint8_t* bad,
+                       unsigned long long* key) {
   const int N = n * n, tid = threadIdx.x;
   for(int p = tid; p < N; p += FM_THREADS) {
     const int lx = p % n, ly = p / n;
@@ -652,46 +649,142 @@ __device__ void fmBuild(const T* img, const uint16_t* mask, int w, int cx, int c
                  ? (unsigned long long)__double_as_longlong((double)img[a]) : 0ull;
   }
   __syncthreads();
-  for(int p = tid; p < N; p += FM_THREADS) {
-    const int lx = p % n, ly = p / n, row = ly * n;
-    unsigned long long bk = 0;
-    int bi = 0xFFFF;
-    for(int x = max(lx - hSS, 0); x <= min(lx + hSS, n - 1); x++) {
-      const unsigned long long k = key[row + x];
-      if(keyBetter(k, x, bk, bi)) {
-        bk = k;
-        bi = x;
+}
+
+// Window maps over the columns [x0, x1] of the rows [k0, k1] (row maps) and
+// [r0, r1] (column maps), by the block scans of k_find_substamps_sm (van
+// Herk / Gil-Werman: prefix and suffix argmax / OR within blocks of the window
+// width; ties keep the smaller index), with 16-bit indices for stamps up to
+// 2048 pixels wide.
+__device__ void fmMaps(int n, int sx, int sy, int hSS, const uint8_t* flags, const uint8_t* bad,
+                       const unsigned long long* key, unsigned short* hx, uint8_t* rowf, int* arg,
+                       uint8_t* okw, unsigned short* tPA, unsigned short* tSA, uint8_t* tPO,
+                       uint8_t* tSO, int x0, int x1, int k0, int k1, int r0, int r1) {
+  const int tid = threadIdx.x, W = 2 * hSS + 1;
+  constexpr unsigned short NONE = 0xFFFF;
+  auto orAt = [&](int p) -> uint8_t {
+    const uint8_t fl = flags[p];
+    return (bad[p] ? OK_BAD : 0) | ((fl & FL_PRED) ? OK_PRED : 0) | ((fl & FL_NONPOS) ? OK_NONPOS : 0);
+  };
+  const int kw = x1 - x0 + 1;
+  {
+    const int ba = max(x0 - hSS, 0) / W, bb = min(x1 + hSS, n - 1) / W;
+    const int nr = k1 - k0 + 1, nTask = nr * (bb - ba + 1);
+    for(int t = tid; t < 2 * nTask; t += FM_THREADS) {
+      const bool suffix = t >= nTask;
+      const int tt = suffix ? t - nTask : t;
+      const int ly = k0 + tt % nr, blk = ba + tt / nr;
+      const size_t row = (size_t)ly * n;
+      const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
+      unsigned long long bk = 0;
+      unsigned short bi = NONE;
+      uint8_t o = 0;
+      if(!suffix) {
+        for(int x = b0; x <= b1; x++) {
+          const unsigned long long k = key[row + x];
+          if(k > bk) {
+            bk = k;
+            bi = (unsigned short)x;
+          }
+          if(x < sx) o |= orAt((int)(row + x));
+          tPA[row + x] = bi;
+          tPO[row + x] = o;
+        }
+      } else {
+        for(int x = b1; x >= b0; x--) {
+          const unsigned long long k = key[row + x];
+          if(k != 0 && k >= bk) {
+            bk = k;
+            bi = (unsigned short)x;
+          }
+          if(x < sx) o |= orAt((int)(row + x));
+          tSA[row + x] = bi;
+          tSO[row + x] = o;
+        }
       }
     }
-    hx[p] = bk ? (unsigned short)bi : (unsigned short)0xFFFF;
-    uint8_t o = 0;
-    for(int x = max(lx - hSS, 0); x <= min(lx + hSS, sx - 1); x++) {
-      const uint8_t f = flags[row + x];
-      o |= bad[row + x] ? OK_BAD : 0;
-      o |= (f & FL_PRED) ? OK_PRED : 0;
-      o |= (f & FL_NONPOS) ? OK_NONPOS : 0;
-    }
-    rowf[p] = o;
   }
   __syncthreads();
-  for(int p = tid; p < N; p += FM_THREADS) {
-    const int lx = p % n, ly = p / n;
-    unsigned long long bk = 0;
-    int bi = -1;
-    for(int y = max(ly - hSS, 0); y <= min(ly + hSS, n - 1); y++) {
-      const unsigned short xx = hx[y * n + lx];
-      if(xx == 0xFFFF) continue;
-      const int q = y * n + xx;
-      const unsigned long long k = key[q];
-      if(k > bk) {  // rows visited in ascending y: the first row keeps ties
-        bk = k;
-        bi = q;
+  for(int i = tid; i < (k1 - k0 + 1) * kw; i += FM_THREADS) {
+    const int ly = k0 + i / kw, lx = x0 + i % kw;
+    const size_t row = (size_t)ly * n;
+    const int a = max(lx - hSS, 0), b = min(lx + hSS, n - 1);
+    unsigned short h;
+    uint8_t o;
+    if(a / W != b / W) {
+      const unsigned short L = tSA[row + a], R = tPA[row + b];
+      h = L == NONE ? R : R == NONE ? L : (key[row + R] > key[row + L] ? R : L);
+      o = tSO[row + a] | tPO[row + b];
+    } else if(a % W == 0) {
+      h = tPA[row + b];
+      o = tPO[row + b];
+    } else {
+      h = tSA[row + a];
+      o = tSO[row + a];
+    }
+    hx[row + lx] = h;
+    rowf[row + lx] = o;
+  }
+  __syncthreads();
+  {
+    auto candKey = [&](int y, int lx) -> unsigned long long {
+      const unsigned short xx = hx[(size_t)y * n + lx];
+      return xx == NONE ? 0ull : key[(size_t)y * n + xx];
+    };
+    const int ba = max(r0 - hSS, 0) / W, bb = min(r1 + hSS, n - 1) / W;
+    const int nTask = kw * (bb - ba + 1);
+    for(int t = tid; t < 2 * nTask; t += FM_THREADS) {
+      const bool suffix = t >= nTask;
+      const int tt = suffix ? t - nTask : t;
+      const int lx = x0 + tt % kw, blk = ba + tt / kw;
+      const int b0 = blk * W, b1 = min(b0 + W - 1, n - 1);
+      unsigned long long bk = 0;
+      unsigned short bi = NONE;
+      uint8_t o = 0;
+      if(!suffix) {
+        for(int y = b0; y <= b1; y++) {
+          const unsigned long long k = candKey(y, lx);
+          if(k > bk) {
+            bk = k;
+            bi = (unsigned short)y;
+          }
+          if(y < sy) o |= rowf[(size_t)y * n + lx];
+          tPA[(size_t)y * n + lx] = bi;
+          tPO[(size_t)y * n + lx] = o;
+        }
+      } else {
+        for(int y = b1; y >= b0; y--) {
+          const unsigned long long k = candKey(y, lx);
+          if(k != 0 && k >= bk) {
+            bk = k;
+            bi = (unsigned short)y;
+          }
+          if(y < sy) o |= rowf[(size_t)y * n + lx];
+          tSA[(size_t)y * n + lx] = bi;
+          tSO[(size_t)y * n + lx] = o;
+        }
       }
     }
-    arg[p] = bi;
-    uint8_t o = 0;
-    for(int y = max(ly - hSS, 0); y <= min(ly + hSS, sy - 1); y++) o |= rowf[y * n + lx];
-    okw[p] = o;
+    __syncthreads();
+    for(int i = tid; i < (r1 - r0 + 1) * kw; i += FM_THREADS) {
+      const int ly = r0 + i / kw, lx = x0 + i % kw;
+      const int a = max(ly - hSS, 0), b = min(ly + hSS, n - 1);
+      unsigned short yb;
+      uint8_t o;
+      if(a / W != b / W) {
+        const unsigned short L = tSA[(size_t)a * n + lx], R = tPA[(size_t)b * n + lx];
+        yb = L == NONE ? R : R == NONE ? L : (candKey(R, lx) > candKey(L, lx) ? R : L);
+        o = tSO[(size_t)a * n + lx] | tPO[(size_t)b * n + lx];
+      } else if(a % W == 0) {
+        yb = tPA[(size_t)b * n + lx];
+        o = tPO[(size_t)b * n + lx];
+      } else {
+        yb = tSA[(size_t)a * n + lx];
+        o = tSO[(size_t)a * n + lx];
+      }
+      arg[(size_t)ly * n + lx] = yb == NONE ? -1 : yb * n + hx[(size_t)yb * n + lx];
+      okw[(size_t)ly * n + lx] = o;
+    }
   }
   __syncthreads();
 }
@@ -726,6 +819,10 @@ __global__ void __launch_bounds__(FM_THREADS)
   uint8_t* bad = flags + N;                             // N
   uint8_t* rowf = bad + N;                              // N
   uint8_t* okw = rowf + N;                              // N
+  unsigned short* tPA = (unsigned short*)(okw + N);     // N (block scans of fmMaps)
+  unsigned short* tSA = tPA + N;                        // N
+  uint8_t* tPO = (uint8_t*)(tSA + N);                   // N
+  uint8_t* tSO = tPO + N;                               // N
   __shared__ int2 locXY[MAX_MAXSS];
   __shared__ double locVal[MAX_MAXSS];
   __shared__ int sBest;
@@ -744,7 +841,9 @@ __global__ void __launch_bounds__(FM_THREADS)
     flags[p] = f;
   }
   __syncthreads();
-  fmBuild(img, mask, w, cx, cy, n, sx, sy, hSS, badMask, flags, bad, key, hx, rowf, arg, okw);
+  fmInit(img, mask, w, cx, cy, n, badMask, flags, bad, key);
+  fmMaps(n, sx, sy, hSS, flags, bad, key, hx, rowf, arg, okw, tPA, tSA, tPO, tSO, 0, n - 1, 0,
+         n - 1, 0, n - 1);
   const double floorV = sky + tKF * fwhm;
   double dfrac = 0.9;
   int cnt = 0, passes = 0;
@@ -834,11 +933,23 @@ __global__ void __launch_bounds__(FM_THREADS)
         locVal[cnt] = ret;
       }
       cnt++;
-      for(int i = tid; i < un; i += FM_THREADS)
-        orMask(mask, (size_t)(u0 + i % uw) + (size_t)(v0 + i / uw) * w, skipMask);
+      // the window turns bad (its skip bit is part of this image's bad mask,
+      // and no other CTA touches this image's bits of the stamp): keys inside
+      // it vanish, and only maps within hSS of it can change
+      for(int i = tid; i < un; i += FM_THREADS) {
+        const int gx = u0 + i % uw, gy = v0 + i / uw;
+        orMask(mask, (size_t)gx + (size_t)gy * w, skipMask);
+        const size_t q = (size_t)(gx - cx) + (size_t)(gy - cy) * n;
+        bad[q] = 1;
+        key[q] = 0ull;
+      }
       __syncthreads();
-      if(cnt < maxSS)
-        fmBuild(img, mask, w, cx, cy, n, sx, sy, hSS, badMask, flags, bad, key, hx, rowf, arg, okw);
+      if(cnt < maxSS) {
+        const int a0 = u0 - cx, a1 = u1 - cx, b0 = v0 - cy, b1 = v1 - cy;
+        fmMaps(n, sx, sy, hSS, flags, bad, key, hx, rowf, arg, okw, tPA, tSA, tPO, tSO,
+               max(a0 - hSS, 0), min(a1 + hSS, n - 1), b0, b1, max(b0 - hSS, 0),
+               min(b1 + hSS, n - 1));
+      }
     }
     if(cnt >= maxSS || lim == floorV) break;
     dfrac -= 0.2;
@@ -1362,7 +1473,7 @@ static void sssPass(xb_ctx* c, int* nKept) {
   }
   dim3 grid(nAll, 2);
   { KT_SCOPE(c, "find_substamps");
-  const size_t perCta = ((size_t)fSW * fSW * 18 + 255) / 256 * 256;
+  const size_t perCta = ((size_t)fSW * fSW * 24 + 255) / 256 * 256;
   unsigned char* scratch = buf<unsigned char>(c, "fm_scratch", (size_t)2 * nAll * perCta);
   const size_t fsSmem = fsSmemBytes(fSW);
   if(!c->imgIsF64 && fSW <= 120) {
