@@ -267,6 +267,12 @@ def run_config4(args):
     batch = xbach.Batch(params[0], workers=args.workers)
     batch.set_params(params)
     use_graph = bool(args.graph) and args.mode == "mixed"
+    use_rank = bool(args.rank) and args.mode == "mixed"
+    if use_rank:
+        from xbach import ranker
+        w_rank = ranker.preset5_weights()
+        for i in range(batch.n_workers):
+            ranker.enable(batch.worker(i), w_rank, policy=1, tau=0.5)
     if use_graph:
         batch.set_option("graph", 1)
     st = torch.cuda.Stream()
@@ -304,6 +310,8 @@ def run_config4(args):
     same = []
     for i in check:
         ctx = xbach.Context(params[i])
+        if use_rank:
+            ranker.enable(ctx, w_rank, policy=1, tau=0.5)
         ctx.init_device(dT[i].data_ptr(), dS[i].data_ptr(), ws[i], hs[i])
         for stage in (ctx.sss, ctx.cmv, ctx.cd, ctx.ksc, ctx.conv, ctx.sub):
             stage()
@@ -326,6 +334,8 @@ def run_config4(args):
                    "mode": args.mode, "frames_per_step": n_pairs, "workers": args.workers,
                    "frame_graphs": use_graph, "schedule": "fixed, largest first" if use_graph
                    else "shared queue",
+                   "learned_ranking": "policy 1, tau 0.5, xbach/ranker_preset5.npy" if use_rank
+                   else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "l2": "flushed before every step; inputs exceed L2",
                    "inputs": "device-resident FP32 T,S"},

@@ -121,6 +121,17 @@ Basis buildBasis(const xb_params& p, const Geo& g) {
   return b;
 }
 
+cudaError_t allowMaxDynamicSmem(const void* func, int device) {
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if(e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, func);
+  if(e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes);
+}
+
 void* poolGet(xb_ctx* c, const char* name, size_t bytes) {
   DevBuf& b = c->pool[name];
   if(b.bytes >= bytes) return b.p;

@@ -950,7 +950,7 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, const int* list,
   const int CL = luSmem(8) <= (size_t)maxSmem ? 8 : 16;
   const size_t smem = luSmem(CL);
   auto luKernel = CL == 8 ? k_global_lu<8> : k_global_lu<16>;
-  XB_CUDA(cudaFuncSetAttribute(luKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  XB_CUDA(allowMaxDynamicSmem((const void*)luKernel, c->device));
   if(CL > 8) XB_CUDA(cudaFuncSetAttribute(luKernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);

@@ -380,14 +380,12 @@ bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, 
   StampSetDev& S = c->set[si];
   int* err = deviceStatus(c) + 1;  // the context's device-timeout word
   if(c->imgIsF64) {
-    XB_CUDA(cudaFuncSetAttribute(k_gram_tc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)GT_SMEM));
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_gram_tc<double>, c->device));
     k_gram_tc<double><<<nList, GT_THREADS, GT_SMEM, c->stream>>>(
         (const double*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
         g.hSS, g.wRows, mixedLd(g), S.Wf, G, err);
   } else {
-    XB_CUDA(cudaFuncSetAttribute(k_gram_tc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)GT_SMEM));
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_gram_tc<float>, c->device));
     k_gram_tc<float><<<nList, GT_THREADS, GT_SMEM, c->stream>>>(
         (const float*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
         g.hSS, g.wRows, mixedLd(g), S.Wf, G, err);

@@ -217,6 +217,13 @@ struct XbError {
 // Named, grow-only device buffers: a repeated run on the same context
 // reuses its allocations, so steady-state runs allocate nothing.
 void* poolGet(xb_ctx* c, const char* name, size_t bytes);
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum.  The limit belongs to the function, process-wide, and concurrent
+// contexts (batch workers) launch the same kernels with different sizes, so
+// a per-launch setting could undercut another context's launch or captured
+// graph; occupancy follows each launch's own request, not this limit.
+cudaError_t allowMaxDynamicSmem(const void* func, int device);
 template <class T>
 T* buf(xb_ctx* c, const char* name, size_t n) {
   return static_cast<T*>(poolGet(c, name, (n ? n : 1) * sizeof(T)));

@@ -719,7 +719,7 @@ template <class Kern, class... Args>
 cudaError_t launchCluster(xb_ctx* c, Kern kernel, int CL, int threads, size_t smem,
                           Args... args) {
   cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      allowMaxDynamicSmem((const void*)kernel, c->device);
   if(e != cudaSuccess) return e;
   if(CL > 8) {
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

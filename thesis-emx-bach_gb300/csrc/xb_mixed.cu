@@ -1066,7 +1066,7 @@ void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, 
   auto launchLu = [&](auto kernel, int CL) -> cudaError_t {
     const int ncol = (n + CL - 1) / CL;
     const size_t smem = ((size_t)ncol * ld + ld + 2 * (ld + 1) + ld) * sizeof(double);
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allowMaxDynamicSmem((const void*)kernel, c->device);
     if(e != cudaSuccess) return e;
     if(CL > 8) {
       e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

@@ -1474,11 +1474,13 @@ static void sssPass(xb_ctx* c, int* nKept) {
   dim3 grid(nAll, 2);
   { KT_SCOPE(c, "find_substamps");
   const size_t perCta = ((size_t)fSW * fSW * 24 + 255) / 256 * 256;
-  unsigned char* scratch = buf<unsigned char>(c, "fm_scratch", (size_t)2 * nAll * perCta);
   const size_t fsSmem = fsSmemBytes(fSW);
-  if(!c->imgIsF64 && fSW <= 120) {
-    XB_CUDA(cudaFuncSetAttribute(k_find_substamps_sm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fsSmem));
+  const bool inShared = !c->imgIsF64 && fSW <= 120;
+  // global-memory maps only for the kernel that uses them
+  unsigned char* scratch =
+      inShared ? nullptr : buf<unsigned char>(c, "fm_scratch", (size_t)2 * nAll * perCta);
+  if(inShared) {
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_find_substamps_sm, c->device));
     k_find_substamps_sm<<<grid, FS_T, fsSmem, c->stream>>>(
         (const float*)c->img[0], (const float*)c->img[1], c->mask, c->geomAll, c->skyAll[0],
         c->fwhmAll[0], c->skyAll[1], c->fwhmAll[1], c->ssxyAll[0], c->ssvalAll[0], c->cntAll[0],
