@@ -174,20 +174,43 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------- roofline --
+# DRAM bytes (read + write) of one k_conv_sub_f32 launch on the 2048^2
+# workload, from `ncu --set full` (profiles/mixed_kernels_2048_ncu.md):
+# 33.877 MB read + 1.665 MB written, cold cache.
+CONV_DRAM_BYTES_2048 = 33.876992e6 + 1.664512e6
+
+
 def roofline_for(name, ms_per_launch, n_pix, mode, hbm_peak):
-    """Algorithmic bytes of one launch of the dominant kernel (per-pixel byte
-    counts are derived in the design doc) and the achieved bandwidth."""
+    """Algorithmic bytes of one launch of the frame-wide kernel and the
+    achieved bandwidth.  The conv reads I and O (FP32) and the mask (2 B) and
+    writes the mask, conv and diff (FP32; plain mode also FP64 copies)."""
     if name == "conv_sub":
-        # reads I, O (FP32), writes mask (2 B), conv and diff (FP32; plain
-        # mode also the FP64 copies)
         per_px = 4 + 4 + 2 + 4 + 4 + (16 if mode == "plain" else 0)
         traffic_bytes = per_px * n_pix
     else:
         return None
     achieved = traffic_bytes / (ms_per_launch * 1e-3) / 1e9
+    traffic = CONV_DRAM_BYTES_2048 if (mode == "mixed" and n_pix == 2048 * 2048) else None
     return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None, "kernel": name,
+            "frac": achieved / hbm_peak, "traffic": traffic, "kernel": name,
             "algorithmic_bytes_per_launch": traffic_bytes, "ms_per_launch": ms_per_launch}
+
+
+def gram_tensor_roofline(kernels, ctx, bf16_peak_tflops, wcols=961, rows=64, kc=64):
+    """BF16 tensor work of the exact-slice Gram (k_gram_tc) over one frame:
+    per stamp and 64-column chunk of W, four K-steps of three MMAs (M128 x
+    N256, N64, N128, K16), i.e. 2*128*(256+64+128)*16*4 FLOP per chunk, for
+    every stamp filled (both sets in cmv, then the ksc refills)."""
+    if "gram" not in kernels:
+        return None
+    chunks = -(-wcols // kc)
+    flop_stamp = chunks * 4 * 2 * 128 * (256 + 64 + 128) * 16
+    stamps = ctx.scalar("nstamps0") + ctx.scalar("nstamps1") + ctx.scalar("ksc_refills")
+    ms = kernels["gram"]["ms_total"]
+    achieved = flop_stamp * stamps / (ms * 1e-3) / 1e12
+    return {"bound": "tensor", "kernel": "gram_tc", "achieved": achieved,
+            "peak": bf16_peak_tflops, "unit": "TFLOP/s", "frac": achieved / bf16_peak_tflops,
+            "flop_per_stamp": flop_stamp, "stamps_per_frame": stamps, "ms_per_frame": ms}
 
 
 def run_result(xbach, cx):
@@ -564,6 +587,8 @@ def main():
         roof = roofline_for("conv_sub", cs["ms_total"] / cs["launches"], n_pix, args.mode, hbm_peak)
     if roof is not None:
         roof["peak_source"] = peak_src
+    bf16_peak = measured_peaks()[1]
+    roof_tc = gram_tensor_roofline(kernels, ctx, bf16_peak) if args.mode == "mixed" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -580,6 +605,7 @@ def main():
                    else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+        "roofline_tensor": roof_tc,
         "single_frame": {"value": single_value, "unit": UNIT,
                          "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single,
                          "path": "stages, host-driven (per-kernel timers on)"},

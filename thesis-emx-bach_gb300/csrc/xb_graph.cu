@@ -550,6 +550,8 @@ void runFrame(xb_ctx* c, const float* T, const float* S, int w, int h, float* co
   c->scalars["sss_retry"] = c->sssRetry = r.sssRetry;
   c->set[0].n = r.nKept[0];
   c->set[1].n = r.nKept[1];
+  c->scalars["nstamps0"] = r.nKept[0];
+  c->scalars["nstamps1"] = r.nKept[1];
   c->launches += fg.lTop + (r.sssRetry ? fg.lRetry : 0);
   if(r.nKept[0] == 0 && r.nKept[1] == 0) {
     c->stage = 2;

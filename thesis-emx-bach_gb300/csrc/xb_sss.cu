@@ -1610,6 +1610,8 @@ void stageSss(xb_ctx* c) {
   }
   c->set[0].n = nKept[0];
   c->set[1].n = nKept[1];
+  c->scalars["nstamps0"] = nKept[0];
+  c->scalars["nstamps1"] = nKept[1];
   if(nKept[0] == 0 && nKept[1] == 0) throw XbError{XB_ERR_NO_SUBSTAMPS, "No substamps found"};
   if(c->rank && c->rankW) rankSubstamps(c);  // learned order of each stamp's substamps
   if(c->trace) {
