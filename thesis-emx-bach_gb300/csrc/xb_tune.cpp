@@ -10,7 +10,9 @@
 // other threads that reach the same key meanwhile use the default variant.
 // With XB_TUNE_CACHE set, the table is read from and appended to that file
 // ("key variant" lines), so later processes skip the timing.  Option
-// "autotune" (default on) turns the timing off: variant 0 is used.
+// "autotune" (default on) turns the timing off: variant 0 is used; so does
+// XB_AUTOTUNE=0 in the environment (for runs under a profiler, whose
+// serialisation would make the timings meaningless).
 
 #include <cstdlib>
 #include <fstream>
@@ -52,7 +54,11 @@ void appendCache(const std::string& key, int v) {
 int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
                  const std::function<void(int)>& launch) {
   if(c->tuneForce >= 0) return c->tuneForce < nVariants ? c->tuneForce : nVariants - 1;
-  if(!c->autotune || nVariants <= 1) return 0;
+  static const bool envOff = [] {
+    const char* e = std::getenv("XB_AUTOTUNE");
+    return e && e[0] == '0';
+  }();
+  if(!c->autotune || envOff || nVariants <= 1) return 0;
   const std::string key = std::string(kernel) + "@dev" + std::to_string(c->device) + ":" +
                           std::to_string(shape);
   if(c->capturing) {  // a graph being captured cannot time: the table's choice or variant 0
