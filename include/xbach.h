@@ -197,6 +197,17 @@ int xb_run_device(xb_ctx* ctx, const float* dT, const float* dS, int w, int h,
 int xb_get_image(xb_ctx* ctx, int which, float* out);
 int xb_get_image_f64(xb_ctx* ctx, int which, double* out);
 int xb_get_mask(xb_ctx* ctx, uint16_t* out);
+/* Input mask for the following frames (no counterpart in the reference,
+ * which defines the INPUT_MASK bit, include/datatypeUtil.h:179, but never
+ * sets it): pixels whose byte is nonzero get XB_MASK_INPUT_MASK and
+ * XB_MASK_BAD_INPUT when a frame is initialised, before the bad-input mask is
+ * dilated, so they are treated like the frame's own bad pixels in the
+ * substamp search; the convolution treats them as bad input too, as HOTPANTS
+ * does with its input masks: they get XB_MASK_BAD_OUTPUT (difference 1e-30)
+ * and the pixels whose kernel covers them XB_MASK_BAD_CONV or XB_MASK_OK_CONV.
+ * mask is w x h (row-major); a frame of another size fails with
+ * XB_ERR_SIZE_MISMATCH.  NULL clears it. */
+int xb_set_input_mask(xb_ctx* ctx, const uint8_t* mask, int w, int h);
 /* Device pointers of the FP32 conv / diff images (valid until the next init
  * or destroy); for callers that keep results on the GPU. */
 int xb_get_device_images(xb_ctx* ctx, const float** dConv, const float** dDiff);

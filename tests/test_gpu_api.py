@@ -85,3 +85,102 @@ def test_device_resident_input(test01):
     ctx.init_device(dT.data_ptr(), dS.data_ptr(), T.shape[1], T.shape[0])
     ctx.sss(); ctx.cmv(); ctx.cd(); ctx.ksc(); ctx.conv(); ctx.sub()
     assert np.array_equal(ctx.image(xbach.XB_IMG_DIFF), ref.image(xbach.XB_IMG_DIFF))
+
+
+def test_cli_input_mask_mask_and_noise_outputs(tmp_path):
+    """-im excludes the pixels of an input-mask FITS, -om writes the output
+    mask and -on writes sqrt(|target| + |conv| + 2 rn^2), the target being the
+    frame that is not convolved."""
+    import shutil
+    import build_native
+    import xbach
+    BAD_CONV, INPUT_MASK, OK_CONV = 1 << 4, 1 << 5, 1 << 6  # XB_MASK_* of include/xbach.h
+    BAD_INPUT, BAD_OUTPUT = 1 << 7, 1 << 12
+    L = xbach.lib()
+    for f in ("test0.fits", "test1.fits"):
+        shutil.copy(GOLDEN / f, tmp_path / f)
+    T = read_fits(GOLDEN / "test1.fits")
+    S = read_fits(GOLDEN / "test0.fits")
+    h, w = T.shape
+    m = np.zeros((h, w))
+    m[100:110, 150:170] = 1.0  # a block of pixels to exclude
+    assert L.xb_fits_write(str(tmp_path / "inmask.fits").encode(), m.ctypes.data, w, h) == 0
+    out = tmp_path / "o_"
+    r = subprocess.run([str(build_native.CLI_BIN), "-ip", str(tmp_path), "-s", "test0.fits",
+                        "-t", "test1.fits", "-op", str(out), "-im", "inmask.fits",
+                        "-om", "mask.fits", "-on", "noise.fits", "-rn", "5", "-v"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    # the convolution treats the excluded pixels as bad input (HOTPANTS'
+    # input masks): they are BAD_OUTPUT and every pixel whose kernel covers
+    # one is BAD_CONV or OK_CONV
+    mask = read_fits(f"{out}mask.fits").astype(np.int64)
+    blk = mask[100:110, 150:170]
+    assert np.all((blk & (INPUT_MASK | BAD_INPUT | BAD_OUTPUT)) == INPUT_MASK | BAD_INPUT | BAD_OUTPUT)
+    assert np.all(blk & (BAD_CONV | OK_CONV))
+    assert not np.any(mask[m == 0] & INPUT_MASK)
+    assert np.all(read_fits(f"{out}sub.fits")[100:110, 150:170] == np.float32(1e-30))
+    r0 = subprocess.run([str(build_native.CLI_BIN), "-ip", str(tmp_path), "-s", "test0.fits",
+                         "-t", "test1.fits", "-op", str(tmp_path / "n_"), "-om", "mask.fits"],
+                        capture_output=True, text=True, timeout=300)
+    assert r0.returncode == 0, r0.stdout + r0.stderr
+    mask0 = read_fits(f"{tmp_path / 'n_'}mask.fits").astype(np.int64)
+    assert not np.all(mask0[100:110, 150:170] & (BAD_CONV | OK_CONV))
+    conv = read_fits(f"{out}diff.fits")
+    noise = read_fits(f"{out}noise.fits")
+    target = S if "test1.fits chosen to be convolved" in r.stdout else T
+    want = np.sqrt(np.abs(target) + np.abs(conv) + 2 * 5.0 ** 2)
+    assert np.allclose(noise, want, rtol=2e-6, atol=0)
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_input_mask_excludes_pixels(test01, mode):
+    """xb_set_input_mask: the pixels get INPUT_MASK | BAD_INPUT at init (before
+    the bad-input dilation), no substamp is centred on them, the convolution
+    leaves them BAD_OUTPUT, a mask of the wrong size is refused and clearing
+    it restores the unmasked run."""
+    import xbach
+    INPUT_MASK, BAD_INPUT, BAD_OUTPUT = 1 << 5, 1 << 7, 1 << 12  # XB_MASK_* of include/xbach.h
+    T, S = test01["T"], test01["S"]
+    md = xbach.XB_MODE_PLAIN
+    if mode == "mixed":
+        T, S, md = T.astype(np.float32), S.astype(np.float32), xbach.XB_MODE_MIXED
+    h, w = T.shape
+    m = np.zeros((h, w), np.uint8)
+    m[100:110, 150:170] = 1
+    m[200, :] = 1  # a bad row
+    ctx = xbach.Context(xbach.default_params(mode=md), trace=True)
+    ctx.set_input_mask(m)
+    ctx.init(T, S)
+    got = ctx.mask().astype(np.int64)
+    assert np.all((got[m != 0] & (INPUT_MASK | BAD_INPUT)) == INPUT_MASK | BAD_INPUT)
+    assert not np.any(got[m == 0] & INPUT_MASK)
+    ctx.sss()
+    for si in (0, 1):
+        cnt = ctx.array("ss_count_all%d" % si, np.int32)
+        xy = ctx.array("ss_xy_all%d" % si, np.int32).reshape(len(cnt), -1, 2)
+        for s in range(len(cnt)):
+            for x, y in xy[s, :cnt[s]]:
+                assert m[y, x] == 0, (si, s, x, y)
+    ctx.cmv(), ctx.cd(), ctx.ksc(), ctx.conv(), ctx.sub()
+    masked = ctx.image(xbach.XB_IMG_DIFF)
+    got = ctx.mask().astype(np.int64)
+    assert np.all((got[m != 0] & (INPUT_MASK | BAD_OUTPUT)) == INPUT_MASK | BAD_OUTPUT)
+    assert np.all(masked[m != 0] == (np.float32(1e-30) if mode == "mixed" else 1e-30))
+    with pytest.raises(xbach.XbError):
+        ctx.set_input_mask(np.zeros((h, w + 1)))
+        ctx.init(T, S)
+    ctx.set_input_mask(None)
+    ctx.run_all(T, S)
+    ref = xbach.Context(xbach.default_params(mode=md))
+    ref.run_all(T, S)
+    assert np.array_equal(ctx.image(xbach.XB_IMG_DIFF), ref.image(xbach.XB_IMG_DIFF))
+    assert not np.array_equal(masked, ref.image(xbach.XB_IMG_DIFF))
+    if mode == "mixed":  # a frame graph with the mask replays the stage-by-stage run
+        g = xbach.Context(xbach.default_params(mode=md))
+        g.set_option("graph", 1)
+        g.set_input_mask(m)
+        for _ in range(2):
+            g.run(T, S)
+            assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False),
+                                  masked.astype(np.float32))

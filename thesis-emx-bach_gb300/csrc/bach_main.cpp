@@ -11,9 +11,18 @@
 //   -kw n  -ssw n       half kernel width / half substamp width
 //   -th x  -tl x        threshHigh / threshLow
 //   -gauss s:d,s:d,...  Gaussian sigmas and polynomial degrees
+//   -im file            input mask (FITS, <ip>/file; nonzero pixels are
+//                       excluded: INPUT_MASK | BAD_INPUT before the dilation)
+//   -om name            also write the final mask (<op>name, the 13 flag bits
+//                       as FITS values)
+//   -on name            also write the noise image of the difference
+//                       (<op>name: sqrt(|target| + |conv| + 2 rn^2), gain 1,
+//                       the noise model of the reference's chi^2, cd.cl:578)
+//   -rn x               read noise for -on (ADU, default 0)
 // Output: <op><o> (the convolved image, default diff.fits) and <op>sub.fits.
 
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -47,6 +56,8 @@ bool exists(int argc, const char** argv, const std::string& o) {
 struct Cli {
   std::string templateName, scienceName, outName = "diff.fits", inputPath = "res/",
                                          outPath = "out/";
+  std::string maskIn, maskOut, noiseOut;
+  double readNoise = 0.0;
   bool verbose = false, verboseTime = false;
   int device = 0;
   xb_params p{};
@@ -93,6 +104,10 @@ void parse(int argc, const char** argv, Cli& c) {
     }
     c.p.nGauss = n;
   }
+  if(exists(argc, argv, "-im")) c.maskIn = option(argc, argv, "-im");
+  if(exists(argc, argv, "-om")) c.maskOut = option(argc, argv, "-om");
+  if(exists(argc, argv, "-on")) c.noiseOut = option(argc, argv, "-on");
+  if(exists(argc, argv, "-rn")) c.readNoise = std::atof(option(argc, argv, "-rn"));
   c.p.verbose = c.verbose;
   const char* t = option(argc, argv, "-t");
   if(!t) throw std::invalid_argument("Template file Input is required!");
@@ -144,7 +159,34 @@ int main(int argc, const char* argv[]) {
     std::cout << "context creation failed (" << rc << ")" << std::endl;
     return 1;
   }
+  if(!cli.maskIn.empty()) {
+    double* M = nullptr;
+    int mw = 0, mh = 0;
+    const std::string mPath = cli.inputPath + "/" + cli.maskIn;
+    if(xb_fits_read(mPath.c_str(), &M, &mw, &mh) != XB_OK) {
+      std::cout << "Unable to open file '" << mPath << "'" << std::endl;
+      xb_free(T);
+      xb_free(S);
+      xb_ctx_destroy(ctx);
+      return 1;
+    }
+    std::vector<uint8_t> m((size_t)mw * mh);
+    for(size_t i = 0; i < m.size(); i++) m[i] = M[i] != 0.0 ? 1 : 0;
+    xb_free(M);
+    rc = xb_set_input_mask(ctx, m.data(), mw, mh);
+    if(rc != XB_OK) {
+      xb_free(T);
+      xb_free(S);
+      return fail(ctx, rc);
+    }
+  }
   rc = xb_init(ctx, T, tw, th, S, sw, sh);
+  // the noise image needs the target frame after the fit
+  std::vector<double> tCopy, sCopy;
+  if(rc == XB_OK && !cli.noiseOut.empty()) {
+    tCopy.assign(T, T + (size_t)tw * th);
+    sCopy.assign(S, S + (size_t)sw * sh);
+  }
   xb_free(T);
   xb_free(S);
   if(rc != XB_OK) return fail(ctx, rc);
@@ -222,6 +264,30 @@ int main(int argc, const char* argv[]) {
     std::cout << "Unable to save file '" << subPath << "'" << std::endl;
     xb_ctx_destroy(ctx);
     return 1;
+  }
+  if(!cli.maskOut.empty()) {
+    std::vector<uint16_t> m((size_t)tw * th);
+    if((rc = xb_get_mask(ctx, m.data())) != XB_OK) return fail(ctx, rc);
+    for(size_t i = 0; i < m.size(); i++) img[i] = m[i];
+    const std::string path = cli.outPath + cli.maskOut;
+    if(xb_fits_write(path.c_str(), img.data(), tw, th) != XB_OK) {
+      std::cout << "Unable to save file '" << path << "'" << std::endl;
+      xb_ctx_destroy(ctx);
+      return 1;
+    }
+  }
+  if(!cli.noiseOut.empty()) {
+    if((rc = xb_get_image_f64(ctx, XB_IMG_CONV, img.data())) != XB_OK) return fail(ctx, rc);
+    const std::vector<double>& target = convTemplate ? sCopy : tCopy;
+    for(size_t i = 0; i < img.size(); i++)
+      img[i] = std::sqrt(std::fabs(target[i]) + std::fabs(img[i]) +
+                         2.0 * cli.readNoise * cli.readNoise);
+    const std::string path = cli.outPath + cli.noiseOut;
+    if(xb_fits_write(path.c_str(), img.data(), tw, th) != XB_OK) {
+      std::cout << "Unable to save file '" << path << "'" << std::endl;
+      xb_ctx_destroy(ctx);
+      return 1;
+    }
   }
   auto p16 = Clock::now();
   if(cli.verboseTime) std::cout << "Fin took " << msBetween(p15, p16) << " ms" << std::endl;

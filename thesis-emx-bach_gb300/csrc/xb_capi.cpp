@@ -187,6 +187,23 @@ int xb_ctx_destroy(xb_ctx* c) {
 
 const char* xb_last_error(const xb_ctx* c) { return c ? c->lastError.c_str() : "null context"; }
 
+int xb_set_input_mask(xb_ctx* c, const uint8_t* mask, int w, int h) {
+  return guarded(c, [&] {
+    if(!mask) {
+      c->inputMask = nullptr;  // the buffer stays in the pool
+      c->inputMaskW = c->inputMaskH = 0;
+      return;
+    }
+    if(w <= 0 || h <= 0) throw XbError{XB_ERR_ARG, "bad mask size"};
+    const size_t n = (size_t)w * h;
+    c->inputMask = buf<uint8_t>(c, "input_mask", n);
+    XB_CUDA(cudaMemcpyAsync(c->inputMask, mask, n, cudaMemcpyHostToDevice, c->stream));
+    XB_CUDA(cudaStreamSynchronize(c->stream));
+    c->inputMaskW = w;
+    c->inputMaskH = h;
+  });
+}
+
 int xb_ctx_set_params(xb_ctx* c, const xb_params* p) {
   return guarded(c, [&] {
     if(!p) throw XbError{XB_ERR_ARG, "null parameters"};

@@ -50,7 +50,8 @@ template <class T>
 __global__ void __launch_bounds__(CONV_THREADS)
     k_conv_sub_f64(const T* __restrict__ I, const T* __restrict__ O,
                    const double* __restrict__ sol, const double* __restrict__ vec,
-                   const double* __restrict__ kernSumPtr, ConvArgs a, uint16_t* __restrict__ mask,
+                   const double* __restrict__ kernSumPtr, ConvArgs a,
+                   const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
                    double* __restrict__ convD, float* __restrict__ convF,
                    double* __restrict__ diffD, float* __restrict__ diffF) {
   extern __shared__ double cv_s[];
@@ -92,7 +93,8 @@ __global__ void __launch_bounds__(CONV_THREADS)
     int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
     double v = (double)I[(size_t)gx + (size_t)gy * a.w];
     tile[i] = v;
-    bad[i] = (convMaskOf(v, a.tH, a.tL) & BAD_INPUT) ? 1 : 0;
+    bad[i] = ((convMaskOf(v, a.tH, a.tL) & BAD_INPUT) ||
+              (inMask && inMask[(size_t)gx + (size_t)gy * a.w])) ? 1 : 0;
   }
   __syncthreads();
   for(int p = tid; p < nk; p += CONV_THREADS) {
@@ -148,7 +150,8 @@ __global__ void __launch_bounds__(CONV_THREADS)
     acc *= invKernMult;
     const size_t id = (size_t)x + (size_t)y * a.w;
     const double tc = tile[(ly + hK) * tw + lx + hK];
-    const uint16_t cm = convMaskOf(tc, a.tH, a.tL);
+    uint16_t cm = convMaskOf(tc, a.tH, a.tL);
+    if(inMask && inMask[id]) cm |= INPUT_MASK | BAD_INPUT;
     uint16_t nm = cm;
     if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
     if(anyBad) {
@@ -174,7 +177,8 @@ __global__ void __launch_bounds__(CONV_THREADS)
 // keeps its value plus maskAfterConv's bits.
 template <class T>
 __global__ void k_border(const T* __restrict__ O, int w, int h, int hK, double tH, double tL,
-                         uint16_t* __restrict__ mask, double* __restrict__ convD,
+                         const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
+                         double* __restrict__ convD,
                          float* __restrict__ convF, double* __restrict__ diffD,
                          float* __restrict__ diffF) {
   const long long n = (long long)w * h;
@@ -183,6 +187,7 @@ __global__ void k_border(const T* __restrict__ O, int w, int h, int hK, double t
     const int x = (int)(id % w), y = (int)(id / w);
     if(x >= hK && x < w - hK && y >= hK && y < h - hK) continue;
     mask[id] |= afterMaskOf((double)O[id], tH, tL);
+    if(inMask && inMask[id]) mask[id] |= INPUT_MASK | BAD_INPUT | BAD_OUTPUT;
     convD[id] = 1e-30;
     convF[id] = (float)1e-30;
     diffD[id] = 1e-30;
@@ -243,22 +248,22 @@ void stageConvSub(xb_ctx* c, bool doSub) {
   if(c->imgIsF64) {
     { KT_SCOPE(c, "conv_sub");
     k_conv_sub_f64<double><<<grid, CONV_THREADS, smem, c->stream>>>(
-        (const double*)c->img[I], (const double*)c->img[O], c->dSol, c->dVec, ks, a, c->mask,
-        c->convD, c->convF, c->diffD, c->diffF);
+        (const double*)c->img[I], (const double*)c->img[O], c->dSol, c->dVec, ks, a, c->inputMask,
+        c->mask, c->convD, c->convF, c->diffD, c->diffF);
     XB_LAUNCHED(c);
     }
     k_border<double><<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
-        (const double*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convD, c->convF,
+        (const double*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convD, c->convF,
         c->diffD, c->diffF);
   } else {
     { KT_SCOPE(c, "conv_sub");
     k_conv_sub_f64<float><<<grid, CONV_THREADS, smem, c->stream>>>(
-        (const float*)c->img[I], (const float*)c->img[O], c->dSol, c->dVec, ks, a, c->mask,
-        c->convD, c->convF, c->diffD, c->diffF);
+        (const float*)c->img[I], (const float*)c->img[O], c->dSol, c->dVec, ks, a, c->inputMask,
+        c->mask, c->convD, c->convF, c->diffD, c->diffF);
     XB_LAUNCHED(c);
     }
     k_border<float><<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
-        (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convD, c->convF,
+        (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convD, c->convF,
         c->diffD, c->diffF);
   }
   XB_LAUNCHED(c);

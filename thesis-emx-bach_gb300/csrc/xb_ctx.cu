@@ -250,8 +250,17 @@ __global__ void __launch_bounds__(SP_TX * 4) k_spread_mask(uint16_t* __restrict_
   }
 }
 
+__global__ void k_apply_input_mask(const uint8_t* __restrict__ in, uint16_t* __restrict__ mask,
+                                   long long n) {
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    if(in[i]) mask[i] |= INPUT_MASK | BAD_INPUT;
+}
+
 void stageInitMask(xb_ctx* c) {
   const int border = c->p.hSStampWidth + c->p.hKernelWidth;
+  if(c->inputMask && (c->inputMaskW != c->w || c->inputMaskH != c->h))
+    throw XbError{XB_ERR_SIZE_MISMATCH, "input mask and frame differ in size"};
   const long long n = (long long)c->w * c->h;
   int blocks = (int)std::min<long long>((n + 1023) / 1024, (long long)c->smCount * 16);
   { KT_SCOPE(c, "mask_input");
@@ -264,6 +273,10 @@ void stageInitMask(xb_ctx* c) {
         (const float*)c->img[0], (const float*)c->img[1], c->mask, c->w, c->h,
         border, c->p.threshHigh, c->p.threshLow);
   XB_LAUNCHED(c);
+  }
+  if(c->inputMask) {
+    k_apply_input_mask<<<blocks, 256, 0, c->stream>>>(c->inputMask, c->mask, n);
+    XB_LAUNCHED(c);
   }
   const int spreadWidth = (int)(c->p.hKernelWidth * c->p.inSpreadMaskFactor);
   const int r = spreadWidth / 2;

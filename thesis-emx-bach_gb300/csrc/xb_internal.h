@@ -28,7 +28,7 @@ namespace xb {
 
 constexpr uint16_t BAD_PIX_VAL = 1u << 0, SAT_PIXEL = 1u << 1,
                    LOW_PIXEL = 1u << 2, NAN_PIXEL = 1u << 3,
-                   BAD_CONV = 1u << 4, OK_CONV = 1u << 6,
+                   BAD_CONV = 1u << 4, INPUT_MASK = 1u << 5, OK_CONV = 1u << 6,
                    BAD_INPUT = 1u << 7, BAD_PIXEL_T = 1u << 8,
                    SKIP_T = 1u << 9, BAD_PIXEL_S = 1u << 10,
                    SKIP_S = 1u << 11, BAD_OUTPUT = 1u << 12,
@@ -166,6 +166,8 @@ struct xb_ctx {
   float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
   int mxTables = 0;        // the mixed build's monomial tables are on the device
   int ldlPanel = 1;        // option "ldl_panel": panel LDL^T kernel (0: the column kernel)
+  uint8_t* inputMask = nullptr;  // xb_set_input_mask (device, inputMaskW x inputMaskH) or none
+  int inputMaskW = 0, inputMaskH = 0;
   // frame graphs (xb_graph.cu)
   int graph = 0;           // option "graph": whole frames replay as captured CUDA graphs
   int capturing = 0;       // stage code is being captured: no host reads, no timers

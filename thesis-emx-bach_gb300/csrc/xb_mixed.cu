@@ -605,8 +605,8 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     k_conv_sub_f32(const float* __restrict__ I, const float* __restrict__ O,
                    const double* __restrict__ sol, const double* __restrict__ Kt,
                    const double* __restrict__ kernSumPtr, ConvArgsF a,
-                   uint16_t* __restrict__ mask, float* __restrict__ convF,
-                   float* __restrict__ diffF) {
+                   const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
+                   float* __restrict__ convF, float* __restrict__ diffF) {
   constexpr int HK = FK / 2, NK = FK * FK, PX = 7, TPR = FK / PX;  // threads per block row
   constexpr int TW = CV_BX * FK + 2 * HK, TH = FK + 2 * HK;
   // row padding with at most 2-way bank conflicts for the pixel loop's lanes
@@ -642,7 +642,8 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     const int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
     const float v = I[(size_t)gx + (size_t)gy * a.w];
     tile[ly][lx] = v;
-    bad[ly][lx] = (convMaskF(v, a.tH, a.tL) & BAD_INPUT) ? 1 : 0;
+    bad[ly][lx] = ((convMaskF(v, a.tH, a.tL) & BAD_INPUT) ||
+                   (inMask && inMask[(size_t)gx + (size_t)gy * a.w])) ? 1 : 0;
   }
   __syncthreads();
   // kernel of each block from the FP64 spatial-term images, rounded once
@@ -744,7 +745,8 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     const float v = (acc[q] + bgv) * invKernMult;
     const size_t id = (size_t)x + (size_t)y * a.w;
     const float tc = tile[ly + HK][lx0 + q + HK];
-    const uint16_t cm = convMaskF(tc, a.tH, a.tL);
+    uint16_t cm = convMaskF(tc, a.tH, a.tL);
+    if(inMask && inMask[id]) cm |= INPUT_MASK | BAD_INPUT;
     uint16_t nm = cm;
     if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
     if(anyq[q]) {
@@ -774,7 +776,7 @@ __global__ void k_kernel_terms(const double* __restrict__ sol, const double* __r
 }
 
 __global__ void k_border_f32(const float* __restrict__ O, int w, int h, int hK, float tH, float tL,
-                             uint16_t* __restrict__ mask, float* __restrict__ convF,
+                             const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask, float* __restrict__ convF,
                              float* __restrict__ diffF) {
   const long long n = (long long)w * h;
   for(long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < n;
@@ -782,6 +784,7 @@ __global__ void k_border_f32(const float* __restrict__ O, int w, int h, int hK, 
     const int x = (int)(id % w), y = (int)(id / w);
     if(x >= hK && x < w - hK && y >= hK && y < h - hK) continue;
     mask[id] |= afterMaskF(O[id], tH, tL);
+    if(inMask && inMask[id]) mask[id] |= INPUT_MASK | BAD_INPUT | BAD_OUTPUT;
     convF[id] = 1e-30f;
     diffF[id] = 1e-30f;
   }
@@ -1186,15 +1189,15 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
     switch(variant) {
       case 0:
         k_conv_sub_f32<21, 4><<<dim3((xSteps + 3) / 4, ySteps), 4 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
       case 1:
         k_conv_sub_f32<21, 2><<<dim3((xSteps + 1) / 2, ySteps), 2 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
       default:
         k_conv_sub_f32<21, 8><<<dim3((xSteps + 7) / 8, ySteps), 8 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->mask, c->convF, c->diffF);
+            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
     }
     XB_LAUNCHED(c);
@@ -1207,7 +1210,7 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   }
   const long long n = (long long)c->w * c->h;
   k_border_f32<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
-      (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->mask, c->convF, c->diffF);
+      (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convF, c->diffF);
   XB_LAUNCHED(c);
 }
 

@@ -52,7 +52,7 @@ _lib = None
 
 EXPORTS = [
     "xb_params_default", "xb_params_npsf", "xb_ctx_create", "xb_ctx_destroy",
-    "xb_last_error", "xb_ctx_set_params", "xb_set_option", "xb_init", "xb_init_f32",
+    "xb_last_error", "xb_ctx_set_params", "xb_set_option", "xb_set_input_mask", "xb_init", "xb_init_f32",
     "xb_init_device_f32", "xb_sss", "xb_cmv", "xb_cd", "xb_ksc", "xb_conv",
     "xb_sub", "xb_run", "xb_run_device", "xb_get_image", "xb_get_image_f64", "xb_get_mask",
     "xb_get_device_images", "xb_get_solution", "xb_get_array",
@@ -115,6 +115,7 @@ def lib():
     L.xb_batch_set_stream.argtypes = [vp, vp]
     L.xb_batch_set_params.argtypes = [vp, i, vp]
     L.xb_ctx_set_params.argtypes = [vp, vp]
+    L.xb_set_input_mask.argtypes = [vp, vp, i, i]
     L.xb_ranker_param_count.argtypes = []
     L.xb_ranker_set.argtypes = [vp, vp, i]
     L.xb_ranker_features.argtypes = [vp, i, vp, vp, vp, vp, i, P(i)]
@@ -277,6 +278,16 @@ class Context:
 
     def set_option(self, name, value):
         return self._check(self.L.xb_set_option(self.h, name.encode(), int(value)))
+
+    def set_input_mask(self, mask):
+        """Pixels to exclude from the following frames ((h, w), nonzero = bad;
+        None clears): they get INPUT_MASK | BAD_INPUT at init."""
+        if mask is None:
+            return self._check(self.L.xb_set_input_mask(self.h, None, 0, 0))
+        m = np.ascontiguousarray(mask != 0, dtype=np.uint8)
+        self._keep_mask = m
+        h, w = m.shape
+        return self._check(self.L.xb_set_input_mask(self.h, m.ctypes.data, w, h))
 
     def set_params(self, params):
         """Other parameters with the same basis, widths, orders and mode."""
