@@ -299,6 +299,43 @@ int xb_batch_set_params(xb_batch* b, int nFrames, const xb_params* params);
  * `stream` before and after a run bracket all of its GPU work.  NULL detaches. */
 int xb_batch_set_stream(xb_batch* b, void* stream);
 
+/* ---- streaming pipeline over FITS files ---------------------------------- */
+/* No counterpart in the reference, whose main (src/main.cpp:16-159) reads
+ * two FITS files, runs the stages and writes conv and sub once per process.
+ * A pipeline overlaps those steps across pairs: nIo reader threads decode
+ * FITS pairs into pinned host slots (FP32 for unscaled BITPIX -32, FP64
+ * otherwise), nWorkers contexts run xb_run on them (the frame graph when
+ * option "graph" is on; FP64 pairs run the plain stages and are refused in
+ * mixed mode), and nIo writer threads encode conv and diff as BITPIX -32.
+ * Each pair's images are those of xb_run on a single context. */
+typedef struct xb_pipeline xb_pipeline;
+typedef struct {
+  double wall_ms;       /* last run, start to last write */
+  double read_ms;       /* summed over reader threads: open + decode */
+  double compute_ms;    /* summed over workers: xb_run, copies included */
+  double write_ms;      /* summed over writer threads: encode + write */
+  double bytes_read;    /* FITS sample bytes decoded */
+  double bytes_written; /* FITS sample bytes encoded */
+  int pairs;            /* pairs in the last run */
+} xb_pipeline_stats;
+int xb_pipeline_create(const xb_params* p, int device, int nWorkers, int nIo,
+                       xb_pipeline** out);
+int xb_pipeline_destroy(xb_pipeline* pl);
+const char* xb_pipeline_last_error(const xb_pipeline* pl);
+/* Worker context i (options such as "graph", "rank", an input mask). */
+int xb_pipeline_worker(xb_pipeline* pl, int i, xb_ctx** ctx);
+/* Pair i: templatePath[i] and sciencePath[i] in; convPath[i] and diffPath[i]
+ * out (a NULL list or entry skips that output).  pairStatus[i] and
+ * kernSum[i] (each may be NULL) receive each pair's status (XB_ERR_IO for a
+ * file that cannot be opened, read or written) and kernel sum.  Returns
+ * XB_OK when every pair succeeded, else the first failing pair's status (its
+ * message in xb_pipeline_last_error). */
+int xb_pipeline_run_files(xb_pipeline* pl, int nPairs, const char* const* templatePath,
+                          const char* const* sciencePath, const char* const* convPath,
+                          const char* const* diffPath, int* pairStatus, double* kernSum);
+/* Timings and byte counts of the last run. */
+int xb_pipeline_stats_get(const xb_pipeline* pl, xb_pipeline_stats* out);
+
 /* ---- learned substamp ranking -------------------------------------------- */
 /* No counterpart in the reference.  A small network (a 3-layer CNN over the
  * 2x31x31 template/science window pair plus an MLP over 16 window

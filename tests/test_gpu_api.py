@@ -184,3 +184,49 @@ def test_input_mask_excludes_pixels(test01, mode):
             g.run(T, S)
             assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False),
                                   masked.astype(np.float32))
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_cli_pairs_stream_matches_single_runs(tmp_path, mode):
+    """-pairs: each listed pair's files equal those of a single-pair run of
+    the CLI (mixed mode with -graph replays frame graphs)."""
+    import shutil
+    import build_native
+    for f in ("test0.fits", "test1.fits"):
+        shutil.copy(GOLDEN / f, tmp_path / f)
+    pairs = [("test1.fits", "test0.fits", "a_"), ("test0.fits", "test1.fits", "b_"),
+             ("test1.fits", "test0.fits", None)]
+    lines = ["# template science prefix"] + [" ".join(x for x in p if x) for p in pairs]
+    (tmp_path / "list.txt").write_text("\n".join(lines) + "\n")
+    out = tmp_path / "o" / ""
+    out.mkdir()
+    extra = ["-mode", mode] + (["-graph"] if mode == "mixed" else [])
+    r = subprocess.run([str(build_native.CLI_BIN), "-pairs", str(tmp_path / "list.txt"),
+                        "-ip", str(tmp_path), "-op", str(out) + "/", "-pw", "2", "-pio", "2"] + extra,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert re.search(r"^3 of 3 pairs in ", r.stdout, flags=re.M), r.stdout
+    for i, (t, s, prefix) in enumerate(pairs):
+        prefix = prefix or f"{i}_"
+        single = tmp_path / f"single{i}_"
+        r1 = subprocess.run([str(build_native.CLI_BIN), "-ip", str(tmp_path), "-t", t, "-s", s,
+                             "-op", str(single), "-mode", mode], capture_output=True, text=True,
+                            timeout=300)
+        assert r1.returncode == 0, r1.stdout + r1.stderr
+        for name in ("diff.fits", "sub.fits"):
+            assert np.array_equal(read_fits(f"{out}/{prefix}{name}"), read_fits(f"{single}{name}")), \
+                (i, name)
+
+
+def test_cli_pairs_reports_a_failing_pair(tmp_path):
+    import shutil
+    import build_native
+    for f in ("test0.fits", "test1.fits"):
+        shutil.copy(GOLDEN / f, tmp_path / f)
+    (tmp_path / "list.txt").write_text("test1.fits test0.fits\nnothere.fits test0.fits\n")
+    r = subprocess.run([str(build_native.CLI_BIN), "-pairs", str(tmp_path / "list.txt"),
+                        "-ip", str(tmp_path), "-op", str(tmp_path) + "/"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1
+    assert "pair 1 (" in r.stdout and "status 8" in r.stdout, r.stdout
+    assert (tmp_path / "0_sub.fits").exists() and not (tmp_path / "1_sub.fits").exists()

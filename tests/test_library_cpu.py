@@ -68,6 +68,32 @@ def test_fits_roundtrip(xb, tmp_path):
     assert np.array_equal(read_fits(out), ref)
 
 
+def test_fits_reads_f64_and_scaled_files(xb, tmp_path):
+    """BITPIX -64 samples come back as written; BSCALE/BZERO are applied in
+    FP64 (bzero + bscale * v) for either width."""
+    from xbach_testlib import write_fits
+    L = xb.lib()
+    rng = np.random.default_rng(3)
+    a = rng.normal(100.0, 30.0, (37, 53))
+
+    def read(p):
+        d = ctypes.c_void_p()
+        w, h = ctypes.c_int(), ctypes.c_int()
+        assert L.xb_fits_read(str(p).encode(), ctypes.byref(d), ctypes.byref(w),
+                              ctypes.byref(h)) == 0
+        out = np.ctypeslib.as_array(ctypes.cast(d, ctypes.POINTER(ctypes.c_double)),
+                                    shape=(h.value, w.value)).copy()
+        L.xb_free(d)
+        return out
+
+    write_fits(tmp_path / "d.fits", a, bitpix=-64)
+    assert np.array_equal(read(tmp_path / "d.fits"), a)
+    write_fits(tmp_path / "s32.fits", a, bitpix=-32, bscale=2.5, bzero=-7.0)
+    assert np.array_equal(read(tmp_path / "s32.fits"), -7.0 + 2.5 * a.astype(np.float32).astype(np.float64))
+    write_fits(tmp_path / "s64.fits", a, bitpix=-64, bscale=0.5, bzero=1000.0)
+    assert np.array_equal(read(tmp_path / "s64.fits"), 1000.0 + 0.5 * a)
+
+
 def test_fits_rejects_missing_and_integer_files(xb, tmp_path):
     L = xb.lib()
     d = ctypes.c_void_p()

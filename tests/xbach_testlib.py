@@ -69,6 +69,25 @@ def read_fits(path):
     return a.astype(np.float64)
 
 
+def write_fits(path, a, bitpix=-32, bscale=None, bzero=None):
+    """Writes a 2-D array as a primary HDU (BITPIX -32 or -64, optional
+    BSCALE/BZERO cards; the samples are written as given)."""
+    a = np.asarray(a)
+    ny, nx = a.shape
+    cards = ["SIMPLE  =                    T", "BITPIX  = %20d" % bitpix,
+             "NAXIS   =                    2", "NAXIS1  = %20d" % nx, "NAXIS2  = %20d" % ny]
+    if bscale is not None:
+        cards.append("BSCALE  = %20r" % float(bscale))
+    if bzero is not None:
+        cards.append("BZERO   = %20r" % float(bzero))
+    cards.append("END")
+    hdr = "".join(c.ljust(80) for c in cards)
+    hdr = hdr.ljust((len(hdr) + 2879) // 2880 * 2880)
+    data = np.ascontiguousarray(a, dtype={-32: ">f4", -64: ">f8"}[bitpix]).tobytes()
+    data += bytes((2880 - len(data) % 2880) % 2880)
+    pathlib.Path(path).write_bytes(hdr.encode() + data)
+
+
 class Oracle:
     """ctypes view of oracle/liboracle_xbach.so (test infrastructure)."""
 

@@ -20,12 +20,22 @@
 //                       the noise model of the reference's chi^2, cd.cl:578)
 //   -rn x               read noise for -on (ADU, default 0)
 // Output: <op><o> (the convolved image, default diff.fits) and <op>sub.fits.
+//
+// Many pairs in one process (no counterpart in the reference):
+//   BACH -pairs list.txt [-pw n] [-pio n] [-graph] [other flags]
+// list.txt holds one pair per line, "template science [prefix]" (paths under
+// -ip; '#' starts a comment); pair i writes <op><prefix><o> and
+// <op><prefix>sub.fits (default prefix "<i>_").  The pairs stream through
+// xb_pipeline: -pio reader and writer threads (default 4) overlap FITS decode
+// and encode with -pw GPU workers (default 8); -graph replays frame graphs
+// (mixed mode); -im applies to every pair (-om / -on are single-pair only).
 
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
@@ -56,7 +66,9 @@ bool exists(int argc, const char** argv, const std::string& o) {
 struct Cli {
   std::string templateName, scienceName, outName = "diff.fits", inputPath = "res/",
                                          outPath = "out/";
-  std::string maskIn, maskOut, noiseOut;
+  std::string maskIn, maskOut, noiseOut, pairsFile;
+  int pipeWorkers = 8, pipeIo = 4;
+  bool graph = false;
   double readNoise = 0.0;
   bool verbose = false, verboseTime = false;
   int device = 0;
@@ -109,12 +121,108 @@ void parse(int argc, const char** argv, Cli& c) {
   if(exists(argc, argv, "-on")) c.noiseOut = option(argc, argv, "-on");
   if(exists(argc, argv, "-rn")) c.readNoise = std::atof(option(argc, argv, "-rn"));
   c.p.verbose = c.verbose;
+  if(exists(argc, argv, "-pairs")) {
+    const char* f = option(argc, argv, "-pairs");
+    if(!f) throw std::invalid_argument("-pairs expects a list file");
+    c.pairsFile = f;
+    if(exists(argc, argv, "-pw")) c.pipeWorkers = std::atoi(option(argc, argv, "-pw"));
+    if(exists(argc, argv, "-pio")) c.pipeIo = std::atoi(option(argc, argv, "-pio"));
+    c.graph = exists(argc, argv, "-graph");
+    return;
+  }
   const char* t = option(argc, argv, "-t");
   if(!t) throw std::invalid_argument("Template file Input is required!");
   c.templateName = t;
   const char* s = option(argc, argv, "-s");
   if(!s) throw std::invalid_argument("Science file input is required!");
   c.scienceName = s;
+}
+
+// -pairs: every listed pair through one streaming pipeline.
+int runPairs(const Cli& cli) {
+  std::ifstream in(cli.pairsFile);
+  if(!in) {
+    std::cout << "Unable to open file '" << cli.pairsFile << "'" << std::endl;
+    return 1;
+  }
+  std::vector<std::string> tp, sp, cp, dp;
+  std::string line;
+  while(std::getline(in, line)) {
+    const size_t hash = line.find('#');
+    if(hash != std::string::npos) line.resize(hash);
+    std::istringstream ls(line);
+    std::string t, s, prefix;
+    if(!(ls >> t)) continue;
+    if(!(ls >> s)) {
+      std::cout << "pair list line without a science image: " << line << std::endl;
+      return 1;
+    }
+    if(!(ls >> prefix)) prefix = std::to_string(tp.size()) + "_";
+    tp.push_back(cli.inputPath + "/" + t);
+    sp.push_back(cli.inputPath + "/" + s);
+    cp.push_back(cli.outPath + prefix + cli.outName);
+    dp.push_back(cli.outPath + prefix + "sub.fits");
+  }
+  const int n = (int)tp.size();
+  std::vector<const char*> T(n), S(n), C(n), D(n);
+  for(int i = 0; i < n; i++) {
+    T[i] = tp[i].c_str();
+    S[i] = sp[i].c_str();
+    C[i] = cp[i].c_str();
+    D[i] = dp[i].c_str();
+  }
+  xb_pipeline* pl = nullptr;
+  int rc = xb_pipeline_create(&cli.p, cli.device, cli.pipeWorkers, cli.pipeIo, &pl);
+  if(rc != XB_OK) {
+    std::cout << "pipeline creation failed (" << rc << ")" << std::endl;
+    return 1;
+  }
+  std::vector<uint8_t> mask;
+  int mw = 0, mh = 0;
+  if(!cli.maskIn.empty()) {
+    double* M = nullptr;
+    const std::string mPath = cli.inputPath + "/" + cli.maskIn;
+    if(xb_fits_read(mPath.c_str(), &M, &mw, &mh) != XB_OK) {
+      std::cout << "Unable to open file '" << mPath << "'" << std::endl;
+      xb_pipeline_destroy(pl);
+      return 1;
+    }
+    mask.resize((size_t)mw * mh);
+    for(size_t i = 0; i < mask.size(); i++) mask[i] = M[i] != 0.0 ? 1 : 0;
+    xb_free(M);
+  }
+  for(int i = 0; i < cli.pipeWorkers && rc == XB_OK; i++) {
+    xb_ctx* w = nullptr;
+    rc = xb_pipeline_worker(pl, i, &w);
+    if(rc == XB_OK && cli.graph) rc = xb_set_option(w, "graph", 1);
+    if(rc == XB_OK && !mask.empty()) rc = xb_set_input_mask(w, mask.data(), mw, mh);
+    if(rc != XB_OK) std::cout << (w ? xb_last_error(w) : "no worker") << std::endl;
+  }
+  std::vector<int> st(n, XB_OK);
+  std::vector<double> ks(n, 0.0);
+  if(rc == XB_OK) {
+    std::cout << "Running " << n << " pairs..." << std::endl;
+    xb_pipeline_run_files(pl, n, T.data(), S.data(), C.data(), D.data(), st.data(), ks.data());
+  }
+  xb_pipeline_stats ps{};
+  xb_pipeline_stats_get(pl, &ps);
+  int failed = 0;
+  for(int i = 0; i < n && rc == XB_OK; i++) {
+    if(st[i] != XB_OK) {
+      failed++;
+      std::cout << "pair " << i << " (" << tp[i] << ", " << sp[i] << ") failed with status "
+                << st[i] << std::endl;
+    } else if(cli.verbose) {
+      std::cout << "pair " << i << ": kernel sum " << ks[i] << std::endl;
+    }
+  }
+  if(rc == XB_OK)
+    std::cout << n - failed << " of " << n << " pairs in " << ps.wall_ms << " ms ("
+              << (ps.wall_ms > 0 ? 1000.0 * n / ps.wall_ms : 0.0) << " pairs/s); read "
+              << ps.read_ms << " ms, compute " << ps.compute_ms << " ms, write " << ps.write_ms
+              << " ms (thread totals)" << std::endl;
+  xb_pipeline_destroy(pl);
+  return rc == XB_OK && failed == 0 ? 0 : 1;
 }
 
 int fail(xb_ctx* ctx, int rc) {
@@ -135,6 +243,7 @@ int main(int argc, const char* argv[]) {
     std::cout << e.what() << '\n';
     return 1;
   }
+  if(!cli.pairsFile.empty()) return runPairs(cli);
   std::cout << "\nReading in images..." << std::endl;
   if(cli.verbose)
     std::cout << "template image name: " << cli.templateName
@@ -180,7 +289,30 @@ int main(int argc, const char* argv[]) {
       return fail(ctx, rc);
     }
   }
-  rc = xb_init(ctx, T, tw, th, S, sw, sh);
+  // the mixed path computes on FP32 images: FITS -32 samples convert
+  // exactly; anything FP32 cannot hold is refused rather than rounded
+  std::vector<float> t32, s32;
+  if(cli.p.mode == XB_MODE_MIXED && tw == sw && th == sh) {
+    const size_t n = (size_t)tw * th;
+    t32.resize(n);
+    s32.resize(n);
+    bool exact = true;
+    for(size_t i = 0; i < n; i++) {
+      t32[i] = (float)T[i];
+      s32[i] = (float)S[i];
+      exact = exact && ((double)t32[i] == T[i] || std::isnan(T[i])) &&
+              ((double)s32[i] == S[i] || std::isnan(S[i]));
+    }
+    if(!exact) {
+      std::cout << "mixed mode takes FP32 images; use -mode plain for FP64 data" << std::endl;
+      xb_free(T);
+      xb_free(S);
+      xb_ctx_destroy(ctx);
+      return 1;
+    }
+  }
+  rc = t32.empty() ? xb_init(ctx, T, tw, th, S, sw, sh)
+                   : xb_init_f32(ctx, t32.data(), tw, th, s32.data(), sw, sh);
   // the noise image needs the target frame after the fit
   std::vector<double> tCopy, sCopy;
   if(rc == XB_OK && !cli.noiseOut.empty()) {

@@ -5,15 +5,19 @@
 // does), NAXIS1 x NAXIS2 big-endian samples, BSCALE/BZERO applied when
 // present, returned as FP64.  Write: BITPIX -32 (FLOAT_IMG,
 // fitsUtil.cpp:47), 2880-byte blocks, big-endian.  Byte order is handled
-// with shifts, so the code is the same on x86-64 and aarch64.
+// with shifts, so the code is the same on x86-64 and aarch64.  The helpers in
+// namespace xb (xb_fits.h) also decode unscaled BITPIX -32 samples straight
+// into FP32 buffers, for the streaming pipeline.
 
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
+#include "xb_fits.h"
 #include "xbach.h"
 
 namespace {
@@ -32,26 +36,33 @@ bool cardValue(const char* card, const char* key, std::string& val) {
   return true;
 }
 
-uint64_t loadBE(const unsigned char* p, int n) {
-  uint64_t v = 0;
-  for(int i = 0; i < n; i++) v = (v << 8) | p[i];
-  return v;
+inline uint32_t loadBE32(const unsigned char* p) {
+  return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | (uint32_t)p[3];
 }
+inline uint64_t loadBE64(const unsigned char* p) {
+  return (uint64_t)loadBE32(p) << 32 | loadBE32(p + 4);
+}
+inline void storeBE32(unsigned char* p, uint32_t u) {
+  p[0] = (unsigned char)(u >> 24);
+  p[1] = (unsigned char)(u >> 16);
+  p[2] = (unsigned char)(u >> 8);
+  p[3] = (unsigned char)u;
+}
+
+constexpr size_t CHUNK = 1 << 16;  // samples converted per fread / fwrite
 
 }  // namespace
 
-extern "C" {
+namespace xb {
 
-int xb_fits_read(const char* path, double** data, int* w, int* h) {
-  if(!path || !data || !w || !h) return XB_ERR_ARG;
-  *data = nullptr;
+int fitsOpen(const char* path, FitsHeader& hd, FILE** fp) {
+  *fp = nullptr;
   FILE* f = std::fopen(path, "rb");
   if(!f) return XB_ERR_IO;
-  std::vector<unsigned char> raw;
   unsigned char blk[2880];
-  int bitpix = 0, naxis = -1;
+  int naxis = -1;
   long n1 = 0, n2 = 0;
-  double bscale = 1.0, bzero = 0.0;
+  hd = FitsHeader{};
   bool end = false;
   while(!end) {
     if(std::fread(blk, 1, 2880, f) != 2880) {
@@ -62,53 +73,67 @@ int xb_fits_read(const char* path, double** data, int* w, int* h) {
       const char* card = (const char*)blk + 80 * c;
       std::string v;
       if(std::strncmp(card, "END     ", 8) == 0) end = true;
-      else if(cardValue(card, "BITPIX", v)) bitpix = std::atoi(v.c_str());
+      else if(cardValue(card, "BITPIX", v)) hd.bitpix = std::atoi(v.c_str());
       else if(cardValue(card, "NAXIS", v)) naxis = std::atoi(v.c_str());
       else if(cardValue(card, "NAXIS1", v)) n1 = std::atol(v.c_str());
       else if(cardValue(card, "NAXIS2", v)) n2 = std::atol(v.c_str());
-      else if(cardValue(card, "BSCALE", v)) bscale = std::atof(v.c_str());
-      else if(cardValue(card, "BZERO", v)) bzero = std::atof(v.c_str());
+      else if(cardValue(card, "BSCALE", v)) hd.bscale = std::atof(v.c_str());
+      else if(cardValue(card, "BZERO", v)) hd.bzero = std::atof(v.c_str());
     }
   }
-  if(bitpix != -32 && bitpix != -64) {
+  // BITPIX -32 / -64 only, as src/fitsUtil.cpp:20-24 accepts
+  if((hd.bitpix != -32 && hd.bitpix != -64) || naxis != 2 || n1 <= 0 || n2 <= 0 ||
+     n1 > (1L << 20) || n2 > (1L << 20)) {
     std::fclose(f);
     return XB_ERR_UNSUPPORTED;
   }
-  if(naxis != 2 || n1 <= 0 || n2 <= 0 || n1 > (1L << 20) || n2 > (1L << 20)) {
-    std::fclose(f);
-    return XB_ERR_UNSUPPORTED;
-  }
-  const size_t n = (size_t)n1 * (size_t)n2, bytes = n * (size_t)(-bitpix / 8);
-  raw.resize(bytes);
-  if(std::fread(raw.data(), 1, bytes, f) != bytes) {
-    std::fclose(f);
-    return XB_ERR_IO;
-  }
-  std::fclose(f);
-  double* out = (double*)std::malloc(n * sizeof(double));
-  if(!out) return XB_ERR_NOMEM;
-  const bool scaled = bscale != 1.0 || bzero != 0.0;
-  for(size_t i = 0; i < n; i++) {
-    double v;
-    if(bitpix == -32) {
-      uint32_t u = (uint32_t)loadBE(&raw[i * 4], 4);
-      float fv;
-      std::memcpy(&fv, &u, 4);
-      v = fv;
-    } else {
-      uint64_t u = loadBE(&raw[i * 8], 8);
-      std::memcpy(&v, &u, 8);
-    }
-    out[i] = scaled ? bzero + bscale * v : v;
-  }
-  *data = out;
-  *w = (int)n1;
-  *h = (int)n2;
+  hd.w = (int)n1;
+  hd.h = (int)n2;
+  *fp = f;
   return XB_OK;
 }
 
-int xb_fits_write(const char* path, const double* data, int w, int h) {
-  if(!path || !data || w <= 0 || h <= 0) return XB_ERR_ARG;
+int fitsReadSamples(FILE* f, const FitsHeader& hd, void* dst, bool asDouble) {
+  const size_t n = (size_t)hd.w * hd.h, sz = (size_t)(-hd.bitpix / 8);
+  if(!asDouble && !hd.exactF32()) return XB_ERR_UNSUPPORTED;
+  if((sz == 4) == !asDouble) {
+    // same width: read in place, then swap in place
+    unsigned char* b = (unsigned char*)dst;
+    if(std::fread(b, sz, n, f) != n) return XB_ERR_IO;
+    if(sz == 4) {
+      for(size_t i = 0; i < n; i++) {
+        const uint32_t u = loadBE32(b + 4 * i);
+        std::memcpy(b + 4 * i, &u, 4);
+      }
+    } else {
+      for(size_t i = 0; i < n; i++) {
+        const uint64_t u = loadBE64(b + 8 * i);
+        std::memcpy(b + 8 * i, &u, 8);
+      }
+    }
+  } else {
+    // FP32 samples widened to FP64, through a chunk buffer
+    std::vector<unsigned char> raw(CHUNK * 4);
+    double* out = (double*)dst;
+    for(size_t i0 = 0; i0 < n; i0 += CHUNK) {
+      const size_t m = std::min(CHUNK, n - i0);
+      if(std::fread(raw.data(), 4, m, f) != m) return XB_ERR_IO;
+      for(size_t i = 0; i < m; i++) {
+        const uint32_t u = loadBE32(&raw[4 * i]);
+        float fv;
+        std::memcpy(&fv, &u, 4);
+        out[i0 + i] = fv;
+      }
+    }
+  }
+  if(asDouble && hd.scaled()) {
+    double* out = (double*)dst;
+    for(size_t i = 0; i < n; i++) out[i] = hd.bzero + hd.bscale * out[i];
+  }
+  return XB_OK;
+}
+
+int fitsWrite(const char* path, const float* f32, const double* f64, int w, int h) {
   // the reference writes to "!" + path: overwrite an existing file
   FILE* f = std::fopen(path, "wb");
   if(!f) return XB_ERR_IO;
@@ -131,19 +156,57 @@ int xb_fits_write(const char* path, const double* data, int w, int h) {
   hdr.resize((hdr.size() + 2879) / 2880 * 2880, ' ');
   bool ok = std::fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size();
   const size_t n = (size_t)w * h;
-  std::vector<unsigned char> out(((n * 4 + 2879) / 2880) * 2880, 0);
-  for(size_t i = 0; i < n; i++) {
-    float fv = (float)data[i];
-    uint32_t u;
-    std::memcpy(&u, &fv, 4);
-    out[i * 4 + 0] = (unsigned char)(u >> 24);
-    out[i * 4 + 1] = (unsigned char)(u >> 16);
-    out[i * 4 + 2] = (unsigned char)(u >> 8);
-    out[i * 4 + 3] = (unsigned char)u;
+  std::vector<unsigned char> out(CHUNK * 4);
+  for(size_t i0 = 0; ok && i0 < n; i0 += CHUNK) {
+    const size_t m = std::min(CHUNK, n - i0);
+    for(size_t i = 0; i < m; i++) {
+      const float fv = f32 ? f32[i0 + i] : (float)f64[i0 + i];
+      uint32_t u;
+      std::memcpy(&u, &fv, 4);
+      storeBE32(&out[4 * i], u);
+    }
+    ok = std::fwrite(out.data(), 4, m, f) == m;
   }
-  ok = ok && std::fwrite(out.data(), 1, out.size(), f) == out.size();
+  const size_t pad = (2880 - (n * 4) % 2880) % 2880;
+  if(ok && pad) {
+    std::memset(out.data(), 0, pad);
+    ok = std::fwrite(out.data(), 1, pad, f) == pad;
+  }
   ok = (std::fclose(f) == 0) && ok;
   return ok ? XB_OK : XB_ERR_IO;
+}
+
+}  // namespace xb
+
+extern "C" {
+
+int xb_fits_read(const char* path, double** data, int* w, int* h) {
+  if(!path || !data || !w || !h) return XB_ERR_ARG;
+  *data = nullptr;
+  xb::FitsHeader hd;
+  FILE* f = nullptr;
+  int rc = xb::fitsOpen(path, hd, &f);
+  if(rc != XB_OK) return rc;
+  double* out = (double*)std::malloc((size_t)hd.w * hd.h * sizeof(double));
+  if(!out) {
+    std::fclose(f);
+    return XB_ERR_NOMEM;
+  }
+  rc = xb::fitsReadSamples(f, hd, out, true);
+  std::fclose(f);
+  if(rc != XB_OK) {
+    std::free(out);
+    return rc;
+  }
+  *data = out;
+  *w = hd.w;
+  *h = hd.h;
+  return XB_OK;
+}
+
+int xb_fits_write(const char* path, const double* data, int w, int h) {
+  if(!path || !data || w <= 0 || h <= 0) return XB_ERR_ARG;
+  return xb::fitsWrite(path, nullptr, data, w, h);
 }
 
 void xb_free(void* p) { std::free(p); }

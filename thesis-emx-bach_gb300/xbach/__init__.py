@@ -61,7 +61,17 @@ EXPORTS = [
     "xb_batch_destroy", "xb_batch_last_error", "xb_batch_run", "xb_batch_run_device",
     "xb_batch_worker", "xb_batch_set_stream", "xb_batch_set_params", "xb_ranker_param_count", "xb_ranker_set",
     "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
+    "xb_pipeline_create", "xb_pipeline_destroy", "xb_pipeline_last_error", "xb_pipeline_worker",
+    "xb_pipeline_run_files", "xb_pipeline_stats_get",
 ]
+
+
+class PipelineStats(ctypes.Structure):
+    """xb_pipeline_stats of include/xbach.h."""
+    _fields_ = [("wall_ms", ctypes.c_double), ("read_ms", ctypes.c_double),
+                ("compute_ms", ctypes.c_double), ("write_ms", ctypes.c_double),
+                ("bytes_read", ctypes.c_double), ("bytes_written", ctypes.c_double),
+                ("pairs", ctypes.c_int)]
 
 
 def lib():
@@ -122,6 +132,14 @@ def lib():
     L.xb_ranker_forward.argtypes = [vp, vp, vp, i, vp, vp]
     L.xb_ranker_grad.argtypes = [vp, vp, vp, vp, vp, i, vp, vp, vp, vp]
     L.xb_ranker_adam.argtypes = [vp, vp, vp, vp, i, ctypes.c_float, vp]
+    L.xb_pipeline_create.argtypes = [P(XbParams), i, i, i, P(vp)]
+    L.xb_pipeline_destroy.argtypes = [vp]
+    L.xb_pipeline_last_error.argtypes = [vp]
+    L.xb_pipeline_last_error.restype = ctypes.c_char_p
+    L.xb_pipeline_worker.argtypes = [vp, i, P(vp)]
+    L.xb_pipeline_run_files.argtypes = [vp, i, P(ctypes.c_char_p), P(ctypes.c_char_p),
+                                        P(ctypes.c_char_p), P(ctypes.c_char_p), P(i), P(d)]
+    L.xb_pipeline_stats_get.argtypes = [vp, P(PipelineStats)]
     _lib = L
     return L
 
@@ -408,3 +426,64 @@ class Batch:
         f = self.L.xb_batch_run_device if device else self.L.xb_batch_run
         rc = f(self.h, n, self._ptrs(T_ptrs), self._ptrs(S_ptrs), w, h, cv, df, st, ks)
         return self._finish(rc, n, st, ks)
+
+
+class Pipeline:
+    """Streaming difference imaging over FITS files (an `xb_pipeline`):
+    `io` reader threads decode pairs into pinned slots, `workers` contexts run
+    them, `io` writer threads encode the outputs."""
+
+    def __init__(self, params=None, device=0, workers=8, io=4):
+        self.L = lib()
+        self.params = params if params is not None else default_params()
+        h = ctypes.c_void_p()
+        rc = self.L.xb_pipeline_create(ctypes.byref(self.params), device, workers, io,
+                                       ctypes.byref(h))
+        if rc != 0:
+            raise XbError(rc, "xb_pipeline_create failed")
+        self.h = h
+        self.n_workers = workers
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.xb_pipeline_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def worker(self, i):
+        c = ctypes.c_void_p()
+        if self.L.xb_pipeline_worker(self.h, i, ctypes.byref(c)):
+            raise IndexError(i)
+        return _Borrowed(c, self.params)
+
+    def set_option(self, name, value):
+        """xb_set_option on every worker context (e.g. "graph", "rank")."""
+        for i in range(self.n_workers):
+            self.worker(i).set_option(name, value)
+
+    @staticmethod
+    def _paths(vals):
+        if vals is None:
+            return None
+        return (ctypes.c_char_p * max(len(vals), 1))(
+            *[None if v is None else str(v).encode() for v in vals])
+
+    def run_files(self, templates, sciences, convs=None, diffs=None, check=True):
+        """Pair i: templates[i], sciences[i] in; convs[i], diffs[i] out (None
+        skips).  Returns (statuses, kernel sums); raises on the first failing
+        pair when `check`."""
+        n = len(templates)
+        st = (ctypes.c_int * max(n, 1))()
+        ks = (ctypes.c_double * max(n, 1))()
+        rc = self.L.xb_pipeline_run_files(self.h, n, self._paths(templates), self._paths(sciences),
+                                          self._paths(convs), self._paths(diffs), st, ks)
+        if rc != 0 and check:
+            raise XbError(rc, self.L.xb_pipeline_last_error(self.h).decode())
+        return [int(st[i]) for i in range(n)], [float(ks[i]) for i in range(n)]
+
+    def stats(self):
+        out = PipelineStats()
+        if self.L.xb_pipeline_stats_get(self.h, ctypes.byref(out)):
+            raise XbError(5, "xb_pipeline_stats_get failed")
+        return {k: getattr(out, k) for k, _ in PipelineStats._fields_}
