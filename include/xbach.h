@@ -102,6 +102,16 @@ typedef struct xb_params {
   float bg[XB_MAX_GAUSS];   /* 1/(2 sigma^2) stored as float, sigma 0.7/1.5/3.0 */
   int mode;                 /* XB_MODE_PLAIN or XB_MODE_MIXED */
   int verbose;              /* -v */
+  /* HOTPANTS-style extensions; the xb_params_default values (all zero) keep
+   * the reference's behaviour exactly. */
+  double gain;              /* e-/ADU of the noise model of the stamp chi^2:
+                             * sigma^2 = (|convolved frame| + |target|) / gain
+                             * + 2 readNoise^2 (cd.cl:578 is gain 1, no read
+                             * noise); <= 0 means 1 */
+  double readNoise;         /* ADU per frame in that model (0) */
+  int convPerPixel;         /* 1: the spatially varying kernel is evaluated at
+                             * every output pixel instead of once per
+                             * fK x fK block (conv.cl, bach.cpp:339-350) */
 } xb_params;
 
 /* Fill `p` with the reference defaults (include/argsUtil.h:7-57). */

@@ -978,11 +978,16 @@ double getBackground(const xbo_handle& o, int x, int y, const std::vector<double
 // calcSigs: src/cdkscUtil.cpp:477-583 -> calcSigBg (cd.cl:469-487), makeModel
 // (:489-531, FP32 model), calcSig (:533-598), reduceSig (:600-655).  Returns
 // one chi^2 per listed stamp (-1 when no pixel counts or chi^2 >= 1e10).
-// `T` supplies the |t| of the denominator, `Simg` the data modelled.
+// `T` supplies the |t| of the denominator, `Simg` the data modelled.  The
+// denominator (|t| + |s|) of cd.cl:578 becomes (|t| + |s|) * (1 / gain) +
+// 2 readNoise^2 with the noise-model extension of xb_params (the same value
+// for the defaults, gain 1 and no read noise).
 void calcSigs(xbo_handle& o, const StampSet& S, const std::vector<int>& ids,
               const std::vector<double>& sol, const std::vector<double>& T,
               const std::vector<double>& Simg, std::vector<double>& sig) {
   const Geo& g = o.g;
+  const double invGain = o.p.gain > 0.0 ? 1.0 / o.p.gain : 1.0;
+  const double rn2x2 = 2.0 * o.p.readNoise * o.p.readNoise;
   const int nT = (int)ids.size(), fSS = g.fSS, pix = fSS * fSS, w = o.w;
   const int reduceCount = (pix + 31) / 32;
   sig.assign(nT, 0.0);
@@ -1046,7 +1051,7 @@ void calcSigs(xbo_handle& o, const StampSet& S, const std::vector<int>& ids,
               o.mask[ai] |= NAN_PIXEL;
             } else {
               lc++;
-              s0 = diff * diff / (std::fabs(T[ai]) + std::fabs(sD));
+              s0 = diff * diff / ((std::fabs(T[ai]) + std::fabs(sD)) * invGain + rn2x2);
             }
           }
         }
@@ -1228,6 +1233,88 @@ void fitKernel(xbo_handle& o) {
   o.put("solution", o.solution);
 }
 
+// ------------------------------------------------------ per-pixel conv ---
+// Extension (xb_params.convPerPixel; the reference evaluates the kernel once
+// per fK x fK block, src/bach.cpp:339-350).  The kernel at pixel (x, y) is
+// sum_t P_t Kt[t], P_t = xf^i yf^j of the pixel (x power outer) and
+// Kt[t] = sol[1] vec_0 [t = 0] + sum_{n>=1} sol[2 + (n-1) nC2 + t] vec_n (FMA
+// chain over n); the convolved value is sum_t P_t (Kt[t] * I)(x, y), each
+// convolution an FMA chain over the window (rows, then columns), combined by
+// an FMA chain over t.  Pixels with a bad input in the window evaluate their
+// kernel tap by tap (FMA chain over t) for the 0.99 |kernel| rule of
+// conv.cl:70-100.
+void convPerPixel(xbo_handle& o, const std::vector<uint16_t>& cmask, double invKernMult) {
+  const Geo& g = o.g;
+  const int w = o.w, h = o.h, fK = g.fK, hK = g.hK, nk = fK * fK, nC2 = g.nComp2;
+  const int kOrder = o.p.kernelOrder;
+  const std::vector<double>& I = o.img[o.chosen];
+  const std::vector<double>& sol = o.solution;
+  std::vector<double> Kt((size_t)nC2 * nk);
+  for(int t = 0; t < nC2; t++)
+    for(int p = 0; p < nk; p++) {
+      double k0 = t == 0 ? sol[1] * o.vec[p] : 0.0;
+      for(int n = 1; n < g.nPSF; n++)
+        k0 = std::fma(sol[2 + (size_t)(n - 1) * nC2 + t], o.vec[(size_t)n * nk + p], k0);
+      Kt[(size_t)t * nk + p] = k0;
+    }
+  const double hx = 0.5 * w, hy = 0.5 * h;
+#pragma omp parallel for schedule(static)
+  for(int y = hK; y < h - hK; y++) {
+    std::vector<double> P(nC2);
+    for(int x = hK; x < w - hK; x++) {
+      const size_t id = (size_t)x + (size_t)y * w;
+      const double xf = (x - hx) / hx, yf = (y - hy) / hy;
+      double ax = 1.0;
+      int t = 0;
+      for(int i = 0; i <= kOrder; i++) {
+        double ay = 1.0;
+        for(int j = 0; j <= kOrder - i; j++) {
+          P[t++] = ax * ay;
+          ay *= yf;
+        }
+        ax *= xf;
+      }
+      double acc = 0.0;
+      for(t = 0; t < nC2; t++) {
+        const double* kk = &Kt[(size_t)t * nk];
+        double ct = 0.0;
+        for(int jj = 0; jj < fK; jj++)
+          for(int ii = 0; ii < fK; ii++)
+            ct = std::fma(kk[(2 * hK - ii) + (2 * hK - jj) * fK],
+                          I[(size_t)(x - hK + ii) + (size_t)(y - hK + jj) * w], ct);
+        acc = std::fma(P[t], ct, acc);
+      }
+      bool anyBad = false;
+      for(int jj = 0; jj < fK && !anyBad; jj++)
+        for(int ii = 0; ii < fK; ii++)
+          anyBad = anyBad || (cmask[(size_t)(x - hK + ii) + (size_t)(y - hK + jj) * w] & BAD_INPUT);
+      acc += getBackground(o, x, y, sol);
+      acc *= invKernMult;
+      o.conv[id] = acc;
+      uint16_t nm = cmask[id];
+      if(cmask[id] & BAD_INPUT) nm |= BAD_OUTPUT;
+      if(anyBad) {
+        double aks = 0.0, uks = 0.0;
+        for(int jj = 0; jj < fK; jj++)
+          for(int ii = 0; ii < fK; ii++) {
+            const int tap = (2 * hK - ii) + (2 * hK - jj) * fK;
+            double kv = 0.0;
+            for(t = 0; t < nC2; t++) kv = std::fma(P[t], Kt[(size_t)t * nk + tap], kv);
+            aks += std::fabs(kv);
+            if(!(cmask[(size_t)(x - hK + ii) + (size_t)(y - hK + jj) * w] & BAD_INPUT))
+              uks += std::fabs(kv);
+          }
+        if((uks / aks) < (double)0.99f) nm |= BAD_OUTPUT | BAD_CONV;
+        else nm |= OK_CONV;
+      }
+      o.mask[id] = nm;
+    }
+  }
+  for(int y = 0; y < h; y++)
+    for(int x = 0; x < w; x++)
+      if(!(x >= hK && x < w - hK && y >= hK && y < h - hK)) o.conv[(size_t)x + (size_t)y * w] = 1e-30;
+}
+
 // ---------------------------------------------------------- conv + sub ---
 // conv: src/bach.cpp:325-413, createConvMask (cl_kern/conv.cl:15-29), conv
 // (:31-97), maskAfterConv (:99-113).  sub: src/bach.cpp:415-440 ->
@@ -1260,6 +1347,9 @@ void convSub(xbo_handle& o) {
     cmask[id] = m;
   }
   o.conv.assign((size_t)w * h, 0.0);
+  if(o.p.convPerPixel) {
+    convPerPixel(o, cmask, invKernMult);
+  } else
 #pragma omp parallel for schedule(static)
   for(int y = 0; y < h; y++)
     for(int x = 0; x < w; x++) {

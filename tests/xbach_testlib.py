@@ -40,6 +40,9 @@ class XbParams(ctypes.Structure):
         ("bg", ctypes.c_float * XB_MAX_GAUSS),
         ("mode", ctypes.c_int),
         ("verbose", ctypes.c_int),
+        ("gain", ctypes.c_double),
+        ("readNoise", ctypes.c_double),
+        ("convPerPixel", ctypes.c_int),
     ]
 
 

@@ -16,9 +16,14 @@
 //   -om name            also write the final mask (<op>name, the 13 flag bits
 //                       as FITS values)
 //   -on name            also write the noise image of the difference
-//                       (<op>name: sqrt(|target| + |conv| + 2 rn^2), gain 1,
-//                       the noise model of the reference's chi^2, cd.cl:578)
-//   -rn x               read noise for -on (ADU, default 0)
+//                       (<op>name: sqrt((|target| + |conv|) / gain + 2 rn^2),
+//                       the noise model of the stamp chi^2, cd.cl:578)
+//   -rn x               read noise (ADU per frame, default 0) of that model,
+//                       used by the stamp chi^2 and by -on
+//   -gain x             gain (e-/ADU, default 1) of that model
+//   -pk                 evaluate the spatially varying kernel at every pixel
+//                       (default: once per kernel-sized block, as the
+//                       reference does)
 // Output: <op><o> (the convolved image, default diff.fits) and <op>sub.fits.
 //
 // Many pairs in one process (no counterpart in the reference):
@@ -119,7 +124,9 @@ void parse(int argc, const char** argv, Cli& c) {
   if(exists(argc, argv, "-im")) c.maskIn = option(argc, argv, "-im");
   if(exists(argc, argv, "-om")) c.maskOut = option(argc, argv, "-om");
   if(exists(argc, argv, "-on")) c.noiseOut = option(argc, argv, "-on");
-  if(exists(argc, argv, "-rn")) c.readNoise = std::atof(option(argc, argv, "-rn"));
+  if(exists(argc, argv, "-rn")) c.readNoise = c.p.readNoise = std::atof(option(argc, argv, "-rn"));
+  if(exists(argc, argv, "-gain")) c.p.gain = std::atof(option(argc, argv, "-gain"));
+  c.p.convPerPixel = exists(argc, argv, "-pk") ? 1 : 0;
   c.p.verbose = c.verbose;
   if(exists(argc, argv, "-pairs")) {
     const char* f = option(argc, argv, "-pairs");
@@ -411,8 +418,9 @@ int main(int argc, const char* argv[]) {
   if(!cli.noiseOut.empty()) {
     if((rc = xb_get_image_f64(ctx, XB_IMG_CONV, img.data())) != XB_OK) return fail(ctx, rc);
     const std::vector<double>& target = convTemplate ? sCopy : tCopy;
+    const double invGain = cli.p.gain > 0.0 ? 1.0 / cli.p.gain : 1.0;
     for(size_t i = 0; i < img.size(); i++)
-      img[i] = std::sqrt(std::fabs(target[i]) + std::fabs(img[i]) +
+      img[i] = std::sqrt((std::fabs(target[i]) + std::fabs(img[i])) * invGain +
                          2.0 * cli.readNoise * cli.readNoise);
     const std::string path = cli.outPath + cli.noiseOut;
     if(xb_fits_write(path.c_str(), img.data(), tw, th) != XB_OK) {

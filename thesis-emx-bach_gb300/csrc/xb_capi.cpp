@@ -4,6 +4,7 @@
 // parameter errors, the reference's exit paths) into status codes and keeps
 // a readable message for xb_last_error().
 
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -45,6 +46,9 @@ int validate(const xb_params& p, std::string& why) {
      g.nSol > MAX_SOL)
     return why = "parameters exceed this build's limits", XB_ERR_UNSUPPORTED;
   if(p.mode != XB_MODE_PLAIN && p.mode != XB_MODE_MIXED) return why = "unknown mode", XB_ERR_ARG;
+  if(!(p.readNoise >= 0.0) || !std::isfinite(p.readNoise) || !std::isfinite(p.gain))
+    return why = "bad gain or read noise", XB_ERR_ARG;
+  if(p.convPerPixel != 0 && p.convPerPixel != 1) return why = "convPerPixel is 0 or 1", XB_ERR_ARG;
   return XB_OK;
 }
 

@@ -175,6 +175,128 @@ __global__ void __launch_bounds__(CONV_THREADS)
 
 // Border pixels: conv = diff = 1e-30 (conv.cl:167, sub.cl:209); the mask
 // keeps its value plus maskAfterConv's bits.
+// Per-pixel kernel (option convPerPixel; no counterpart in the reference,
+// whose conv.cl evaluates the kernel once per fK x fK block at the block
+// centre).  The kernel at output pixel (x, y) is sum_t P_t(x, y) Kt[t] with
+// P_t = xf^i yf^j of the pixel itself, so the convolved value is
+// sum_t P_t (Kt[t] * I)(x, y): nComp2 convolutions per pixel, each summed in
+// the block kernel's tap order, then combined in t order.  Pixels whose
+// window holds a bad input evaluate the kernel tap by tap for the
+// 0.99 |kernel| rule (conv.cl:70-100).
+template <class T>
+__global__ void __launch_bounds__(CONV_THREADS)
+    k_conv_sub_pp_f64(const T* __restrict__ I, const T* __restrict__ O,
+                      const double* __restrict__ sol, const double* __restrict__ Kt,
+                      const double* __restrict__ kernSumPtr, ConvArgs a,
+                      const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
+                      double* __restrict__ convD, float* __restrict__ convF,
+                      double* __restrict__ diffD, float* __restrict__ diffF) {
+  extern __shared__ double cv_s[];
+  const int fK = a.fK, hK = a.hK, nk = fK * fK, tw = fK + 2 * hK;
+  const int nC2 = (a.kOrder + 1) * (a.kOrder + 2) / 2;
+  double* kt = cv_s;                         // nC2 * nk
+  double* tile = kt + nC2 * nk;              // tw * tw
+  uint8_t* bad = (uint8_t*)(tile + tw * tw); // tw * tw
+  const int xS = blockIdx.x, yS = blockIdx.y, tid = threadIdx.x;
+  for(int i = tid; i < nC2 * nk; i += CONV_THREADS) kt[i] = Kt[i];
+  const int x0 = xS * fK, y0 = yS * fK;
+  for(int i = tid; i < tw * tw; i += CONV_THREADS) {
+    int lx = i % tw, ly = i / tw;
+    int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
+    double v = (double)I[(size_t)gx + (size_t)gy * a.w];
+    tile[i] = v;
+    bad[i] = ((convMaskOf(v, a.tH, a.tL) & BAD_INPUT) ||
+              (inMask && inMask[(size_t)gx + (size_t)gy * a.w])) ? 1 : 0;
+  }
+  __syncthreads();
+  const double kernSum = *kernSumPtr;
+  const double invKernMult = a.scaleConv ? 1.0 / kernSum : 1.0;
+  const double convFactor = a.scaleConv ? kernSum : 1.0;
+  const double finalFactor = a.scaleConv ? -(1.0 / kernSum) : 1.0;
+  const double hx = 0.5 * a.w, hy = 0.5 * a.h;
+  for(int p = tid; p < nk; p += CONV_THREADS) {
+    const int lx = p % fK, ly = p / fK;
+    const int x = x0 + hK + lx, y = y0 + hK + ly;
+    if(x >= a.w - hK || y >= a.h - hK) continue;
+    // spatial monomials of this pixel, x power outer (makeKernelCoeffs order)
+    double P[(MAX_KORDER + 1) * (MAX_KORDER + 2) / 2];
+    {
+      const double xf = (x - hx) / hx, yf = (y - hy) / hy;
+      double ax = 1.0;
+      int t = 0;
+      for(int i = 0; i <= a.kOrder; i++) {
+        double ay = 1.0;
+        for(int j = 0; j <= a.kOrder - i; j++) {
+          P[t++] = ax * ay;
+          ay *= yf;
+        }
+        ax *= xf;
+      }
+    }
+    double acc = 0.0;
+    int anyBad = 0;
+    for(int t = 0; t < nC2; t++) {
+      const double* kk = kt + t * nk;
+      double ct = 0.0;
+      for(int jj = 0; jj < fK; jj++) {
+        const double* trow = tile + (ly + jj) * tw + lx;
+        const double* krow = kk + (2 * hK - jj) * fK;
+#pragma unroll 7
+        for(int ii = 0; ii < fK; ii++) ct = fma(krow[2 * hK - ii], trow[ii], ct);
+      }
+      acc = fma(P[t], ct, acc);
+    }
+    for(int jj = 0; jj < fK && !anyBad; jj++) {
+      const uint8_t* brow = bad + (ly + jj) * tw + lx;
+      for(int ii = 0; ii < fK; ii++) anyBad |= brow[ii];
+    }
+    // background polynomial (getBackground, cd.cl:444-467)
+    {
+      const double bxf = (x - 0.5 * a.w) / (0.5 * a.w), byf = (y - 0.5 * a.h) / (0.5 * a.h);
+      double bg = 0.0, ax = 1.0;
+      int k = a.nComp + 2;
+      for(int i = 0; i <= a.bgOrder; i++) {
+        double ay = 1.0;
+        for(int j = 0; j <= a.bgOrder - i; j++) {
+          bg += sol[k++] * ax * ay;
+          ay *= byf;
+        }
+        ax *= bxf;
+      }
+      acc += bg;
+    }
+    acc *= invKernMult;
+    const size_t id = (size_t)x + (size_t)y * a.w;
+    const double tc = tile[(ly + hK) * tw + lx + hK];
+    uint16_t cm = convMaskOf(tc, a.tH, a.tL);
+    if(inMask && inMask[id]) cm |= INPUT_MASK | BAD_INPUT;
+    uint16_t nm = cm;
+    if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
+    if(anyBad) {
+      // this pixel's kernel, tap by tap in window order
+      double aks = 0.0, uks = 0.0;
+      for(int jj = 0; jj < fK; jj++)
+        for(int ii = 0; ii < fK; ii++) {
+          const int tap = (2 * hK - ii) + (2 * hK - jj) * fK;
+          double kv = 0.0;
+          for(int t = 0; t < nC2; t++) kv = fma(P[t], kt[t * nk + tap], kv);
+          aks += fabs(kv);
+          if(!bad[(ly + jj) * tw + lx + ii]) uks += fabs(kv);
+        }
+      if((uks / aks) < (double)0.99f) nm |= BAD_OUTPUT | BAD_CONV;
+      else nm |= OK_CONV;
+    }
+    const double o = (double)O[id];
+    nm |= afterMaskOf(o, a.tH, a.tL);
+    mask[id] = nm;
+    convD[id] = acc;
+    convF[id] = (float)acc;
+    const double d = (nm & BAD_OUTPUT) ? 1e-30 : (acc * convFactor - o) * finalFactor;
+    diffD[id] = d;
+    diffF[id] = (float)d;
+  }
+}
+
 template <class T>
 __global__ void k_border(const T* __restrict__ O, int w, int h, int hK, double tH, double tL,
                          const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
@@ -245,7 +367,38 @@ void stageConvSub(xb_ctx* c, bool doSub) {
   const size_t smem = ((size_t)g.fK * g.fK + (size_t)tw * tw + g.nPSF) * sizeof(double) + (size_t)tw * tw;
   const int I = c->chosen, O = 1 - c->chosen;
   dim3 grid(a.xSteps, ySteps);
-  if(c->imgIsF64) {
+  if(c->p.convPerPixel) {
+    const double* Kt = kernelTermsLaunch(c);
+    const size_t smemPP = ((size_t)g.nComp2 * g.fK * g.fK + (size_t)tw * tw) * sizeof(double) +
+                          (size_t)tw * tw;
+    int optin = 0;
+    XB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    if(c->p.kernelOrder > MAX_KORDER || smemPP > (size_t)optin)
+      throw XbError{XB_ERR_UNSUPPORTED, "per-pixel kernel: kernel order or width too large"};
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_pp_f64<double>, c->device));
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_pp_f64<float>, c->device));
+    KT_SCOPE(c, "conv_sub");
+    if(c->imgIsF64)
+      k_conv_sub_pp_f64<double><<<grid, CONV_THREADS, smemPP, c->stream>>>(
+          (const double*)c->img[I], (const double*)c->img[O], c->dSol, Kt, ks, a, c->inputMask,
+          c->mask, c->convD, c->convF, c->diffD, c->diffF);
+    else
+      k_conv_sub_pp_f64<float><<<grid, CONV_THREADS, smemPP, c->stream>>>(
+          (const float*)c->img[I], (const float*)c->img[O], c->dSol, Kt, ks, a, c->inputMask,
+          c->mask, c->convD, c->convF, c->diffD, c->diffF);
+    XB_LAUNCHED(c);
+  }
+  if(c->p.convPerPixel) {
+    const int blocks = (int)std::min<long long>((n + 255) / 256, c->smCount * 8);
+    if(c->imgIsF64)
+      k_border<double><<<blocks, 256, 0, c->stream>>>(
+          (const double*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convD,
+          c->convF, c->diffD, c->diffF);
+    else
+      k_border<float><<<blocks, 256, 0, c->stream>>>(
+          (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convD,
+          c->convF, c->diffD, c->diffF);
+  } else if(c->imgIsF64) {
     { KT_SCOPE(c, "conv_sub");
     k_conv_sub_f64<double><<<grid, CONV_THREADS, smem, c->stream>>>(
         (const double*)c->img[I], (const double*)c->img[O], c->dSol, c->dVec, ks, a, c->inputMask,

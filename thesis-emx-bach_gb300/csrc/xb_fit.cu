@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(SIG_THREADS)
            const double* __restrict__ W, int wRows, int hSS, int nPSF, int kOrder, int bgOrder,
            int nComp, const double* __restrict__ sol, const T* __restrict__ tImg,
            const T* __restrict__ sImg, uint16_t* __restrict__ mask, int w, int h,
-           double* __restrict__ sig) {
+           double invGain, double rn2x2, double* __restrict__ sig) {
   extern __shared__ double sig_s[];
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, pix = fSS * fSS, reduceCount = (pix + 31) / 32;
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(SIG_THREADS)
           maskOr(mask, ai, NAN_PIXEL);
         } else {
           ok = 1;
-          s0 = diff * diff / (fabs((double)tImg[ai]) + fabs(sD));
+          s0 = diff * diff / ((fabs((double)tImg[ai]) + fabs(sD)) * invGain + rn2x2);
         }
       }
     }
@@ -992,12 +992,14 @@ static void computeSigs(xb_ctx* c, int si, const int* dList, int nList, const do
     k_sigs<double><<<nList, SIG_THREADS, smem, c->stream>>>(
         dList, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const double*)c->img[convImg],
-        (const double*)c->img[other], c->mask, c->w, c->h, dSig);
+        (const double*)c->img[other], c->mask, c->w, c->h, noiseInvGain(c->p),
+        noiseRn2x2(c->p), dSig);
   else
     k_sigs<float><<<nList, SIG_THREADS, smem, c->stream>>>(
         dList, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const float*)c->img[convImg],
-        (const float*)c->img[other], c->mask, c->w, c->h, dSig);
+        (const float*)c->img[other], c->mask, c->w, c->h, noiseInvGain(c->p),
+        noiseRn2x2(c->p), dSig);
   XB_LAUNCHED(c);
   }
 }

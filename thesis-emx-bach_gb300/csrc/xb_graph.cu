@@ -262,6 +262,9 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
     put(p.bg[i]);
   }
   put(p.mode);
+  put(p.gain);
+  put(p.readNoise);
+  put(p.convPerPixel);
   put(c->gramFp64);
   put(c->ldlPanel);
   const uintptr_t im = (uintptr_t)c->inputMask;  // the mask's content is read at replay

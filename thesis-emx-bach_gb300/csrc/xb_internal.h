@@ -40,6 +40,7 @@ constexpr int MAX_FK = 41;          // kernel width (hKernelWidth <= 20)
 constexpr int MAX_FSS = 63;         // substamp width (hSStampWidth <= 31)
 constexpr int MAX_SOL = 2048;       // solution length
 constexpr int MAX_MAXSS = 16;       // substamp slots per stamp
+constexpr int MAX_KORDER = 8;       // per-pixel kernel: spatial terms kept per thread
 
 struct Geo {
   int fSS, hSS, fK, hK, nPSF, nComp1, nComp2, nComp, nBG, matSize, nSol;
@@ -303,6 +304,10 @@ void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSo
 void luFallbackSolve(xb_ctx* c, const double* M, double* F, int n, double* rhs, int* piv,
                      int* singular, const int* status);
 void convSubMixed(xb_ctx* c, double* dKernSum);
+// Kernel images of the spatial terms, FP64 (nComp2 x fK^2): the kernel at
+// (xf, yf) is sum_t xf^i yf^j Kt[t], t over the (i, j) of the kernel
+// polynomial, x power outer.
+double* kernelTermsLaunch(xb_ctx* c);
 void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase, double* M,
                       double* rhs, const int* liveN = nullptr);
 
@@ -327,6 +332,10 @@ void rankSubstamps(xb_ctx* c);
 bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G,
                      const int* liveN = nullptr);
 inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
+// Noise model of the stamp chi^2: sigma^2 = (|a| + |b|) * invGain + rn2x2,
+// which is |a| + |b| exactly for the defaults (gain 1, no read noise).
+inline double noiseInvGain(const xb_params& p) { return p.gain > 0.0 ? 1.0 / p.gain : 1.0; }
+inline double noiseRn2x2(const xb_params& p) { return 2.0 * p.readNoise * p.readNoise; }
 
 // ---- frame graphs (xb_graph.cu) -------------------------------------------
 // Capture helpers for stage code running under c->capturing: a conditional

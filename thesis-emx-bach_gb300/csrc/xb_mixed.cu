@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(MX_THREADS)
                const float* __restrict__ W, int wRows, int ldW, int hSS, int nPSF, int kOrder,
                int bgOrder, int nComp, const double* __restrict__ sol, const T* __restrict__ tImg,
                const T* __restrict__ sImg, uint16_t* __restrict__ mask, int w, int h,
-               double* __restrict__ sig) {
+               float invGain, float rn2x2, double* __restrict__ sig) {
   __shared__ double coeff[MAX_NPSF];
   __shared__ float cHi[MAX_NPSF], cLo[MAX_NPSF];
   __shared__ double sBg;
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(MX_THREADS)
           maskOr(mask, ai, NAN_PIXEL);
         } else {
           const float d = (m0 - sF) + bgF;
-          part += d * d / (fabsf((float)tImg[ai]) + fabsf(sF));
+          part += d * d / ((fabsf((float)tImg[ai]) + fabsf(sF)) * invGain + rn2x2);
           cnt++;
         }
       }
@@ -761,6 +761,202 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
   }
 }
 
+// Per-pixel kernel in FP32 (option convPerPixel; the FP64 statement is
+// k_conv_sub_pp_f64).  The kernel at pixel (x, y) is written as the block
+// kernel plus corrections, k(x, y) = k(xc, yc) + sum_{t>=1} dP_t Kt[t] with
+// dP_t = P_t(x, y) - P_t(xc, yc): the block kernel is evaluated in FP64 and
+// rounded once (as k_conv_sub_f32 does), and the FP32 rounding of the
+// term images only scales the small dP_t (|dP| <= ~fK / frame size), so
+// fits whose spatial terms cancel keep the block kernel's accuracy.  Same
+// tiling as k_conv_sub_f32: 7 pixels of one row per thread, the window in
+// registers, one pass over the tile per term.
+template <int FK, int CV_BX>
+__global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
+    k_conv_sub_pp_f32(const float* __restrict__ I, const float* __restrict__ O,
+                      const double* __restrict__ sol, const double* __restrict__ Kt,
+                      const double* __restrict__ kernSumPtr, ConvArgsF a,
+                      const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
+                      float* __restrict__ convF, float* __restrict__ diffF) {
+  constexpr int HK = FK / 2, NK = FK * FK, PX = 7, TPR = FK / PX;
+  constexpr int TH = FK + 2 * HK, TW = CV_BX * FK + 2 * HK;
+  constexpr int MAXT = (MAX_KORDER + 1) * (MAX_KORDER + 2) / 2;
+  __shared__ float tile[TH][TW + 1];
+  __shared__ unsigned char bad[TH][TW + 1];
+  __shared__ unsigned char rowBad[TH][CV_BX * FK];
+  __shared__ float kern[CV_BX][NK];
+  __shared__ double poly[CV_BX][MAXT];
+  __shared__ float bgc[16];
+  extern __shared__ float ktf[];  // nC2 * NK, term 0 unused
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int xB0 = blockIdx.x * CV_BX, yB = blockIdx.y;
+  const int x0 = xB0 * FK, y0 = yB * FK;
+  const int nC2 = (a.kOrder + 1) * (a.kOrder + 2) / 2;
+  const double hx = 0.5 * a.w, hy = 0.5 * a.h;
+  if(tid < CV_BX) {
+    // spatial terms at the block centre (conv(), src/bach.cpp:339-350)
+    const double xf = ((xB0 + tid) * FK + 2 * HK - hx) / hx, yf = (yB * FK + 2 * HK - hy) / hy;
+    double ax = 1.0;
+    int t = 0;
+    for(int i = 0; i <= a.kOrder; i++) {
+      double ay = 1.0;
+      for(int j = 0; j <= a.kOrder - i; j++) {
+        poly[tid][t++] = ax * ay;
+        ay *= yf;
+      }
+      ax *= xf;
+    }
+  }
+  for(int e = tid; e < nC2 * NK; e += nthr) ktf[e] = (float)Kt[e];
+  for(int i = tid; i < TH * TW; i += nthr) {
+    const int ly = i / TW, lx = i % TW;
+    const int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
+    const float v = I[(size_t)gx + (size_t)gy * a.w];
+    tile[ly][lx] = v;
+    bad[ly][lx] = ((convMaskF(v, a.tH, a.tL) & BAD_INPUT) ||
+                   (inMask && inMask[(size_t)gx + (size_t)gy * a.w])) ? 1 : 0;
+  }
+  const int nBgC = (a.bgOrder + 1) * (a.bgOrder + 2) / 2;
+  if(tid < nBgC && tid < 16) bgc[tid] = (float)sol[a.nComp + 2 + tid];
+  __syncthreads();
+  for(int e = tid; e < CV_BX * NK; e += nthr) {
+    const int b = e / NK, p = e % NK;
+    double k0 = 0.0;
+    for(int t = 0; t < nC2; t++) k0 = fma(poly[b][t], Kt[(size_t)t * NK + p], k0);
+    kern[b][p] = (float)k0;
+  }
+  for(int e = tid; e < TH * CV_BX * FK; e += nthr) {
+    const int ly = e / (CV_BX * FK), lx = e % (CV_BX * FK);
+    unsigned char o = 0;
+#pragma unroll
+    for(int d = 0; d < FK; d++) o |= bad[ly][lx + d];
+    rowBad[ly][lx] = o;
+  }
+  __syncthreads();
+  const float kernSum = (float)*kernSumPtr;
+  const float invKernMult = a.scaleConv ? 1.f / kernSum : 1.f;
+  const float convFactor = a.scaleConv ? kernSum : 1.f;
+  const float finalFactor = a.scaleConv ? -(1.f / kernSum) : 1.f;
+  const int perBlock = FK * TPR;
+  if(tid >= CV_BX * perBlock) return;
+  const int b = tid / perBlock, r = tid % perBlock, ly = r / TPR, lx0 = b * FK + (r % TPR) * PX;
+  const double yf = ((double)(y0 + HK + ly) - hy) / hy;
+  double xf[PX], xp[PX];
+  float base[PX], corr[PX];
+#pragma unroll
+  for(int q = 0; q < PX; q++) {
+    xf[q] = ((double)(x0 + HK + lx0 + q) - hx) / hx;
+    xp[q] = 1.0;
+    corr[q] = 0.f;
+  }
+  // t = 0 pass: the block kernel
+  {
+#pragma unroll
+    for(int q = 0; q < PX; q++) base[q] = 0.f;
+    for(int jj = 0; jj < FK; jj++) {
+      float win[PX + FK - 1];
+#pragma unroll
+      for(int q = 0; q < PX + FK - 1; q++) win[q] = tile[ly + jj][lx0 + q];
+      const float* krow = kern[b] + (FK - 1 - jj) * FK;
+#pragma unroll
+      for(int ii = 0; ii < FK; ii++) {
+        const float kk = krow[FK - 1 - ii];
+#pragma unroll
+        for(int q = 0; q < PX; q++) base[q] = fmaf(kk, win[q + ii], base[q]);
+      }
+    }
+  }
+  // t >= 1 passes: the spatial-term images weighted by dP_t
+  int t = 0;
+  for(int i = 0; i <= a.kOrder; i++) {
+    double yp = 1.0;
+    for(int j = 0; j <= a.kOrder - i; j++, t++) {
+      if(t > 0) {
+        const float* kb = ktf + t * NK;
+        float ct[PX];
+#pragma unroll
+        for(int q = 0; q < PX; q++) ct[q] = 0.f;
+        for(int jj = 0; jj < FK; jj++) {
+          float win[PX + FK - 1];
+#pragma unroll
+          for(int q = 0; q < PX + FK - 1; q++) win[q] = tile[ly + jj][lx0 + q];
+          const float* krow = kb + (FK - 1 - jj) * FK;
+#pragma unroll
+          for(int ii = 0; ii < FK; ii++) {
+            const float kk = krow[FK - 1 - ii];
+#pragma unroll
+            for(int q = 0; q < PX; q++) ct[q] = fmaf(kk, win[q + ii], ct[q]);
+          }
+        }
+#pragma unroll
+        for(int q = 0; q < PX; q++)
+          corr[q] = fmaf((float)(xp[q] * yp - poly[b][t]), ct[q], corr[q]);
+      }
+      yp *= yf;
+    }
+#pragma unroll
+    for(int q = 0; q < PX; q++) xp[q] *= xf[q];
+  }
+  const float hxF = 0.5f * (float)a.w, hyF = 0.5f * (float)a.h;
+  const float ihxF = 1.f / hxF, ihyF = 1.f / hyF;
+#pragma unroll
+  for(int q = 0; q < PX; q++) {
+    const int x = x0 + HK + lx0 + q, y = y0 + HK + ly;
+    if(x >= a.w - HK || y >= a.h - HK) continue;
+    unsigned char any = 0;
+    for(int jj = 0; jj < FK; jj++) any |= rowBad[ly + jj][lx0 + q];
+    const float bxf = ((float)x - hxF) * ihxF, byf = ((float)y - hyF) * ihyF;
+    float bgv = 0.f, ax = 1.f;
+    int k = 0;
+    for(int i = 0; i <= a.bgOrder; i++) {
+      float ay = 1.f;
+      for(int j = 0; j <= a.bgOrder - i; j++) {
+        bgv = fmaf(bgc[k++], ax * ay, bgv);
+        ay *= byf;
+      }
+      ax *= bxf;
+    }
+    const float v = (base[q] + corr[q] + bgv) * invKernMult;
+    const size_t id = (size_t)x + (size_t)y * a.w;
+    const float tc = tile[ly + HK][lx0 + q + HK];
+    uint16_t cm = convMaskF(tc, a.tH, a.tL);
+    if(inMask && inMask[id]) cm |= INPUT_MASK | BAD_INPUT;
+    uint16_t nm = cm;
+    if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
+    if(any) {
+      // this pixel's kernel tap by tap, for the 0.99 |kernel| rule
+      float dP[MAXT];
+      {
+        double xpw = 1.0;
+        int tt = 0;
+        for(int i = 0; i <= a.kOrder; i++) {
+          double ypw = 1.0;
+          for(int j = 0; j <= a.kOrder - i; j++, tt++) {
+            dP[tt] = (float)(xpw * ypw - poly[b][tt]);
+            ypw *= yf;
+          }
+          xpw *= xf[q];
+        }
+      }
+      float aks = 0.f, uks = 0.f;
+      for(int jj = 0; jj < FK; jj++)
+        for(int ii = 0; ii < FK; ii++) {
+          const int tap = (FK - 1 - ii) + (FK - 1 - jj) * FK;
+          float kv = kern[b][tap];
+          for(int tt = 1; tt < nC2; tt++) kv = fmaf(dP[tt], ktf[tt * NK + tap], kv);
+          aks += fabsf(kv);
+          if(!bad[ly + jj][lx0 + q + ii]) uks += fabsf(kv);
+        }
+      if((uks / aks) < 0.99f) nm |= BAD_OUTPUT | BAD_CONV;
+      else nm |= OK_CONV;
+    }
+    const float o = O[id];
+    nm |= afterMaskF(o, a.tH, a.tL);
+    mask[id] = nm;
+    convF[id] = v;
+    diffF[id] = (nm & BAD_OUTPUT) ? 1e-30f : (v * convFactor - o) * finalFactor;
+  }
+}
+
 // Kernel images of the spatial terms, FP64: Kt[t] = sum_n sol[2+(n-1)*nC2+t]
 // * basis_n (+ sol[1] * basis_0 for the constant term), so that the kernel at
 // (xf, yf) is sum_t xf^i yf^j Kt[t] (makeKernelCoeffs + makeKernel,
@@ -1050,12 +1246,14 @@ void sigsMixed(xb_ctx* c, int si, const int* dList, int nList, const double* dSo
     k_sigs_f32<double><<<nList, MX_THREADS, 0, c->stream>>>(
         dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const double*)c->img[convImg],
-        (const double*)c->img[other], c->mask, c->w, c->h, dSig);
+        (const double*)c->img[other], c->mask, c->w, c->h, (float)noiseInvGain(c->p),
+        (float)noiseRn2x2(c->p), dSig);
   else
     k_sigs_f32<float><<<nList, MX_THREADS, 0, c->stream>>>(
         dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Wf, g.wRows, mixedLd(g), g.hSS, g.nPSF,
         c->p.kernelOrder, c->p.backgroundOrder, g.nComp, dSol, (const float*)c->img[convImg],
-        (const float*)c->img[other], c->mask, c->w, c->h, dSig);
+        (const float*)c->img[other], c->mask, c->w, c->h, (float)noiseInvGain(c->p),
+        (float)noiseRn2x2(c->p), dSig);
   XB_LAUNCHED(c);
 }
 
@@ -1166,11 +1364,7 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   if(g.fK != 21) throw XbError{XB_ERR_UNSUPPORTED, "mixed conv is built for 21-px kernels"};
   const int I = c->chosen, O = 1 - c->chosen;
   if(c->imgIsF64) throw XbError{XB_ERR_UNSUPPORTED, "mixed mode takes FP32 images"};
-  const int nk = g.fK * g.fK;
-  double* Kt = buf<double>(c, "kernel_terms", (size_t)g.nComp2 * nk);
-  k_kernel_terms<<<(g.nComp2 * nk + 255) / 256, 256, 0, c->stream>>>(c->dSol, c->dVec, g.nPSF,
-                                                                      g.nComp2, nk, Kt);
-  XB_LAUNCHED(c);
+  const double* Kt = kernelTermsLaunch(c);
   ConvArgsF a{};
   a.w = c->w;
   a.h = c->h;
@@ -1202,9 +1396,22 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
     }
     XB_LAUNCHED(c);
   };
-  // blocks per CTA: 4 (default), 2 or 8; the three give identical images
-  const int v = tunedVariant(c, "conv_sub_f32", (long long)c->w * 100003LL + c->h, 3, launch);
-  {
+  if(c->p.convPerPixel) {
+    const int nC2 = g.nComp2, nk = g.fK * g.fK;
+    const size_t smemPP = (size_t)nC2 * nk * sizeof(float);
+    int optin = 0;
+    XB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    if(c->p.kernelOrder > MAX_KORDER || smemPP + 16 * 1024 > (size_t)optin)
+      throw XbError{XB_ERR_UNSUPPORTED, "per-pixel kernel: kernel order too large"};
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_pp_f32<21, 2>, c->device));
+    KT_SCOPE(c, "conv_sub");
+    k_conv_sub_pp_f32<21, 2><<<dim3((xSteps + 1) / 2, ySteps), 2 * 63, smemPP, c->stream>>>(
+        (const float*)c->img[I], (const float*)c->img[O], c->dSol, Kt, dKernSum, a, c->inputMask,
+        c->mask, c->convF, c->diffF);
+    XB_LAUNCHED(c);
+  } else {
+    // blocks per CTA: 4 (default), 2 or 8; the three give identical images
+    const int v = tunedVariant(c, "conv_sub_f32", (long long)c->w * 100003LL + c->h, 3, launch);
     KT_SCOPE(c, "conv_sub");
     launch(v);
   }
@@ -1212,6 +1419,16 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   k_border_f32<<<std::min<long long>((n + 255) / 256, c->smCount * 8), 256, 0, c->stream>>>(
       (const float*)c->img[O], c->w, c->h, g.hK, a.tH, a.tL, c->inputMask, c->mask, c->convF, c->diffF);
   XB_LAUNCHED(c);
+}
+
+double* kernelTermsLaunch(xb_ctx* c) {
+  const Geo& g = c->g;
+  const int nk = g.fK * g.fK;
+  double* Kt = buf<double>(c, "kernel_terms", (size_t)g.nComp2 * nk);
+  k_kernel_terms<<<(g.nComp2 * nk + 255) / 256, 256, 0, c->stream>>>(c->dSol, c->dVec, g.nPSF,
+                                                                      g.nComp2, nk, Kt);
+  XB_LAUNCHED(c);
+  return Kt;
 }
 
 }  // namespace xb

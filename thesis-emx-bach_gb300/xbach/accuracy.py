@@ -6,7 +6,7 @@ mixed path) or with the FP64 oracle.  The figures:
 * difference pixels in units of the per-pixel noise,
   sigma_pix = sqrt(|target| + |conv| + 2 sigma_rn^2) (gain 1; target is the
   image the convolved one is subtracted from), over pixels neither run set to
-  the 1e-30 border/bad value;
+  the 1e-30 border/bad value (in FP64 or FP32);
 * kernel coefficients sol[1 .. nComp+1] and background terms
   sol[nComp+2 .. nComp+1+nBG] (the solution layout of the reference's
   fitKernel, cdkscUtil.cpp:585-684), as max |delta| / max |reference|;
@@ -25,10 +25,19 @@ def layout(params):
     return (n_psf - 1) * n_c2, n_bg
 
 
+BAD_VALUES = (1e-30, float(np.float32(1e-30)))  # the bad-pixel value, FP64 and FP32
+
+
+def is_bad(img):
+    """Pixels holding the border / bad-output value 1e-30 (FP64 or FP32)."""
+    img = np.asarray(img, dtype=np.float64)
+    return (img == BAD_VALUES[0]) | (img == BAD_VALUES[1])
+
+
 def diff_error(diff, diff_ref, conv_ref, target, sigma_rn=SIGMA_RN):
     diff = np.asarray(diff, dtype=np.float64)
     diff_ref = np.asarray(diff_ref, dtype=np.float64)
-    ok = (diff != 1e-30) & (diff_ref != 1e-30)
+    ok = ~is_bad(diff) & ~is_bad(diff_ref)
     sigma = np.sqrt(np.abs(np.asarray(target, np.float64)) +
                     np.abs(np.asarray(conv_ref, np.float64)) + 2 * sigma_rn ** 2)
     e = np.abs(diff - diff_ref)[ok] / sigma[ok]
@@ -73,7 +82,7 @@ def residual_noise(runs, T, S, sigma_rn=SIGMA_RN):
     kernel removes.  runs: dicts with diff, conv, convTemplate."""
     ok = np.ones(np.shape(T), bool)
     for r in runs:
-        ok &= np.asarray(r["diff"]) != 1e-30
+        ok &= ~is_bad(r["diff"])
     out = []
     for r in runs:
         target = S if r["convTemplate"] else T
