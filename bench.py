@@ -128,14 +128,14 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_frames_per_s(T, S, info, runs):
+def cpu_frames_per_s(T, S, info, runs, threads=None):
     import build_native
     build_native.build_oracle()
     from xbach_testlib import Oracle
     o = Oracle()
     p = frame_params(o, info)
     T64, S64 = T.astype("float64"), S.astype("float64")
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     times = []
     last = None
     for _ in range(runs):
@@ -194,6 +194,40 @@ def roofline_for(name, ms_per_launch, n_pix, mode, hbm_peak):
     return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "traffic": traffic, "kernel": name,
             "algorithmic_bytes_per_launch": traffic_bytes, "ms_per_launch": ms_per_launch}
+
+
+def cuda_core_rooflines(kernels, params, n_pix, mode, fp32_peak, fp64_peak):
+    """The kernels bound by a CUDA-core pipe against that pipe's measured
+    FMA peak (xb_measure_fma_peaks in this run):
+    * conv_sub: 2 x 441 FLOP per pixel (one 21x21 kernel per pixel), FP32 in
+      mixed mode, FP64 in plain mode;
+    * global_ldl: the LDL^T of the n x n global system, n^3 / 3 FLOP per
+      launch (n = nComp + nBG + 1 = 292 here), FP64, one 16-CTA cluster: a
+      dependency chain of n pivots, latency-bound by design."""
+    from xbach.accuracy import layout
+    out = {"peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak,
+                            "source": "measured in this run (xb_measure_fma_peaks)"}}
+    fk = 2 * params.hKernelWidth + 1
+    if "conv_sub" in kernels:
+        k = kernels["conv_sub"]
+        ms = k["ms_total"] / k["launches"]
+        flop = 2.0 * fk * fk * n_pix
+        peak = fp32_peak if mode == "mixed" else fp64_peak
+        ach = flop / (ms * 1e-3) / 1e12
+        out["conv_sub"] = {"bound": "fp32" if mode == "mixed" else "fp64", "achieved": ach,
+                           "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                           "flop_per_launch": flop, "ms_per_launch": ms}
+    if "global_ldl" in kernels:
+        k = kernels["global_ldl"]
+        ms = k["ms_total"] / k["launches"]
+        n_comp, n_bg = layout(params)
+        n = n_comp + n_bg + 1
+        flop = n ** 3 / 3.0
+        ach = flop / (ms * 1e-3) / 1e12
+        out["global_ldl"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak,
+                             "unit": "TFLOP/s", "frac": ach / fp64_peak, "n": n,
+                             "flop_per_launch": flop, "ms_per_launch": ms}
+    return out
 
 
 def gram_tensor_roofline(kernels, ctx, bf16_peak_tflops, wcols=961, rows=64, kc=64):
@@ -485,7 +519,10 @@ def main():
     ap.add_argument("--batch", type=int, default=16,
                     help="frame pairs per step, run concurrently (1 = one pair per step)")
     ap.add_argument("--workers", type=int, default=16, help="concurrent frames of a batch")
-    ap.add_argument("--cpu-runs", type=int, default=2)
+    ap.add_argument("--cpu-runs", type=int, default=6,
+                    help="CPU baseline: oracle runs (median reported)")
+    ap.add_argument("--cpu-single", type=int, default=1,
+                    help="CPU baseline: also time one single-threaded oracle run")
     ap.add_argument("--config", type=int, default=2, choices=[2, 4],
                     help="2: the headline 2048^2 workload; 4: 64 pairs of mixed size")
     ap.add_argument("--pairs", type=int, default=64, help="--config 4: pairs per step")
@@ -698,6 +735,8 @@ def main():
         roof["peak_source"] = peak_src
     bf16_peak = measured_peaks()[1]
     roof_tc = gram_tensor_roofline(kernels, ctx, bf16_peak) if args.mode == "mixed" else None
+    fp32_peak, fp64_peak = xbach.measure_fma_peaks(local)
+    roof_pipe = cuda_core_rooflines(kernels, params, n_pix, args.mode, fp32_peak, fp64_peak)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -714,7 +753,7 @@ def main():
                    else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
-        "roofline_tensor": roof_tc,
+        "roofline_tensor": roof_tc, "roofline_cuda_cores": roof_pipe,
         "single_frame": {"value": single_value, "unit": UNIT,
                          "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single,
                          "path": "stages, host-driven (per-kernel timers on)"},
@@ -723,9 +762,16 @@ def main():
     }
     oracle_res = None
     if world == 1 and args.cpu_runs > 0:
-        fps, threads, _, oracle_res = cpu_frames_per_s(T, S, info, args.cpu_runs)
-        line["cpu_baseline"] = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{args.cpu_runs} full 2048x2048 frame pairs"}
+        _, threads, times, oracle_res = cpu_frames_per_s(T, S, info, args.cpu_runs)
+        med = statistics.median(times)
+        line["cpu_baseline"] = {"value": 1.0 / med, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"median of {args.cpu_runs} full 2048x2048 frame pairs "
+                                          f"(FP64 oracle, OpenMP over {threads} host threads)",
+                                "seconds_per_frame": times}
+        if args.cpu_single:
+            _, _, t1, _ = cpu_frames_per_s(T, S, info, 1, threads=1)
+            line["cpu_baseline"]["single_thread"] = {"value": 1.0 / t1[0], "unit": UNIT,
+                                                     "cores": 1, "seconds_per_frame": t1[0]}
     if args.mode == "mixed":
         # the plain FP64 GPU pipeline, one pair per step: the denominator of the
         # chosen-vs-plain ratio, and the acceptance reference

@@ -309,6 +309,11 @@ int xb_batch_set_params(xb_batch* b, int nFrames, const xb_params* params);
  * `stream` before and after a run bracket all of its GPU work.  NULL detaches. */
 int xb_batch_set_stream(xb_batch* b, void* stream);
 
+/* Measured FMA throughput of the device's CUDA cores, FP32 and FP64 (TFLOP/s,
+ * one FMA = 2 operations; best of three ~10-20 ms launches): the
+ * denominators of the roofline figures of kernels bound by those pipes. */
+int xb_measure_fma_peaks(int device, double* fp32Tflops, double* fp64Tflops);
+
 /* ---- streaming pipeline over FITS files ---------------------------------- */
 /* No counterpart in the reference, whose main (src/main.cpp:16-159) reads
  * two FITS files, runs the stages and writes conv and sub once per process.

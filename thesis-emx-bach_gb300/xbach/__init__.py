@@ -63,7 +63,7 @@ EXPORTS = [
     "xb_batch_worker", "xb_batch_set_stream", "xb_batch_set_params", "xb_ranker_param_count", "xb_ranker_set",
     "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
     "xb_pipeline_create", "xb_pipeline_destroy", "xb_pipeline_last_error", "xb_pipeline_worker",
-    "xb_pipeline_run_files", "xb_pipeline_stats_get",
+    "xb_pipeline_run_files", "xb_pipeline_stats_get", "xb_measure_fma_peaks",
 ]
 
 
@@ -141,6 +141,7 @@ def lib():
     L.xb_pipeline_run_files.argtypes = [vp, i, P(ctypes.c_char_p), P(ctypes.c_char_p),
                                         P(ctypes.c_char_p), P(ctypes.c_char_p), P(i), P(d)]
     L.xb_pipeline_stats_get.argtypes = [vp, P(PipelineStats)]
+    L.xb_measure_fma_peaks.argtypes = [i, P(d), P(d)]
     _lib = L
     return L
 
@@ -488,3 +489,12 @@ class Pipeline:
         if self.L.xb_pipeline_stats_get(self.h, ctypes.byref(out)):
             raise XbError(5, "xb_pipeline_stats_get failed")
         return {k: getattr(out, k) for k, _ in PipelineStats._fields_}
+
+
+def measure_fma_peaks(device=0):
+    """(FP32, FP64) CUDA-core FMA throughput of the device, TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib().xb_measure_fma_peaks(device, ctypes.byref(a), ctypes.byref(b))
+    if rc:
+        raise XbError(rc, "xb_measure_fma_peaks failed")
+    return a.value, b.value
