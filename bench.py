@@ -516,9 +516,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"],
                     help="mixed = the chosen pipeline (headline); plain = the FP64 path alone")
-    ap.add_argument("--batch", type=int, default=16,
+    ap.add_argument("--batch", type=int, default=24,
                     help="frame pairs per step, run concurrently (1 = one pair per step)")
-    ap.add_argument("--workers", type=int, default=16, help="concurrent frames of a batch")
+    ap.add_argument("--workers", type=int, default=24, help="concurrent frames of a batch")
     ap.add_argument("--cpu-runs", type=int, default=6,
                     help="CPU baseline: oracle runs (median reported)")
     ap.add_argument("--cpu-single", type=int, default=1,

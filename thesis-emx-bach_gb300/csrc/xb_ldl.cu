@@ -623,67 +623,75 @@ __device__ void ldlSolveCta(const double* __restrict__ F, const double* __restri
 
 }  // namespace
 
-// Refined solve on a cluster: rhs (n+1 entries, index 0 unused) is replaced by
-// the solution.  With status bit 0 set the pivoted LU solves the system
-// instead and this kernel returns at once.  Linv: global scratch for the
-// inverses of the diagonal blocks (ceil(n/32) x 32 x 32).
-template <int CL>
+// Inverses of the diagonal blocks of L, one CTA per block (Linv: global,
+// ceil(n/32) x 32 x 32).  With status bit 0 set the pivoted LU solves the
+// system instead and the kernel returns at once.
 __global__ void __launch_bounds__(SV_THREADS)
-    k_ldl_solve(const double* __restrict__ A, const double* __restrict__ F,
-                const double* __restrict__ rinv, int n, double* __restrict__ rhs,
-                const int* __restrict__ status, double* __restrict__ Linv) {
+    k_ldl_block_inv(const double* __restrict__ F, int n, const int* __restrict__ status,
+                    double* __restrict__ Linv) {
+  __shared__ double X[SV_NB * (SV_NB + 1)];
+  __shared__ double T[256];
+  if(status[0] & 1) return;
+  invertDiagBlock(F, n, blockIdx.x, X, T, Linv);
+}
+
+// One triangular-solve pass of the refined solve, on one CTA (the pivot
+// chain is sequential; no other SM waits on it).  first = 1: x1 = (L D L^T)^-1
+// rhs into x1g.  first = 0: x2 = (L D L^T)^-1 res and rhs <- x1g + x2.
+// With status bit 0 set the pivoted LU solves the system instead.
+__global__ void __launch_bounds__(SV_THREADS)
+    k_ldl_solve(const double* __restrict__ F, const double* __restrict__ rinv, int n,
+                double* __restrict__ rhs, const double* __restrict__ res,
+                double* __restrict__ x1g, const int* __restrict__ status,
+                const double* __restrict__ Linv, int first) {
   extern __shared__ __align__(16) double sv_s[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int)cluster.block_rank(), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ld = n + 1, LX = (n + 2) & ~1, nB = (n + SV_NB - 1) / SV_NB;
-  double* x = sv_s;                  // LX: solution, then correction (CTA 0)
-  double* b = x + LX;                // LX: right-hand side, then residual
-  double* x1 = b + LX;               // LX: first solution
-  double* part = x1 + LX;            // SV_AW x 32
-  double* Li = part + SV_AW * 32;    // nB x 32 x 32 (CTA 0); inversion scratch elsewhere
+  const int tid = threadIdx.x;
+  const int LX = (n + 2) & ~1, nB = (n + SV_NB - 1) / SV_NB;
+  double* x = sv_s;                  // LX
+  double* part = x + LX;             // SV_AW x 32
+  double* Li = part + SV_AW * 32;    // nB x 32 x 32
   if(status[0] & 1) return;  // the LU fallback solves this system
-  {
-    double* X = Li + (rank == 0 ? (size_t)nB * SV_NB * SV_NB : 0);
-    double* T = X + SV_NB * (SV_NB + 1);
-    for(int q = rank; q < nB; q += CL) invertDiagBlock(F, n, q, X, T, Linv);
+  for(int e = tid; e < nB * SV_NB * SV_NB; e += SV_THREADS) Li[e] = Linv[e];
+  const double* src = first ? rhs : res;
+  for(int i = tid; i < LX; i += SV_THREADS) x[i] = i >= 1 && i <= n ? src[i] : 0.0;
+  __syncthreads();
+  ldlSolveCta(F, rinv, n, Li, x, part);
+  if(first) {
+    for(int i = tid; i < LX; i += SV_THREADS) x1g[i] = x[i];
+  } else {
+    for(int i = 1 + tid; i <= n; i += SV_THREADS) rhs[i] = x1g[i] + x[i];
   }
-  cluster.sync();
-  if(rank == 0) {
-    for(int e = tid; e < nB * SV_NB * SV_NB; e += SV_THREADS) Li[e] = Linv[e];
-    for(int i = tid; i < LX; i += SV_THREADS) {
-      const double v = i >= 1 && i <= n ? rhs[i] : 0.0;
-      b[i] = v;
-      x[i] = v;
-    }
-    __syncthreads();
-    ldlSolveCta(F, rinv, n, Li, x, part);
-    for(int i = tid; i < LX; i += SV_THREADS) x1[i] = x[i];
-  }
-  cluster.sync();
-  // residual rows, spread over the cluster: b_i <- b_i - A_i . x1 (in CTA 0)
-  {
-    const double* x0 = cluster.map_shared_rank(x1, 0);
-    double* b0 = cluster.map_shared_rank(b, 0);
-    if(rank != 0)
-      for(int i = tid; i < LX; i += SV_THREADS) x[i] = x0[i];
-    __syncthreads();
-    const double* xs = rank == 0 ? x1 : x;
-    constexpr int NWv = SV_THREADS / 32;
-    for(int i = 1 + rank * NWv + warp; i <= n; i += CL * NWv) {
-      double a = 0.0;
-      for(int j = 1 + lane; j <= n; j += 32) a = fma(A[(size_t)i * ld + j], xs[j], a);
+}
+
+// Residual of the first pass, res_i = rhs_i - A_i . x1, one row per warp
+// (lane-strided FMA chain, loads issued ahead, xor-shuffle sum) over
+// ceil(n / 16) CTAs: FP64 runs at ~1.7 FMA per clock per SM on this part, so
+// the n^2 products are spread over SMs.
+__global__ void __launch_bounds__(SV_THREADS)
+    k_ldl_residual(const double* __restrict__ A, int n, const double* __restrict__ rhs,
+                   const double* __restrict__ x1g, const int* __restrict__ status,
+                   double* __restrict__ res) {
+  if(status[0] & 1) return;
+  constexpr int NW = SV_THREADS / 32, RU = 8;
+  const int lane = threadIdx.x & 31, ld = n + 1;
+  const int i = 1 + blockIdx.x * NW + (threadIdx.x >> 5);
+  if(i > n) return;
+  double a = 0.0;
+  for(int j0 = 1 + lane; j0 <= n; j0 += 32 * RU) {
+    double av[RU], xv[RU];
 #pragma unroll
-      for(int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if(lane == 0) b0[i] -= a;
+    for(int u = 0; u < RU; u++) {
+      const int j = j0 + 32 * u;
+      av[u] = j <= n ? A[(size_t)i * ld + j] : 0.0;
+      xv[u] = j <= n ? x1g[j] : 0.0;
     }
+#pragma unroll
+    for(int u = 0; u < RU; u++)
+      if(j0 + 32 * u <= n) a = fma(av[u], xv[u], a);
   }
-  cluster.sync();
-  if(rank == 0) {
-    for(int i = tid; i < LX; i += SV_THREADS) x[i] = i >= 1 && i <= n ? b[i] : 0.0;
-    __syncthreads();
-    ldlSolveCta(F, rinv, n, Li, x, part);
-    for(int i = 1 + tid; i <= n; i += SV_THREADS) rhs[i] = x1[i] + x[i];
-  }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if(lane == 0) res[i] = rhs[i] - a;
 }
 
 template __global__ void k_global_ldl<8>(const double*, double*, double*, int, int*);
@@ -694,10 +702,6 @@ template __global__ void k_global_ldl_panel<8, 2>(const double*, double*, double
 template __global__ void k_global_ldl_panel<8, 4>(const double*, double*, double*, int, int, int*);
 template __global__ void k_global_ldl_panel<8, 8>(const double*, double*, double*, int, int, int*);
 template __global__ void k_global_ldl<16>(const double*, double*, double*, int, int*);
-template __global__ void k_ldl_solve<8>(const double*, const double*, const double*, int, double*,
-                                        const int*, double*);
-template __global__ void k_ldl_solve<16>(const double*, const double*, const double*, int, double*,
-                                         const int*, double*);
 
 namespace {
 
@@ -820,15 +824,21 @@ void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, 
     KT_SCOPE(c, "global_solve");
     const int nB = (n + SV_NB - 1) / SV_NB;
     double* Linv = buf<double>(c, "ldl_linv", (size_t)nB * SV_NB * SV_NB);
-    const size_t smem = ((size_t)3 * ((n + 2) & ~1) + SV_AW * 32 + (size_t)nB * SV_NB * SV_NB +
-                         SV_NB * (SV_NB + 1) + 256) *
-                        sizeof(double);
-    if(clusterSize.load() == 16)
-      XB_CUDA(launchCluster(c, k_ldl_solve<16>, 16, SV_THREADS, smem, (const double*)M,
-                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status, Linv));
-    else
-      XB_CUDA(launchCluster(c, k_ldl_solve<8>, 8, SV_THREADS, smem, (const double*)M,
-                            (const double*)F, (const double*)rinv, n, rhs, (const int*)status, Linv));
+    const size_t smem =
+        ((size_t)((n + 2) & ~1) + SV_AW * 32 + (size_t)nB * SV_NB * SV_NB) * sizeof(double);
+    double* x1g = buf<double>(c, "ldl_x1", (size_t)n + 2);
+    double* res = buf<double>(c, "ldl_res", (size_t)n + 2);
+    k_ldl_block_inv<<<nB, SV_THREADS, 0, c->stream>>>((const double*)F, n, (const int*)status, Linv);
+    XB_LAUNCHED(c);
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_ldl_solve, c->device));
+    k_ldl_solve<<<1, SV_THREADS, smem, c->stream>>>((const double*)F, (const double*)rinv, n, rhs,
+                                                    res, x1g, (const int*)status, Linv, 1);
+    XB_LAUNCHED(c);
+    k_ldl_residual<<<(n + SV_THREADS / 32 - 1) / (SV_THREADS / 32), SV_THREADS, 0, c->stream>>>(
+        (const double*)M, n, rhs, x1g, (const int*)status, res);
+    XB_LAUNCHED(c);
+    k_ldl_solve<<<1, SV_THREADS, smem, c->stream>>>((const double*)F, (const double*)rinv, n, rhs,
+                                                    res, x1g, (const int*)status, Linv, 0);
     XB_LAUNCHED(c);
   }
 }
