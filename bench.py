@@ -536,6 +536,8 @@ def main():
                     help="> 0: stream this many 2048^2 FITS pairs per step through xb_pipeline "
                          "(FITS in and out) instead of the device-resident batch")
     ap.add_argument("--io", type=int, default=6, help="--files: reader and writer threads each")
+    ap.add_argument("--ldl-cluster", type=int, default=16, choices=[8, 16],
+                    help="batch workers: CTAs of the LDL^T cluster (identical factors)")
     args = ap.parse_args()
     use_graph = bool(args.graph) and args.mode == "mixed"
     use_rank = bool(args.rank) and args.mode == "mixed"
@@ -668,6 +670,8 @@ def main():
         dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
         for i in range(batch.n_workers):
             with_rank(batch.worker(i))
+        if args.mode == "mixed":
+            batch.set_option("ldl_cluster", args.ldl_cluster)
         if use_graph:
             # every worker captures its graph before the timed steps
             batch.set_option("graph", 1)
@@ -751,7 +755,8 @@ def main():
                    "frame_graphs": use_graph,
                    "learned_ranking": "policy 1, tau 0.5, xbach/ranker_preset5.npy" if use_rank
                    else None,
-                   "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
+                   "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+                   "ldl_cluster": args.ldl_cluster if args.mode == "mixed" else None},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
         "roofline_tensor": roof_tc, "roofline_cuda_cores": roof_pipe,
         "single_frame": {"value": single_value, "unit": UNIT,

@@ -1,6 +1,7 @@
 """The LDL^T variants (the column kernel and panels of 2, 4, 8 columns
-broadcast over the cluster) give the same factors bit for bit: every column
-receives the same updates in the same order with the same FMAs.  Checked
+broadcast over the cluster), on 16- or 8-CTA clusters, give the same factors
+bit for bit: every column receives the same updates in the same order with
+the same FMAs.  Checked
 through whole frames (the fit's solution and the difference image), each
 variant forced with option "tune_variant" (which also picks the conv's tile
 shape, whose variants are identical too)."""
@@ -18,10 +19,12 @@ def test_ldl_variants_agree(size, n_src, stamps):
     p = xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=stamps, stampsy=stamps,
                              threshHigh=info["threshHigh"])
     out = []
-    for variant in (0, 1, 2, 3, -1):
+    for variant in (0, 1, 2, 3, -1, -8):
         ctx = xbach.Context(p)
-        if variant < 0:
+        if variant == -1:
             ctx.set_option("ldl_panel", 0)
+        elif variant == -8:  # an 8-CTA cluster instead of 16
+            ctx.set_option("ldl_cluster", 8)
         else:
             ctx.set_option("tune_variant", variant)
         ctx.run_all(T, S)

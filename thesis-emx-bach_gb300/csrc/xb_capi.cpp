@@ -233,6 +233,9 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->gramFp64 = value != 0;
   } else if(n == "ldl_panel") {
     c->ldlPanel = value != 0;
+  } else if(n == "ldl_cluster") {
+    if(value != 8 && value != 16) return XB_ERR_ARG;
+    c->ldlCluster = (int)value;
   } else if(n == "graph") {
     if(value != 0 && !mixedMode(c)) {
       c->lastError = "frame graphs are built for the mixed mode";

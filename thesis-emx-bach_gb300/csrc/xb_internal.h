@@ -167,6 +167,7 @@ struct xb_ctx {
   float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
   int mxTables = 0;        // the mixed build's monomial tables are on the device
   int ldlPanel = 1;        // option "ldl_panel": panel LDL^T kernel (0: the column kernel)
+  int ldlCluster = 16;     // option "ldl_cluster": CTAs of the LDL^T cluster (16, or 8)
   uint8_t* inputMask = nullptr;  // xb_set_input_mask (device, inputMaskW x inputMaskH) or none
   int inputMaskW = 0, inputMaskH = 0;
   // frame graphs (xb_graph.cu)

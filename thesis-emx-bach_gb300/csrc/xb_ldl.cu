@@ -801,21 +801,24 @@ void globalSolveMixed(xb_ctx* c, const double* M, int n, double* rhs, int* piv, 
                     : launchCluster(c, k_global_ldl_panel<8, 8>, 8, LDL_THREADS, sm, M, F, rinv, n,
                                     rg, status);
     };
-    // 16-CTA clusters where the device allows them, else 8
+    // 16-CTA clusters where the device allows them and the context asks for
+    // them, else 8
     auto launch = [&](int v) {
       cudaError_t e = cudaErrorUnknown;
-      if(clusterSize.load() != 8) {
+      if(clusterSize.load() != 8 && c->ldlCluster == 16) {
         e = launchVariant(v, 16);
         if(e == cudaSuccess) clusterSize = 16;
         else cudaGetLastError();
       }
       if(e != cudaSuccess) {
         XB_CUDA(launchVariant(v, 8));
-        clusterSize = 8;
+        if(c->ldlCluster == 16) clusterSize = 8;
       }
       XB_LAUNCHED(c);
     };
-    const int v = c->ldlPanel ? tunedVariant(c, "global_ldl", n, 4, launch) : 0;
+    const int v = c->ldlPanel ? tunedVariant(c, "global_ldl", (long long)n * 32 + c->ldlCluster, 4,
+                                             launch)
+                              : 0;
     KT_SCOPE(c, "global_ldl");
     launch(v);
   }
