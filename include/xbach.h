@@ -112,6 +112,10 @@ typedef struct xb_params {
   int convPerPixel;         /* 1: the spatially varying kernel is evaluated at
                              * every output pixel instead of once per
                              * fK x fK block (conv.cl, bach.cpp:339-350) */
+  int fitWeighted;          /* 1: every substamp pixel enters the normal
+                             * equations (Q, B and the background products)
+                             * with weight 1 / sigma^2 of the noise model
+                             * above; the reference's fit is unweighted */
 } xb_params;
 
 /* Fill `p` with the reference defaults (include/argsUtil.h:7-57). */

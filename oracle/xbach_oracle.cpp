@@ -90,6 +90,7 @@ struct StampSet {
   std::vector<double> sky, fwhm;
   std::vector<SubSt> subs;           // n * maxSS
   std::vector<double> W, Q, B;       // n * wRows*wCols, n * q^2, n * b
+  std::vector<double> omega;         // weighted fit: n * wCols pixel weights
 };
 
 double msSince(std::chrono::steady_clock::time_point t0) {
@@ -658,12 +659,31 @@ void fillStamp(xbo_handle& o, StampSet& S, int s, const std::vector<double>& I,
       }
       W[(size_t)(g.nPSF + b) * g.wCols + p] = a;
     }
+  // weighted fit (extension): weight 1 / sigma^2 of each substamp pixel, the
+  // chi^2 noise model of calcSigs; every product of the normal equations
+  // becomes a * (b * w_k) with b the later factor as written below
+  const bool wfit = o.p.fitWeighted != 0;
+  double* om = wfit ? &S.omega[(size_t)s * g.wCols] : nullptr;
+  if(wfit) {
+    const double invGain = o.p.gain > 0.0 ? 1.0 / o.p.gain : 1.0;
+    const double rn2x2 = 2.0 * o.p.readNoise * o.p.readNoise;
+    for(int p = 0; p < g.wCols; p++) {
+      double v = 0.0;
+      if(live) {
+        const size_t id = (size_t)(ssx + p % fSS - hSS) + (size_t)(ssy + p / fSS - hSS) * w;
+        const double var = (std::fabs(I[id]) + std::fabs(O[id])) * invGain + rn2x2;
+        v = var > 0.0 ? 1.0 / var : 0.0;
+      }
+      om[p] = v;
+    }
+  }
   for(int i = 0; i < g.qCount; i++)
     for(int j = 0; j < g.qCount; j++) {
       double q0 = 0.0;
       if(i > 0 && j > 0 && j <= i)
         for(int k = 0; k < fSS * fSS; k++)
-          q0 += W[(size_t)(i - 1) * g.wCols + k] * W[(size_t)(j - 1) * g.wCols + k];
+          q0 += wfit ? W[(size_t)(i - 1) * g.wCols + k] * (W[(size_t)(j - 1) * g.wCols + k] * om[k])
+                     : W[(size_t)(i - 1) * g.wCols + k] * W[(size_t)(j - 1) * g.wCols + k];
       Q[(size_t)i * g.qCount + j] = q0;
     }
   for(int i = 0; i < g.bCount; i++) {
@@ -672,8 +692,8 @@ void fillStamp(xbo_handle& o, StampSet& S, int s, const std::vector<double>& I,
       for(int x = -hSS; x <= hSS; x++)
         for(int y = -hSS; y <= hSS; y++) {
           int k = x + hSS + fSS * (y + hSS);
-          p0 += W[(size_t)(i - 1) * g.wCols + k] *
-                O[(size_t)(x + ssx) + (size_t)(y + ssy) * w];
+          const double ov = O[(size_t)(x + ssx) + (size_t)(y + ssy) * w];
+          p0 += W[(size_t)(i - 1) * g.wCols + k] * (wfit ? ov * om[k] : ov);
         }
     B[i] = p0;
   }
@@ -788,23 +808,20 @@ void createMatrix(const xbo_handle& o, const StampSet& S, const std::vector<int>
     int s = ids[t];
     live[t] = S.cur[s] < S.count[s];
     const double* W = &S.W[(size_t)s * g.wRows * g.wCols];
+    const double* om = S.omega.empty() ? nullptr : &S.omega[(size_t)s * g.wCols];
+    // a * b, or a * (b * w_k) in the weighted fit
+    auto dot = [&](const double* a, const double* b) {
+      double p = 0.0;
+      for(int k = 0; k < pix; k++) p += om ? a[k] * (b[k] * om[k]) : a[k] * b[k];
+      return p;
+    };
     for(int ib = 0; ib < g.nBG; ib++) {
       const double* wb = W + (size_t)(g.nComp1 + ib + 1) * g.wCols;
-      for(int i1 = 1; i1 <= g.nComp1; i1++) {
-        const double* wi = W + (size_t)i1 * g.wCols;
-        double p = 0.0;
-        for(int k = 0; k < pix; k++) p += wi[k] * wb[k];
-        pKB[((size_t)t * g.nComp1 + (i1 - 1)) * g.nBG + ib] = p;
-      }
-      double p = 0.0;
-      for(int k = 0; k < pix; k++) p += W[k] * wb[k];
-      p0B[(size_t)t * g.nBG + ib] = p;
-      for(int jb = 0; jb <= ib; jb++) {
-        const double* wj = W + (size_t)(g.nComp1 + jb + 1) * g.wCols;
-        double q = 0.0;
-        for(int k = 0; k < pix; k++) q += wb[k] * wj[k];
-        pBB[((size_t)t * g.nBG + ib) * g.nBG + jb] = q;
-      }
+      for(int i1 = 1; i1 <= g.nComp1; i1++)
+        pKB[((size_t)t * g.nComp1 + (i1 - 1)) * g.nBG + ib] = dot(W + (size_t)i1 * g.wCols, wb);
+      p0B[(size_t)t * g.nBG + ib] = dot(W, wb);
+      for(int jb = 0; jb <= ib; jb++)
+        pBB[((size_t)t * g.nBG + ib) * g.nBG + jb] = dot(wb, W + (size_t)(g.nComp1 + jb + 1) * g.wCols);
     }
   }
   // entries of the lower triangle (row >= col >= 1), each summed over stamps
@@ -862,6 +879,7 @@ void createScProd(const xbo_handle& o, const StampSet& S, const std::vector<int>
     if(S.cur[s] >= S.count[s]) continue;
     const SubSt& ss = S.subs[(size_t)s * g.maxSS + S.cur[s]];
     const double* W = &S.W[(size_t)s * g.wRows * g.wCols];
+    const double* om = S.omega.empty() ? nullptr : &S.omega[(size_t)s * g.wCols];
     for(int b = 0; b < g.nBG; b++) {
       const double* wb = W + (size_t)(g.nComp1 + b + 1) * g.wCols;
       double q = 0.0;
@@ -869,14 +887,15 @@ void createScProd(const xbo_handle& o, const StampSet& S, const std::vector<int>
         for(int y = -hSS; y <= hSS; y++)
           for(int x = -hSS; x <= hSS; x++) {
             int index = x + hSS + fSS * (y + hSS);
-            q += wb[index] * img[(size_t)(x + ss.x) + (size_t)(y + ss.y) * w];
+            const double v = img[(size_t)(x + ss.x) + (size_t)(y + ss.y) * w];
+            q += wb[index] * (om ? v * om[index] : v);
           }
       } else {
         for(int x = -hSS; x <= hSS; x++)
           for(int y = -hSS; y <= hSS; y++) {
             int index = x + hSS + fSS * (y + hSS);
-            q += wb[index] *
-                 (double)(float)img[(size_t)(x + ss.x) + (size_t)(y + ss.y) * w];
+            const double v = (double)(float)img[(size_t)(x + ss.x) + (size_t)(y + ss.y) * w];
+            q += wb[index] * (om ? v * om[index] : v);
           }
       }
       bgP[(size_t)t * g.nBG + b] = q;
@@ -1522,6 +1541,7 @@ void allocW(xbo_handle& o, StampSet& S) {
   S.W.assign((size_t)S.n * g.wRows * g.wCols, 0.0);
   S.Q.assign((size_t)S.n * g.qCount * g.qCount, 0.0);
   S.B.assign((size_t)S.n * g.bCount, 0.0);
+  S.omega.assign(o.p.fitWeighted ? (size_t)S.n * g.wCols : 0, 0.0);
 }
 
 void snapshotSets(xbo_handle& o) {

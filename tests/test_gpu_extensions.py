@@ -1,5 +1,5 @@
 """HOTPANTS-style extensions on the GPU (xb_params gain / readNoise /
-convPerPixel) against the oracle's restatement.
+convPerPixel / fitWeighted) against the oracle's restatement.
 
 Plain mode: every decision, the stamp chi^2 and the solution bit-identical;
 the per-pixel convolution is an FMA chain in the oracle's order, so its
@@ -26,6 +26,7 @@ CASES = {
     "noise_model": dict(gain=1.7, readNoise=5.0),
     "per_pixel": dict(convPerPixel=1),
     "both": dict(gain=2.3, readNoise=3.0, convPerPixel=1),
+    "weighted_fit": dict(fitWeighted=1, readNoise=5.0),
 }
 
 
@@ -140,3 +141,40 @@ def test_mixed_per_pixel_graph_replays_stage_by_stage(field):
     g.run(T, S)
     assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False),
                           blk.image(xbach.XB_IMG_DIFF, f64=False))
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_weighted_fit_with_constant_weight_two_is_exact(field, mode):
+    """Unbounded gain, read noise 0.5: every fit weight is exactly 2, so the
+    weighted normal equations are exactly twice the unweighted ones and the
+    results are bit-identical (mixed mode compared with its CUDA-core FP64
+    Gram, the path a weighted fit takes)."""
+    import xbach
+    T, S, kw = field
+    md = xbach.XB_MODE_PLAIN if mode == "plain" else xbach.XB_MODE_MIXED
+    out = []
+    for wfit in (0, 1):
+        ctx = xbach.Context(xbach.default_params(mode=md, gain=1e300, readNoise=0.5,
+                                                 fitWeighted=wfit, **kw))
+        if mode == "mixed":
+            ctx.set_option("gram_fp64", 1)
+        ctx.run_all(T, S)
+        out.append((ctx.solution(), ctx.image(xbach.XB_IMG_DIFF), ctx.scalar("ksc_iterations")))
+    assert _same(out[0][0], out[1][0]) and _same(out[0][1], out[1][1]) and out[0][2] == out[1][2]
+
+
+def test_mixed_weighted_fit_within_1e3_sigma_of_plain(field):
+    import xbach
+    from xbach.accuracy import diff_error
+    T, S, kw = field
+    res = {}
+    for mode in (xbach.XB_MODE_PLAIN, xbach.XB_MODE_MIXED):
+        ctx = xbach.Context(xbach.default_params(mode=mode, fitWeighted=1, readNoise=5.0, **kw))
+        ctx.run_all(T, S)
+        res[mode] = (ctx.image(xbach.XB_IMG_DIFF), ctx.image(xbach.XB_IMG_CONV),
+                     ctx.scalar("convTemplate"))
+    d_p, c_p, ct = res[xbach.XB_MODE_PLAIN]
+    d_m, _, ct_m = res[xbach.XB_MODE_MIXED]
+    assert ct == ct_m
+    e = diff_error(d_m, d_p, c_p, S if ct == 1 else T)
+    assert e["pixels"] > 0.8 * T.size and e["max_sigma"] <= 1e-3, e

@@ -6,7 +6,10 @@ readNoise, convPerPixel), checked through properties the mathematics fixes:
   every decision, being scale-free (sigma clipping of the chi^2 set, the
   ratio of the two directions' merits), stays the same;
 * with a spatially constant kernel (kernel order 0) the per-pixel kernel is
-  the per-block kernel, so both convolutions agree to rounding."""
+  the per-block kernel, so both convolutions agree to rounding;
+* with an unbounded gain and read noise 0.5 every fit weight is exactly 2, so
+  the weighted normal equations are exactly twice the unweighted ones and
+  every decision, the solution and the images are bit-identical."""
 import numpy as np
 
 
@@ -70,3 +73,23 @@ def test_per_pixel_kernel_is_the_polynomial_kernel_at_each_pixel(oracle, test01,
         want = ((kern[::-1, ::-1] * win).sum() + bg) * scale
         assert abs(conv[y, x] - want) <= 1e-11 * np.abs(conv).max(), (x, y, conv[y, x], want)
     assert not np.array_equal(pp.array("conv", np.float64), test01_oracle.array("conv", np.float64))
+
+
+def test_weighted_fit_with_constant_weight_two_is_exact(oracle, test01):
+    kw = dict(gain=1e300, readNoise=0.5)
+    plain = _run(oracle, test01, **kw)
+    wfit = _run(oracle, test01, fitWeighted=1, **kw)
+    for k in ("solution", "ksc_sig_last", "conv", "diff"):
+        assert np.array_equal(wfit.array(k, np.float64), plain.array(k, np.float64)), k
+    for k in ("ksc_rejects", "cur"):
+        assert np.array_equal(wfit.array(k, np.int32), plain.array(k, np.int32)), k
+    assert np.array_equal(2.0 * plain.array("ksc_matrix0", np.float64),
+                          wfit.array("ksc_matrix0", np.float64))
+
+
+def test_weighted_fit_changes_the_solution(oracle, test01, test01_oracle):
+    """Poisson weights (gain 1, read noise 5): another solution of the same
+    system shape, with every stage completing."""
+    w = _run(oracle, test01, fitWeighted=1, readNoise=5.0)
+    a, b = w.array("solution", np.float64), test01_oracle.array("solution", np.float64)
+    assert a.shape == b.shape and np.all(np.isfinite(a)) and not np.array_equal(a, b)

@@ -43,6 +43,7 @@ class XbParams(ctypes.Structure):
         ("gain", ctypes.c_double),
         ("readNoise", ctypes.c_double),
         ("convPerPixel", ctypes.c_int),
+        ("fitWeighted", ctypes.c_int),
     ]
 
 

@@ -21,6 +21,8 @@
 //   -rn x               read noise (ADU per frame, default 0) of that model,
 //                       used by the stamp chi^2 and by -on
 //   -gain x             gain (e-/ADU, default 1) of that model
+//   -wfit               weight the fit's normal equations by 1 / sigma^2 of
+//                       that model (the reference's fit is unweighted)
 //   -pk                 evaluate the spatially varying kernel at every pixel
 //                       (default: once per kernel-sized block, as the
 //                       reference does)
@@ -127,6 +129,7 @@ void parse(int argc, const char** argv, Cli& c) {
   if(exists(argc, argv, "-rn")) c.readNoise = c.p.readNoise = std::atof(option(argc, argv, "-rn"));
   if(exists(argc, argv, "-gain")) c.p.gain = std::atof(option(argc, argv, "-gain"));
   c.p.convPerPixel = exists(argc, argv, "-pk") ? 1 : 0;
+  c.p.fitWeighted = exists(argc, argv, "-wfit") ? 1 : 0;
   c.p.verbose = c.verbose;
   if(exists(argc, argv, "-pairs")) {
     const char* f = option(argc, argv, "-pairs");

@@ -49,6 +49,7 @@ int validate(const xb_params& p, std::string& why) {
   if(!(p.readNoise >= 0.0) || !std::isfinite(p.readNoise) || !std::isfinite(p.gain))
     return why = "bad gain or read noise", XB_ERR_ARG;
   if(p.convPerPixel != 0 && p.convPerPixel != 1) return why = "convPerPixel is 0 or 1", XB_ERR_ARG;
+  if(p.fitWeighted != 0 && p.fitWeighted != 1) return why = "fitWeighted is 0 or 1", XB_ERR_ARG;
   return XB_OK;
 }
 

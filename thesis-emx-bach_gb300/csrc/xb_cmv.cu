@@ -131,10 +131,12 @@ __global__ void __launch_bounds__(FILL_THREADS)
 constexpr int GQ_KT = 32, GQ_E = 8;
 template <class T>
 __global__ void __launch_bounds__(FILL_THREADS)
-    k_gram_qb(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
+    k_gram_qb(const T* __restrict__ other, const T* __restrict__ conv, int w, int h,
+              const int* __restrict__ list,
               const int* __restrict__ count, const int* __restrict__ cur,
               const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int qCount,
-              const double* __restrict__ W, double* __restrict__ Q, double* __restrict__ B) {
+              const double* __restrict__ W, double* __restrict__ Q, double* __restrict__ B,
+              double invGain, double rn2x2, double* __restrict__ omega) {
   extern __shared__ double gq_s[];
   const int s = list[blockIdx.x], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS;
@@ -145,6 +147,23 @@ __global__ void __launch_bounds__(FILL_THREADS)
   double* Bs = B + (size_t)s * qCount;
   double* tile = gq_s;                      // R x (GQ_KT + 1)
   double* sub = gq_s + R * (GQ_KT + 1);     // fSS * fSS image values
+  double* om = sub + wCols;                 // fSS * fSS pixel weights (weighted fit)
+  const bool live = cur[s] < count[s];
+  if(omega) {
+    // weights of the current substamp's pixels (exhausted stamps: zero)
+    const int2 c = live ? ssxy[(size_t)s * maxSS + cur[s]] : make_int2(0, 0);
+    for(int i = tid; i < wCols; i += FILL_THREADS) {
+      double v = 0.0;
+      if(live) {
+        const int gx = min(max(i % fSS - hSS + c.x, 0), w - 1);
+        const int gy = min(max(i / fSS - hSS + c.y, 0), h - 1);
+        const size_t id = (size_t)gx + (size_t)gy * w;
+        v = fitWeight((double)conv[id], (double)other[id], invGain, rn2x2);
+      }
+      om[i] = v;
+      omega[(size_t)s * wCols + i] = v;
+    }
+  }
   int ei[GQ_E], ej[GQ_E];
   double acc[GQ_E];
 #pragma unroll
@@ -175,7 +194,11 @@ __global__ void __launch_bounds__(FILL_THREADS)
       const double* a = tile + ei[e] * (GQ_KT + 1);
       const double* b = tile + ej[e] * (GQ_KT + 1);
       double q = acc[e];
-      for(int kk = 0; kk < kt; kk++) q += a[kk] * b[kk];
+      if(omega) {
+        for(int kk = 0; kk < kt; kk++) q += a[kk] * (b[kk] * om[k0 + kk]);
+      } else {
+        for(int kk = 0; kk < kt; kk++) q += a[kk] * b[kk];
+      }
       acc[e] = q;
     }
     __syncthreads();
@@ -187,7 +210,6 @@ __global__ void __launch_bounds__(FILL_THREADS)
   for(int e = 0; e < GQ_E; e++)
     if(ei[e] >= 0) Qs[(size_t)(ei[e] + 1) * qCount + (ej[e] + 1)] = acc[e];
   // B: W[i-1] . other image, x outer / y inner (column-major)
-  const bool live = cur[s] < count[s];
   if(live) {
     const int2 c = ssxy[(size_t)s * maxSS + cur[s]];
     for(int i = tid; i < wCols; i += FILL_THREADS) {
@@ -204,7 +226,7 @@ __global__ void __launch_bounds__(FILL_THREADS)
       for(int x = 0; x < fSS; x++)
         for(int y = 0; y < fSS; y++) {
           int k = x + fSS * y;
-          p0 += wr[k] * sub[k];
+          p0 += omega ? wr[k] * (sub[k] * om[k]) : wr[k] * sub[k];
         }
     }
     Bs[i] = p0;
@@ -248,17 +270,19 @@ void fillStamps(xb_ctx* c, int si, const int* dList, int nList, int imgConv, con
                                                        g.hSS, c->w, c->h, g.wRows, W);
   XB_LAUNCHED(c);
   }
-  size_t smemGram = ((size_t)(g.qCount - 1) * (GQ_KT + 1) + (size_t)g.wCols) * sizeof(double);
+  size_t smemGram = ((size_t)(g.qCount - 1) * (GQ_KT + 1) + 2 * (size_t)g.wCols) * sizeof(double);
+  const double invGain = noiseInvGain(c->p), rn2x2 = noiseRn2x2(c->p);
+  double* omega = c->p.fitWeighted ? S.omega : nullptr;
   const int other = 1 - imgConv;
   { KT_SCOPE(c, "gram_qb");
   if(c->imgIsF64)
     k_gram_qb<double><<<nList, FILL_THREADS, smemGram, c->stream>>>(
-        (const double*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-        g.wRows, g.qCount, W, S.Q, S.B);
+        (const double*)c->img[other], (const double*)c->img[imgConv], c->w, c->h, dList, S.count,
+        S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, g.qCount, W, S.Q, S.B, invGain, rn2x2, omega);
   else
     k_gram_qb<float><<<nList, FILL_THREADS, smemGram, c->stream>>>(
-        (const float*)c->img[other], c->w, c->h, dList, S.count, S.cur, S.ssxy, g.maxSS, g.hSS,
-        g.wRows, g.qCount, W, S.Q, S.B);
+        (const float*)c->img[other], (const float*)c->img[imgConv], c->w, c->h, dList, S.count,
+        S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, g.qCount, W, S.Q, S.B, invGain, rn2x2, omega);
   XB_LAUNCHED(c);
   }
 }
@@ -279,6 +303,8 @@ void stageCmv(xb_ctx* c) {
       S.dots = buf<double>(c, "dots" + sfx, (size_t)std::max(S.n, 1) * mixedDotStride(g));
     } else {
       S.W = buf<double>(c, "W" + sfx, (size_t)std::max(S.n, 1) * g.wRows * g.wCols);
+      S.omega = c->p.fitWeighted ? buf<double>(c, "omega" + sfx, (size_t)std::max(S.n, 1) * g.wCols)
+                                 : nullptr;
     }
     S.Q = buf<double>(c, "Q" + sfx, (size_t)std::max(S.n, 1) * g.qCount * g.qCount);
     S.B = buf<double>(c, "B" + sfx, (size_t)std::max(S.n, 1) * g.bCount);

@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(DOT_THREADS)
     k_stamp_dots(const int* __restrict__ list, const int* __restrict__ count,
                  const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                  const double* __restrict__ W, int wRows, int hSS, int nPSF, int nBG,
-                 const T* __restrict__ O, int w, int h, double* __restrict__ dots, int stride) {
+                 const T* __restrict__ O, int w, int h, double* __restrict__ dots, int stride,
+                 const double* __restrict__ omega) {
   extern __shared__ double dot_s[];
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS, nC1 = nPSF - 1;
@@ -241,6 +242,9 @@ __global__ void __launch_bounds__(DOT_THREADS)
   const bool live = cur[s] < count[s];
   double* tile = dot_s;                       // wRows x (DOT_KT+1)
   double* sub = dot_s + wRows * (DOT_KT + 1); // wCols (image) values
+  double* om = sub + wCols;                   // wCols pixel weights (weighted fit)
+  if(omega)
+    for(int i = tid; i < wCols; i += DOT_THREADS) om[i] = omega[(size_t)s * wCols + i];
   // products: (rowA, rowB) pairs for this thread
   const int nKB = nC1 * nBG, nPairs = nKB + nBG + nBG * nBG;
   int ra = -1, rb = -1, oi = -1;
@@ -273,7 +277,11 @@ __global__ void __launch_bounds__(DOT_THREADS)
     if(ra >= 0) {
       const double* pa = tile + ra * (DOT_KT + 1);
       const double* pb = tile + rb * (DOT_KT + 1);
-      for(int kk = 0; kk < kt; kk++) acc += pa[kk] * pb[kk];
+      if(omega) {
+        for(int kk = 0; kk < kt; kk++) acc += pa[kk] * (pb[kk] * om[k0 + kk]);
+      } else {
+        for(int kk = 0; kk < kt; kk++) acc += pa[kk] * pb[kk];
+      }
     }
     __syncthreads();
   }
@@ -295,12 +303,12 @@ __global__ void __launch_bounds__(DOT_THREADS)
     double q = 0.0;
     if(live) {
       if(tid < nBG) {
-        for(int k = 0; k < wCols; k++) q += wb[k] * sub[k];
+        for(int k = 0; k < wCols; k++) q += omega ? wb[k] * (sub[k] * om[k]) : wb[k] * sub[k];
       } else {
         for(int x = 0; x < fSS; x++)
           for(int y = 0; y < fSS; y++) {
             int k = x + fSS * y;
-            q += wb[k] * (double)(float)sub[k];
+            q += omega ? wb[k] * ((double)(float)sub[k] * om[k]) : wb[k] * (double)(float)sub[k];
           }
       }
     }
@@ -894,16 +902,17 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, const int* list,
   }
   const double* dots = mixed ? S.dots : f.dots;  // mixed: filled per stamp by the Gram kernel
   if(nList > 0 && !mixed) {
-    const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + g.wCols) * sizeof(double);
+    const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + 2 * (size_t)g.wCols) * sizeof(double);
+    const double* omega = c->p.fitWeighted ? S.omega : nullptr;
     { KT_SCOPE(c, "stamp_dots");
     if(c->imgIsF64)
       k_stamp_dots<double><<<nList, DOT_THREADS, smem, c->stream>>>(
           list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
-          g.nBG, (const double*)c->img[other], c->w, c->h, f.dots, f.stride);
+          g.nBG, (const double*)c->img[other], c->w, c->h, f.dots, f.stride, omega);
     else
       k_stamp_dots<float><<<nList, DOT_THREADS, smem, c->stream>>>(
           list, S.count, S.cur, S.ssxy, g.maxSS, (const double*)S.W, g.wRows, g.hSS, g.nPSF,
-          g.nBG, (const float*)c->img[other], c->w, c->h, f.dots, f.stride);
+          g.nBG, (const float*)c->img[other], c->w, c->h, f.dots, f.stride, omega);
     XB_LAUNCHED(c);
     }
   }

@@ -265,6 +265,7 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
   put(p.gain);
   put(p.readNoise);
   put(p.convPerPixel);
+  put(p.fitWeighted);
   put(c->gramFp64);
   put(c->ldlPanel);
   put(c->ldlCluster);

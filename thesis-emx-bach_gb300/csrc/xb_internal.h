@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <functional>
 #include <map>
 #include <string>
@@ -77,6 +78,7 @@ struct StampSetDev {
   double* B = nullptr;       // n * bCount
   float* Wf = nullptr;       // mixed mode: FP32 W [n][wRows][ld], ld = wCols padded to 32
   double* dots = nullptr;    // mixed mode: per-stamp dot table of the global matrix
+  double* omega = nullptr;   // plain mode, weighted fit: n * wCols pixel weights 1 / sigma^2
   const int* dN = nullptr;   // frame graphs: the kept count on the device (n is its bound)
 };
 
@@ -337,6 +339,12 @@ inline bool mixedMode(const xb_ctx* c) { return c->p.mode == XB_MODE_MIXED; }
 // which is |a| + |b| exactly for the defaults (gain 1, no read noise).
 inline double noiseInvGain(const xb_params& p) { return p.gain > 0.0 ? 1.0 / p.gain : 1.0; }
 inline double noiseRn2x2(const xb_params& p) { return 2.0 * p.readNoise * p.readNoise; }
+// Weight of a substamp pixel in the weighted fit: 1 / sigma^2 of the noise
+// model (0 where the model's variance is not positive).
+__host__ __device__ inline double fitWeight(double a, double b, double invGain, double rn2x2) {
+  const double v = (fabs(a) + fabs(b)) * invGain + rn2x2;
+  return v > 0.0 ? 1.0 / v : 0.0;
+}
 
 // ---- frame graphs (xb_graph.cu) -------------------------------------------
 // Capture helpers for stage code running under c->capturing: a conditional

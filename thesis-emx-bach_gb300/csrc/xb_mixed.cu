@@ -154,11 +154,14 @@ __global__ void __launch_bounds__(MX_THREADS)
 constexpr int GM_KT = 32, GM_SPLIT = 6;
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
-    k_gram_mixed(const T* __restrict__ other, int w, int h, const int* __restrict__ list,
+    k_gram_mixed(const T* __restrict__ other, const T* __restrict__ conv, int w, int h,
+                 const int* __restrict__ list,
                  const int* __restrict__ liveN, const int* __restrict__ count, const int* __restrict__ cur,
                  const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int ldW,
-                 const float* __restrict__ W, double* __restrict__ Gout) {
+                 const float* __restrict__ W, double* __restrict__ Gout, int weighted,
+                 double invGain, double rn2x2) {
   extern __shared__ double gm_s[];
+  __shared__ double omT[GM_KT];  // pixel weights of the tile (weighted fit)
   if(liveN && (int)blockIdx.x >= *liveN) return;
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS, R = wRows + 1;
@@ -196,11 +199,26 @@ __global__ void __launch_bounds__(MX_THREADS)
       }
       tile[r * (GM_KT + 1) + kk] = (double)v;
     }
+    if(weighted && tid < GM_KT) {
+      double v = 0.0;
+      if(tid < kt && live) {
+        const int k = k0 + tid;
+        const int gx = min(max(c.x - hSS + k % fSS, 0), w - 1);
+        const int gy = min(max(c.y - hSS + k / fSS, 0), h - 1);
+        const size_t id = (size_t)gx + (size_t)gy * w;
+        v = fitWeight((double)conv[id], (double)other[id], invGain, rn2x2);
+      }
+      omT[tid] = v;
+    }
     __syncthreads();
     if(ei >= 0) {
       const double* a = tile + ei * (GM_KT + 1);
       const double* b = tile + ej * (GM_KT + 1);
-      for(int kk = 0; kk < kt; kk++) acc = fma(a[kk], b[kk], acc);
+      if(weighted) {
+        for(int kk = 0; kk < kt; kk++) acc = fma(a[kk], b[kk] * omT[kk], acc);
+      } else {
+        for(int kk = 0; kk < kt; kk++) acc = fma(a[kk], b[kk], acc);
+      }
     }
     __syncthreads();
   }
@@ -1217,16 +1235,18 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     const int split = std::max(GM_SPLIT, (R * (R + 1) / 2 + MX_THREADS - 1) / MX_THREADS);
     double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
     dim3 grid(nList, split);
-    if(gramTensorCores(c, si, dList, nList, other, G, liveN)) {
+    if(!c->p.fitWeighted && gramTensorCores(c, si, dList, nList, other, G, liveN)) {
       // exact tensor-core Gram (xb_gram_tc.cu)
     } else if(c->imgIsF64)
       k_gram_mixed<double><<<grid, MX_THREADS, smem, c->stream>>>(
-          (const double*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
-          g.hSS, g.wRows, ldW, S.Wf, G);
+          (const double*)c->img[other], (const double*)c->img[imgConv], c->w, c->h, dList, liveN,
+          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, G, c->p.fitWeighted,
+          noiseInvGain(c->p), noiseRn2x2(c->p));
     else
       k_gram_mixed<float><<<grid, MX_THREADS, smem, c->stream>>>(
-          (const float*)c->img[other], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy, g.maxSS,
-          g.hSS, g.wRows, ldW, S.Wf, G);
+          (const float*)c->img[other], (const float*)c->img[imgConv], c->w, c->h, dList, liveN,
+          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, G, c->p.fitWeighted,
+          noiseInvGain(c->p), noiseRn2x2(c->p));
     XB_LAUNCHED(c);
     k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, liveN, S.count, S.cur, g.wRows,
                                                         g.nPSF, g.nBG, g.qCount, G, S.Q, S.B,

@@ -40,6 +40,7 @@ class XbParams(ctypes.Structure):
         ("dg", ctypes.c_int * XB_MAX_GAUSS), ("bg", ctypes.c_float * XB_MAX_GAUSS),
         ("mode", ctypes.c_int), ("verbose", ctypes.c_int),
         ("gain", ctypes.c_double), ("readNoise", ctypes.c_double), ("convPerPixel", ctypes.c_int),
+        ("fitWeighted", ctypes.c_int),
     ]
 
 
