@@ -528,20 +528,79 @@ __global__ void __launch_bounds__(256)
   if(rank == 0 && tid == 0) idxOut[0] = 0;
 }
 
-__global__ void k_global_lubksb(const double* __restrict__ M, int n, const int* __restrict__ idx,
-                                double* __restrict__ b) {
+// lubksb of the global system (bachUtil.cpp:380-411) on two warps: lane 0 of
+// warp 0 runs each row's sequential chain `sum -= a[i][j] * b[j]` (the
+// reference's order and roundings), while warp 1 forms the next row's
+// products a[i'][j] * b[j] for the b[j] already final; lane 0 forms the one
+// product that needs the row it just finished, from a value it loaded before
+// its chain.  One 64-thread barrier per row.
+constexpr int LUB_THREADS = 64;
+__global__ void __launch_bounds__(LUB_THREADS)
+    k_global_lubksb(const double* __restrict__ M, int n, const int* __restrict__ idx,
+                    double* __restrict__ b) {
   extern __shared__ double sol_s[];
-  double* bs = sol_s;         // n + 1
-  double* prod = bs + n + 1;  // n + 1
-  int* is = (int*)(prod + n + 1);
-  for(int i = threadIdx.x; i <= n; i += blockDim.x) {
+  double* bs = sol_s;          // n + 1
+  double* pA = bs + n + 1;     // n + 1: products of the current row
+  double* pB = pA + n + 1;     // n + 1: products of the next row
+  int* is = (int*)(pB + n + 1);
+  __shared__ int iiS[2];  // ii for row i in slot i & 1 (written one row ahead)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, ld = n + 1;
+  for(int i = tid; i <= n; i += LUB_THREADS) {
     bs[i] = b[i];
     is[i] = idx[i];
   }
+  if(tid == 0) iiS[0] = iiS[1] = 0;
   __syncthreads();
-  if(threadIdx.x < 32) warpLubksb(M, n + 1, n, is, bs, prod);
-  __syncthreads();
-  for(int i = threadIdx.x; i <= n; i += blockDim.x) b[i] = bs[i];
+  double* cur = pA;
+  double* nxt = pB;
+  // forward: L y = P b
+  for(int i = 1; i <= n; i++) {
+    const int ii0 = iiS[i & 1];
+    if(tid == 0) {
+      const double aNext = i < n ? M[(size_t)(i + 1) * ld + i] : 0.0;
+      const int ip = is[i];
+      double sum = bs[ip];
+      bs[ip] = bs[i];
+      int ii = ii0;
+      if(ii0 != 0) {
+#pragma unroll 8
+        for(int j = ii0; j < i; j++) sum -= cur[j];
+      } else if(sum != 0.0) {
+        ii = i;
+      }
+      iiS[(i + 1) & 1] = ii;
+      bs[i] = sum;
+      if(i < n && ii != 0) nxt[i] = aNext * sum;
+    } else if(warp == 1 && ii0 != 0 && i < n) {
+      for(int j = ii0 + lane; j < i; j += 32) nxt[j] = M[(size_t)(i + 1) * ld + j] * bs[j];
+    }
+    __syncthreads();
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  // backward: U x = y (row n has no products)
+  for(int i = n; i >= 1; i--) {
+    if(tid == 0) {
+      const double aii = M[(size_t)i * ld + i];
+      const double aPrev = i > 1 ? M[(size_t)(i - 1) * ld + i] : 0.0;
+      double sum = bs[i];
+      if(i < n) {
+#pragma unroll 8
+        for(int j = i + 1; j <= n; j++) sum -= cur[j];
+      }
+      const double xi = sum / aii;
+      bs[i] = xi;
+      if(i > 1) nxt[i] = aPrev * xi;
+    } else if(warp == 1 && i > 1) {
+      for(int j = i + 1 + lane; j <= n; j += 32) nxt[j] = M[(size_t)(i - 1) * ld + j] * bs[j];
+    }
+    __syncthreads();
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  for(int i = tid; i <= n; i += LUB_THREADS) b[i] = bs[i];
 }
 
 // ----------------------------------------------------- kernel sums --------
@@ -977,9 +1036,9 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, const int* list,
   XB_CUDA(cudaLaunchKernelEx(&cfg, luKernel, f.M, n, f.piv, f.singular));
   XB_LAUNCHED(c);
   }
-  const size_t smemS = (size_t)(2 * (n + 1)) * sizeof(double) + (size_t)(n + 1) * sizeof(int);
+  const size_t smemS = (size_t)(3 * (n + 1)) * sizeof(double) + (size_t)(n + 1) * sizeof(int);
   { KT_SCOPE(c, "global_lubksb");
-  k_global_lubksb<<<1, 256, smemS, c->stream>>>(f.M, n, f.piv, dSol);
+  k_global_lubksb<<<1, LUB_THREADS, smemS, c->stream>>>(f.M, n, f.piv, dSol);
   XB_LAUNCHED(c);
   }
 }
