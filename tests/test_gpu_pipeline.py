@@ -114,3 +114,31 @@ def test_pipeline_many_pairs_few_slots(tmp_path):
     assert st == [0] * len(order)
     for j, i in enumerate(order):
         assert np.array_equal(read_fits(diffs[j]), refs[i].astype(np.float64)), j
+
+
+def test_pipeline_pairs_of_two_sizes(tmp_path):
+    """Frames of 512^2 and 256^2 interleaved in one run: slots grow and are
+    reused across sizes, each worker keeps a graph per shape, and every file
+    holds the single-context result."""
+    import xbach
+    from xbach.synth import make_pair
+    frames = []
+    for f in range(4):
+        T, S, info = make_pair(1, frame=f, size=512 if f % 2 == 0 else 256)
+        tp, sp = tmp_path / f"t{f}.fits", tmp_path / f"s{f}.fits"
+        write_fits(tp, T)
+        write_fits(sp, S)
+        frames.append((tp, sp, T, S))
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=6, stampsy=6,
+                                  threshHigh=info["threshHigh"])
+    refs = [_single(params, T, S)[1] for _, _, T, S in frames]
+    order = [0, 1, 2, 3, 1, 0, 3, 2]
+    diffs = [tmp_path / f"o{j}.fits" for j in range(len(order))]
+    pl = xbach.Pipeline(params, workers=2, io=2)
+    pl.set_option("graph", 1)
+    for rep in range(2):
+        st, _ = pl.run_files([frames[i][0] for i in order], [frames[i][1] for i in order], None,
+                             diffs)
+        assert st == [0] * len(order)
+        for j, i in enumerate(order):
+            assert np.array_equal(read_fits(diffs[j]), refs[i].astype(np.float64)), (rep, j)
