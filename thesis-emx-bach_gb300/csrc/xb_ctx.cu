@@ -8,6 +8,10 @@
 #include <cmath>
 #include <cstring>
 
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "xb_internal.h"
 
 namespace xb {
@@ -122,14 +126,26 @@ Basis buildBasis(const xb_params& p, const Geo& g) {
 }
 
 cudaError_t allowMaxDynamicSmem(const void* func, int device) {
+  // once per (function, device): the attribute outlives the call
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  {
+    std::lock_guard<std::mutex> l(mu);
+    if(done.count({func, device})) return cudaSuccess;
+  }
   int optin = 0;
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if(e != cudaSuccess) return e;
   cudaFuncAttributes fa;
   e = cudaFuncGetAttributes(&fa, func);
   if(e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              optin - (int)fa.sharedSizeBytes);
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes);
+  if(e == cudaSuccess) {
+    std::lock_guard<std::mutex> l(mu);
+    done.insert({func, device});
+  }
+  return e;
 }
 
 void* poolGet(xb_ctx* c, const char* name, size_t bytes) {
