@@ -230,3 +230,38 @@ def test_cli_pairs_reports_a_failing_pair(tmp_path):
     assert r.returncode == 1
     assert "pair 1 (" in r.stdout and "status 8" in r.stdout, r.stdout
     assert (tmp_path / "0_sub.fits").exists() and not (tmp_path / "1_sub.fits").exists()
+
+
+def test_measured_fma_peaks_are_plausible():
+    """xb_measure_fma_peaks: positive, finite, FP32 well above FP64 (the
+    roofline denominators of the CUDA-core-bound kernels)."""
+    import math
+    import xbach
+    fp32, fp64 = xbach.measure_fma_peaks(0)
+    assert math.isfinite(fp32) and math.isfinite(fp64) and fp64 > 0
+    assert fp32 > 4 * fp64
+
+
+def test_cli_pairs_with_input_mask(tmp_path):
+    """-pairs with -im: every pair of the stream excludes the masked pixels
+    (their difference is the bad-output value)."""
+    import shutil
+    import build_native
+    import xbach
+    for f in ("test0.fits", "test1.fits"):
+        shutil.copy(GOLDEN / f, tmp_path / f)
+    T = read_fits(GOLDEN / "test1.fits")
+    h, w = T.shape
+    m = np.zeros((h, w))
+    m[60:70, 200:230] = 1.0
+    L = xbach.lib()
+    assert L.xb_fits_write(str(tmp_path / "inmask.fits").encode(), m.ctypes.data, w, h) == 0
+    (tmp_path / "list.txt").write_text("test1.fits test0.fits p_\ntest0.fits test1.fits q_\n")
+    r = subprocess.run([str(build_native.CLI_BIN), "-pairs", str(tmp_path / "list.txt"),
+                        "-ip", str(tmp_path), "-op", str(tmp_path) + "/", "-im", "inmask.fits",
+                        "-pw", "2", "-pio", "1"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for prefix in ("p_", "q_"):
+        sub = read_fits(tmp_path / f"{prefix}sub.fits")
+        assert np.all(sub[60:70, 200:230] == np.float32(1e-30)), prefix
+        assert np.mean(sub == np.float32(1e-30)) < 0.5
