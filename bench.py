@@ -16,12 +16,22 @@ before every step, max over ranks.  e2e: the same through xb_run() with the
 host->device copy of both FP32 inputs from pinned memory and the
 device->host read of the conv and diff images inside the timed region.
 
-The headline runs 16 frame pairs per step on 16 worker contexts, each frame
-replayed as one captured CUDA graph (--graph 1), with the learned substamp
-order (--rank 1: policy 1 with the shipped weights, xbach/ranker_preset5.npy).  The process asks for 32
-hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS, set before CUDA starts):
-with the default 8, the workers' streams share queues and their graphs
-serialise.
+The headline runs 24 frame pairs per step on 24 worker contexts (--batch,
+--workers), each frame replayed as one captured CUDA graph (--graph 1), with
+the learned substamp order (--rank 1: policy 1 with the shipped weights,
+xbach/ranker_preset5.npy).  The process asks for 32 hardware work queues
+(CUDA_DEVICE_MAX_CONNECTIONS, set before CUDA starts): with the default 8,
+the workers' streams share queues and their graphs serialise.
+
+roofline: the conv kernel's HBM view (the contract's field); roofline_tensor:
+the exact-slice Gram on the tensor pipe; roofline_cuda_cores: the conv
+against the FP32 FMA peak and the global LDL^T against the FP64 FMA peak,
+both measured in the same run (xb_measure_fma_peaks).  cpu_baseline: the
+median of --cpu-runs FP64 oracle runs on all host threads, and one
+single-threaded run.
+
+--config 4: 64 pairs of mixed sizes per step (preset 4).  --files N: N
+2048^2 pairs per step streamed as FITS files through xb_pipeline.
 
 N > 1 (torchrun): replicas - every rank runs its own frame pairs on its own
 GPU; the only cross-rank traffic is the barrier and the max of the timings.
