@@ -73,6 +73,28 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+# ---- replicas (N > 1): every rank runs its own pairs; no data-path traffic ----
+def rank_frames(rank, batch):
+    """Seeds (frame indices) of the pairs one rank runs: disjoint across ranks."""
+    return [rank * batch + i for i in range(batch)]
+
+
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time (the job's time), via one all-reduce."""
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, pairs_per_rank, steps, ms):
+    """Whole-job throughput: every rank's pairs over the slowest rank's time."""
+    return world * pairs_per_rank * steps / (ms / 1000.0)
+
+
 def measured_peaks():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -582,7 +604,7 @@ def main():
         return cx
 
     B = max(1, args.batch)
-    frames = [make_pair(2, frame=rank * B + i) for i in range(B)]
+    frames = [make_pair(2, frame=f) for f in rank_frames(rank, B)]
     T, S, info = frames[0]
     h, w = T.shape
     n_pix = w * h
@@ -620,12 +642,8 @@ def main():
         torch.cuda.synchronize()
         return ms
 
-    def max_over_ranks(ms):
-        if world == 1:
-            return ms
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_ranks(ms):
+        return max_over_ranks(ms, world, "cuda")
 
     # ---- one frame pair per step: per-kernel breakdown ----
     ctx = with_rank(xbach.Context(params, device=local))
@@ -636,7 +654,7 @@ def main():
     torch.cuda.synchronize()
     ctx.set_option("time_kernels", 1)
     launches_single0 = ctx.launches()
-    single_ms = max_over_ranks(timed(single, cst, args.steps))
+    single_ms = max_ranks(timed(single, cst, args.steps))
     launches_single = ctx.launches() - launches_single0
     kernels = {}
     for name in ("mask_input", "spread_mask", "stamp_stats", "find_substamps", "compact_stamps",
@@ -665,7 +683,7 @@ def main():
             single_g()
         torch.cuda.synchronize()
         gl0 = gctx.launches()
-        g_ms = max_over_ranks(timed(single_g, torch.cuda.ExternalStream(gctx.stream()),
+        g_ms = max_ranks(timed(single_g, torch.cuda.ExternalStream(gctx.stream()),
                                     args.steps))
         single_graph = {"value": world * args.steps / (g_ms / 1000.0), "unit": UNIT,
                         "ms_per_step": g_ms / args.steps,
@@ -701,15 +719,15 @@ def main():
         workers = [batch.worker(i) for i in range(batch.n_workers)]
         l0 = sum(wk.launches() for wk in workers)
         with ClockSampler(local) as clk:
-            t_max = max_over_ranks(timed(run_batch, jst, args.steps))
+            t_max = max_ranks(timed(run_batch, jst, args.steps))
         launches = sum(wk.launches() for wk in workers) - l0
         clocks = clk.summary()
     else:
         with ClockSampler(local) as clk:
-            t_max = max_over_ranks(timed(single, cst, args.steps))
+            t_max = max_ranks(timed(single, cst, args.steps))
         launches = launches_single
         clocks = clk.summary()
-    value = world * B * args.steps / (t_max / 1000.0)
+    value = job_value(world, B, args.steps, t_max)
 
     # ---- end to end: host frames (pinned) in, host images out ----
     hT = [torch.from_numpy(f[0]).pin_memory() for f in frames]
@@ -731,7 +749,7 @@ def main():
                 raise RuntimeError(L.xb_last_error(ctx.h).decode())
         est = cst
     run_e2e()
-    e2e_ms = max_over_ranks(timed(run_e2e, est, args.steps))
+    e2e_ms = max_ranks(timed(run_e2e, est, args.steps))
     e2e = {"value": world * B * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
            "h2d_bytes_per_step": B * 2 * 4 * n_pix, "d2h_bytes_per_step": B * 2 * 4 * n_pix}
 
