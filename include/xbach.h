@@ -352,6 +352,11 @@ int xb_pipeline_worker(xb_pipeline* pl, int i, xb_ctx** ctx);
 int xb_pipeline_run_files(xb_pipeline* pl, int nPairs, const char* const* templatePath,
                           const char* const* sciencePath, const char* const* convPath,
                           const char* const* diffPath, int* pairStatus, double* kernSum);
+/* Parameters per pair for later runs: params[i] applies to pair i (stamp
+ * grid, thresholds, clipping, noise model); every set must keep the
+ * pipeline's basis, widths, orders and mode (XB_ERR_ARG otherwise).
+ * nPairs = 0 returns to the pipeline's parameters. */
+int xb_pipeline_set_params(xb_pipeline* pl, int nPairs, const xb_params* params);
 /* Timings and byte counts of the last run. */
 int xb_pipeline_stats_get(const xb_pipeline* pl, xb_pipeline_stats* out);
 

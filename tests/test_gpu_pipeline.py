@@ -142,3 +142,33 @@ def test_pipeline_pairs_of_two_sizes(tmp_path):
         assert st == [0] * len(order)
         for j, i in enumerate(order):
             assert np.array_equal(read_fits(diffs[j]), refs[i].astype(np.float64)), (rep, j)
+
+
+def test_pipeline_per_pair_parameters(tmp_path):
+    """xb_pipeline_set_params: each pair runs with its own stamp grid and
+    noise model (graphs captured per parameter set); a set that changes the
+    basis is refused."""
+    import xbach
+    pr = _pairs(tmp_path, 3)
+    info = pr[0][4]
+    base = _params("mixed", info)
+    per = [xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=g, stampsy=g, readNoise=rn,
+                                threshHigh=info["threshHigh"])
+           for g, rn in ((8, 0.0), (12, 5.0), (10, 2.0))]
+    refs = [_single(p, T, S)[1] for p, (_, _, T, S, _) in zip(per, pr)]
+    pl = xbach.Pipeline(base, workers=2, io=1)
+    pl.set_option("graph", 1)
+    pl.set_params(per)
+    diffs = [tmp_path / f"pp{i}.fits" for i in range(3)]
+    for _ in range(2):
+        st, _ = pl.run_files([p[0] for p in pr], [p[1] for p in pr], None, diffs)
+        assert st == [0, 0, 0]
+        for i in range(3):
+            assert np.array_equal(read_fits(diffs[i]), refs[i].astype(np.float64)), i
+    bad = xbach.default_params(mode=xbach.XB_MODE_MIXED, kernelOrder=1)
+    with pytest.raises(xbach.XbError):
+        pl.set_params([bad])
+    pl.set_params([])
+    st, _ = pl.run_files([pr[0][0]], [pr[0][1]], None, diffs[:1])
+    assert st == [0]
+    assert np.array_equal(read_fits(diffs[0]), _single(base, pr[0][2], pr[0][3])[1].astype(np.float64))

@@ -113,6 +113,8 @@ struct xb_pipeline {
   std::vector<Slot> slots;
   std::string lastError;
   xb_pipeline_stats stats{};
+  xb_params base{};                    // the pipeline's parameters
+  std::vector<xb_params> pairParams;   // per pair (xb_pipeline_set_params), or empty
 };
 
 namespace {
@@ -186,6 +188,7 @@ int xb_pipeline_create(const xb_params* p, int device, int nWorkers, int nIo, xb
   xb_pipeline* pl = new xb_pipeline;
   pl->device = device;
   pl->nIo = nIo;
+  pl->base = *p;
   for(int i = 0; i < nWorkers; i++) {
     xb_ctx* c = nullptr;
     const int rc = xb_ctx_create(p, device, &c);
@@ -229,6 +232,18 @@ int xb_pipeline_worker(xb_pipeline* pl, int i, xb_ctx** ctx) {
   return XB_OK;
 }
 
+int xb_pipeline_set_params(xb_pipeline* pl, int nPairs, const xb_params* params) {
+  if(!pl || nPairs < 0 || (nPairs > 0 && !params)) return XB_ERR_ARG;
+  for(int i = 0; i < nPairs; i++)
+    if(!xb::sameFit(pl->base, params[i])) {
+      pl->lastError = "pair " + std::to_string(i) +
+                      ": parameters change the basis or the fit's sizes of the pipeline";
+      return XB_ERR_ARG;
+    }
+  pl->pairParams.assign(params, params + nPairs);
+  return XB_OK;
+}
+
 int xb_pipeline_stats_get(const xb_pipeline* pl, xb_pipeline_stats* out) {
   if(!pl || !out) return XB_ERR_ARG;
   *out = pl->stats;
@@ -241,6 +256,10 @@ int xb_pipeline_run_files(xb_pipeline* pl, int nPairs, const char* const* templa
   if(!pl) return XB_ERR_ARG;
   if(nPairs < 0 || (nPairs > 0 && (!templatePath || !sciencePath))) {
     pl->lastError = "bad pair lists";
+    return XB_ERR_ARG;
+  }
+  if(!pl->pairParams.empty() && (int)pl->pairParams.size() < nPairs) {
+    pl->lastError = "fewer pair parameter sets than pairs";
     return XB_ERR_ARG;
   }
   const auto t0 = Clock::now();
@@ -290,7 +309,9 @@ int xb_pipeline_run_files(xb_pipeline* pl, int nPairs, const char* const* templa
         Slot& sl = pl->slots[s];
         const int i = sl.pair;
         const auto tc = Clock::now();
-        st[i] = computePair(c, sl, convPath && convPath[i], diffPath && diffPath[i]);
+        st[i] = xb_ctx_set_params(c, pl->pairParams.empty() ? &pl->base : &pl->pairParams[i]);
+        if(st[i] == XB_OK)
+          st[i] = computePair(c, sl, convPath && convPath[i], diffPath && diffPath[i]);
         ms += msSince(tc);
         if(st[i] == XB_OK) ks[i] = c->kernSum;
         else msg[i] = c->lastError;

@@ -64,7 +64,8 @@ EXPORTS = [
     "xb_batch_worker", "xb_batch_set_stream", "xb_batch_set_params", "xb_ranker_param_count", "xb_ranker_set",
     "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
     "xb_pipeline_create", "xb_pipeline_destroy", "xb_pipeline_last_error", "xb_pipeline_worker",
-    "xb_pipeline_run_files", "xb_pipeline_stats_get", "xb_measure_fma_peaks",
+    "xb_pipeline_run_files", "xb_pipeline_stats_get", "xb_pipeline_set_params",
+    "xb_measure_fma_peaks",
 ]
 
 
@@ -142,6 +143,7 @@ def lib():
     L.xb_pipeline_run_files.argtypes = [vp, i, P(ctypes.c_char_p), P(ctypes.c_char_p),
                                         P(ctypes.c_char_p), P(ctypes.c_char_p), P(i), P(d)]
     L.xb_pipeline_stats_get.argtypes = [vp, P(PipelineStats)]
+    L.xb_pipeline_set_params.argtypes = [vp, i, vp]
     L.xb_measure_fma_peaks.argtypes = [i, P(d), P(d)]
     _lib = L
     return L
@@ -484,6 +486,16 @@ class Pipeline:
         if rc != 0 and check:
             raise XbError(rc, self.L.xb_pipeline_last_error(self.h).decode())
         return [int(st[i]) for i in range(n)], [float(ks[i]) for i in range(n)]
+
+    def set_params(self, params_list):
+        """Parameters per pair for later runs (a list of xb_params; [] or None
+        returns to the pipeline's own)."""
+        params_list = list(params_list or [])
+        arr = (XbParams * max(len(params_list), 1))(*params_list)
+        rc = self.L.xb_pipeline_set_params(self.h, len(params_list), arr)
+        if rc:
+            raise XbError(rc, self.L.xb_pipeline_last_error(self.h).decode())
+        self._keep_params = arr
 
     def stats(self):
         out = PipelineStats()
