@@ -9,7 +9,7 @@ in parallel, into in-tree outputs:
   oracle/liboracle_xbach.so                     the CPU oracle (checker)
 
 No cmake: a dependency-free rebuild check on file mtimes keeps repeated
-calls cheap.  Host code is portable C++17 (the GPU machine is aarch64).
+calls cheap.  Host code is portable C++17 (the GPU hosts are aarch64).
 """
 import concurrent.futures as cf
 import os
