@@ -154,6 +154,11 @@ int xb_ctx_set_params(xb_ctx* ctx, const xb_params* p);
  * probability is below "rank_tau" (thousandths, default 500) behind the
  * others, keeping the reference's order within each group; 2 sorts all by
  * score.
+ * "ldl_panel" (0/1, default 1, mixed mode): let the tuner choose among the
+ * column LDL^T kernel and its panel variants (identical factors); 0 keeps
+ * the column kernel.
+ * "ldl_cluster" (16 or 8, default 16, mixed mode): CTAs of the LDL^T cluster
+ * (identical factors).
  * "gram_fp64" (0/1, mixed mode): compute the per-stamp Gram matrices with
  * FP64 accumulation on the CUDA cores instead of the exact tensor-core
  * slicing (a cross-check; the results agree to rounding).
@@ -326,7 +331,8 @@ int xb_measure_fma_peaks(int device, double* fp32Tflops, double* fp64Tflops);
  * otherwise), nWorkers contexts run xb_run on them (the frame graph when
  * option "graph" is on; FP64 pairs run the plain stages and are refused in
  * mixed mode), and nIo writer threads encode conv and diff as BITPIX -32.
- * Each pair's images are those of xb_run on a single context. */
+ * Each pair's images are those of xb_run on a single context.  One call at a
+ * time per pipeline (its workers and slots are reused by every call). */
 typedef struct xb_pipeline xb_pipeline;
 typedef struct {
   double wall_ms;       /* last run, start to last write */
