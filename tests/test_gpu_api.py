@@ -265,3 +265,30 @@ def test_cli_pairs_with_input_mask(tmp_path):
         sub = read_fits(tmp_path / f"{prefix}sub.fits")
         assert np.all(sub[60:70, 200:230] == np.float32(1e-30)), prefix
         assert np.mean(sub == np.float32(1e-30)) < 0.5
+
+
+def test_device_images_hold_the_results(test01):
+    """xb_get_device_images: the device conv and diff images are the ones
+    xb_get_image copies out (read back here through the CUDA runtime)."""
+    import ctypes
+    import ctypes.util
+    import xbach
+    T, S = test01["T"].astype(np.float32), test01["S"].astype(np.float32)
+    ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED))
+    ctx.run_all(T, S)
+    names = [ctypes.util.find_library("cudart"), "libcudart.so", "/usr/local/cuda/lib64/libcudart.so"]
+    rt = None
+    for n in names:
+        try:
+            rt = ctypes.CDLL(n) if n else None
+        except OSError:
+            rt = None
+        if rt is not None:
+            break
+    if rt is None:
+        pytest.skip("no CUDA runtime library to read device memory with")
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    for ptr, which in zip(ctx.device_images(), (xbach.XB_IMG_CONV, xbach.XB_IMG_DIFF)):
+        out = np.empty(T.shape, np.float32)
+        assert rt.cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2) == 0  # device to host
+        assert np.array_equal(out, ctx.image(which, f64=False)), which

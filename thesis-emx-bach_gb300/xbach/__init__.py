@@ -264,6 +264,13 @@ class Context:
         self._check(fn(self.h, which, out.ctypes.data))
         return out.reshape(self.hgt, self.w)
 
+    def device_images(self):
+        """(conv, diff) device pointers (ints) of the FP32 result images,
+        valid until the next init or destroy."""
+        c, d = ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(self.L.xb_get_device_images(self.h, ctypes.byref(c), ctypes.byref(d)))
+        return c.value, d.value
+
     def mask(self):
         out = np.empty(self.w * self.hgt, np.uint16)
         self._check(self.L.xb_get_mask(self.h, out.ctypes.data))
