@@ -292,3 +292,27 @@ def test_device_images_hold_the_results(test01):
         out = np.empty(T.shape, np.float32)
         assert rt.cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2) == 0  # device to host
         assert np.array_equal(out, ctx.image(which, f64=False)), which
+
+
+def test_cli_extension_flags_reach_the_fit(tmp_path):
+    """-gain, -rn, -wfit and -pk: the CLI's images equal those of the API with
+    gain, readNoise, fitWeighted and convPerPixel set."""
+    import build_native
+    import xbach
+    out = tmp_path / "x_"
+    r = subprocess.run([str(build_native.CLI_BIN), "-ip", str(GOLDEN), "-s", "test0.fits",
+                        "-t", "test1.fits", "-op", str(out), "-gain", "2.0", "-rn", "4.0",
+                        "-wfit", "-pk"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    T, S = read_fits(GOLDEN / "test1.fits"), read_fits(GOLDEN / "test0.fits")
+    ctx = xbach.Context(xbach.default_params(gain=2.0, readNoise=4.0, fitWeighted=1,
+                                             convPerPixel=1))
+    ctx.run_all(T, S)
+    assert np.array_equal(read_fits(f"{out}sub.fits"),
+                          ctx.image(xbach.XB_IMG_DIFF, f64=False).astype(np.float64))
+    assert np.array_equal(read_fits(f"{out}diff.fits"),
+                          ctx.image(xbach.XB_IMG_CONV, f64=False).astype(np.float64))
+    plain = xbach.Context(xbach.default_params())
+    plain.run_all(T, S)
+    assert not np.array_equal(read_fits(f"{out}sub.fits"),
+                              plain.image(xbach.XB_IMG_DIFF, f64=False).astype(np.float64))
