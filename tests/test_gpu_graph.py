@@ -154,3 +154,34 @@ def test_graph_option_needs_mixed_mode():
     ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_PLAIN))
     with pytest.raises(xbach.XbError):
         ctx.set_option("graph", 1)
+
+
+def test_graph_input_mask_toggled_between_frames():
+    """Setting, clearing and setting again an input mask between replays:
+    each frame replays (or captures) the graph of its own mask state and
+    equals the stage-by-stage run with that state."""
+    import xbach
+    fr = _pairs(2)
+    info = fr[0][2]
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED, stampsx=info["stamps"],
+                                  stampsy=info["stamps"], threshHigh=info["threshHigh"])
+    T, S = fr[0][0], fr[0][1]
+    m = np.zeros(T.shape, np.uint8)
+    m[200:240, 100:180] = 1
+
+    def ref(mask):
+        ctx = xbach.Context(params)
+        if mask is not None:
+            ctx.set_input_mask(mask)
+        ctx.run_all(T, S)
+        return ctx.image(xbach.XB_IMG_DIFF, f64=False)
+
+    with_mask, without = ref(m), ref(None)
+    assert not np.array_equal(with_mask, without)
+    g = xbach.Context(params)
+    g.set_option("graph", 1)
+    for step, mask in enumerate([m, None, m, None, m]):
+        g.set_input_mask(mask)
+        g.run(T, S)
+        want = with_mask if mask is not None else without
+        assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False), want), step
