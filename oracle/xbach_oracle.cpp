@@ -41,7 +41,7 @@ namespace {
 
 constexpr uint16_t BAD_PIX_VAL = 1u << 0, SAT_PIXEL = 1u << 1,
                    LOW_PIXEL = 1u << 2, NAN_PIXEL = 1u << 3,
-                   BAD_CONV = 1u << 4, OK_CONV = 1u << 6,
+                   BAD_CONV = 1u << 4, INPUT_MASK = 1u << 5, OK_CONV = 1u << 6,
                    BAD_INPUT = 1u << 7, BAD_PIXEL_T = 1u << 8,
                    SKIP_T = 1u << 9, BAD_PIXEL_S = 1u << 10, SKIP_S = 1u << 11,
                    BAD_OUTPUT = 1u << 12, ALL = (1u << 13) - 1u;
@@ -107,6 +107,7 @@ struct xbo_handle {
   int w = 0, h = 0;
   std::vector<double> img[2];   // 0 = template, 1 = science
   std::vector<uint16_t> mask;
+  std::vector<uint8_t> inMask;   // input mask (nonzero: excluded), or empty
   // basis (cl_kern/cmv.cl:1-68, include/datatypeUtil.h:46-118)
   std::vector<int> kgauss, kx, ky;          // per basis function
   std::vector<double> fX, fY, vec;          // nPSF*fK, nPSF*fK, nPSF*fK*fK
@@ -155,6 +156,11 @@ void maskInput(xbo_handle& o) {
       o.mask[id] = m;
     }
   }
+  // input mask (extension; the reference defines INPUT_MASK, datatypeUtil.h:179,
+  // but never sets it): excluded pixels are bad input before the dilation
+  if(!o.inMask.empty())
+    for(size_t id = 0; id < o.mask.size(); id++)
+      if(o.inMask[id]) o.mask[id] |= INPUT_MASK | BAD_INPUT;
   // spreadMask: src/bachUtil.cpp:22-31 -> cl_kern/ini.cl:37-67.  Only
   // BAD_INPUT is read and only OK_CONV is written, so a snapshot of the
   // BAD_INPUT bits gives the in-place kernel's result.
@@ -1331,7 +1337,11 @@ void convPerPixel(xbo_handle& o, const std::vector<uint16_t>& cmask, double invK
   }
   for(int y = 0; y < h; y++)
     for(int x = 0; x < w; x++)
-      if(!(x >= hK && x < w - hK && y >= hK && y < h - hK)) o.conv[(size_t)x + (size_t)y * w] = 1e-30;
+      if(!(x >= hK && x < w - hK && y >= hK && y < h - hK)) {
+        const size_t id = (size_t)x + (size_t)y * w;
+        o.conv[id] = 1e-30;
+        if(!o.inMask.empty() && o.inMask[id]) o.mask[id] |= INPUT_MASK | BAD_INPUT | BAD_OUTPUT;
+      }
 }
 
 // ---------------------------------------------------------- conv + sub ---
@@ -1363,6 +1373,7 @@ void convSub(xbo_handle& o) {
     if(t == 0.0) m |= BAD_INPUT | BAD_PIX_VAL;
     if(t >= o.p.threshHigh) m |= BAD_INPUT | SAT_PIXEL;
     if(t <= o.p.threshLow) m |= BAD_INPUT | LOW_PIXEL;
+    if(!o.inMask.empty() && o.inMask[id]) m |= INPUT_MASK | BAD_INPUT;  // input mask
     cmask[id] = m;
   }
   o.conv.assign((size_t)w * h, 0.0);
@@ -1402,6 +1413,7 @@ void convSub(xbo_handle& o) {
         o.mask[id] = nm;
       } else {
         o.conv[id] = 1e-30;
+        if(!o.inMask.empty() && o.inMask[id]) o.mask[id] |= INPUT_MASK | BAD_INPUT | BAD_OUTPUT;
       }
     }
   for(size_t id = 0; id < cmask.size(); id++) {
@@ -1570,7 +1582,14 @@ extern "C" {
 
 xbo_handle* xbo_run(const xb_params* p, const double* T, const double* S,
                     int w, int h, int nthreads, int keep_w, int* status) {
+  return xbo_run_masked(p, T, S, nullptr, w, h, nthreads, keep_w, status);
+}
+
+xbo_handle* xbo_run_masked(const xb_params* p, const double* T, const double* S,
+                           const uint8_t* inMask, int w, int h, int nthreads, int keep_w,
+                           int* status) {
   auto* o = new xbo_handle();
+  if(inMask) o->inMask.assign(inMask, inMask + (size_t)w * h);
 #ifdef _OPENMP
   if(nthreads > 0) omp_set_num_threads(nthreads);
   o->scalars["threads"] = nthreads > 0 ? nthreads : omp_get_max_threads();

@@ -32,6 +32,12 @@ typedef struct xbo_handle xbo_handle;
  * (free it with xbo_free). */
 xbo_handle* xbo_run(const xb_params* p, const double* T, const double* S,
                     int w, int h, int nthreads, int keep_w, int* status);
+/* The same with an input mask (w*h bytes, nonzero = excluded; the
+ * extension of xb_set_input_mask): INPUT_MASK | BAD_INPUT at init before the
+ * dilation, bad input for the convolution. */
+xbo_handle* xbo_run_masked(const xb_params* p, const double* T, const double* S,
+                           const uint8_t* inMask, int w, int h, int nthreads,
+                           int keep_w, int* status);
 int xbo_get_array(const xbo_handle* h, const char* name, void* out,
                   size_t cap, size_t* nbytes);
 int xbo_get_scalar(const xbo_handle* h, const char* name, double* out);

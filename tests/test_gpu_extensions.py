@@ -178,3 +178,31 @@ def test_mixed_weighted_fit_within_1e3_sigma_of_plain(field):
     assert ct == ct_m
     e = diff_error(d_m, d_p, c_p, S if ct == 1 else T)
     assert e["pixels"] > 0.8 * T.size and e["max_sigma"] <= 1e-3, e
+
+
+def test_plain_input_mask_matches_oracle(oracle, field):
+    """An input mask (a block and a bad column): the plain GPU path equals the
+    oracle's masked run on the init mask, the substamp sets, every ksc
+    decision, the chi^2, the solution and the final mask; images within the
+    parity suite's 1e-11."""
+    import xbach
+    T, S, kw = field
+    m = np.zeros(T.shape, np.uint8)
+    m[200:230, 300:340] = 1
+    m[:, 77] = 1
+    ref = oracle.run(oracle.default_params(**kw), T.astype(np.float64), S.astype(np.float64),
+                     mask=m)
+    assert ref.status == 0
+    ctx = xbach.Context(xbach.default_params(**kw), trace=True)
+    ctx.set_input_mask(m)
+    ctx.run_all(T, S)
+    assert np.array_equal(ctx.array("mask_init", np.uint16), ref.array("mask_init", np.uint16))
+    for k in ("ss_xy0", "ss_xy1", "ksc_rejects", "cur"):
+        assert np.array_equal(ctx.array(k, np.int32), ref.array(k, np.int32)), k
+    for k in ("ksc_sig_last", "solution"):
+        assert _same(ctx.array(k, np.float64), ref.array(k, np.float64)), k
+    assert _same(np.array([ctx.scalar("kernSum")]), np.array([ref.scalar("kernSum")]))
+    assert np.array_equal(ctx.array("mask", np.uint16), ref.array("mask", np.uint16))
+    scale = np.abs(ref.array("conv", np.float64)).max()
+    for k in ("conv", "diff"):
+        assert np.abs(ctx.array(k, np.float64) - ref.array(k, np.float64)).max() <= 1e-11 * scale, k

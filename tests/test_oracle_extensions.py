@@ -93,3 +93,25 @@ def test_weighted_fit_changes_the_solution(oracle, test01, test01_oracle):
     w = _run(oracle, test01, fitWeighted=1, readNoise=5.0)
     a, b = w.array("solution", np.float64), test01_oracle.array("solution", np.float64)
     assert a.shape == b.shape and np.all(np.isfinite(a)) and not np.array_equal(a, b)
+
+
+def test_oracle_input_mask_excludes_pixels(oracle, test01, test01_oracle):
+    """The oracle's input mask: the pixels get INPUT_MASK | BAD_INPUT at
+    init, end BAD_OUTPUT with the bad-output value, and an empty mask gives
+    the unmasked run bit for bit."""
+    INPUT_MASK, BAD_INPUT, BAD_OUTPUT = 1 << 5, 1 << 7, 1 << 12
+    T, S = test01["T"], test01["S"]
+    m = np.zeros(T.shape, np.uint8)
+    m[100:110, 150:170] = 1
+    m[200, :] = 1
+    r = oracle.run(oracle.default_params(), T, S, mask=m)
+    assert r.status == 0
+    init = r.array("mask_init", np.uint16).reshape(T.shape)
+    assert np.all((init[m != 0] & (INPUT_MASK | BAD_INPUT)) == INPUT_MASK | BAD_INPUT)
+    fin = r.array("mask", np.uint16).reshape(T.shape)
+    assert np.all(fin[m != 0] & BAD_OUTPUT)
+    assert np.all(r.array("diff", np.float64).reshape(T.shape)[m != 0] == 1e-30)
+    empty = oracle.run(oracle.default_params(), T, S, mask=np.zeros_like(m))
+    for k in ("solution", "diff", "mask"):
+        dt = np.uint16 if k == "mask" else np.float64
+        assert np.array_equal(empty.array(k, dt), test01_oracle.array(k, dt)), k

@@ -102,6 +102,11 @@ class Oracle:
                                 ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(ctypes.c_int)]
+        lib.xbo_run_masked.restype = ctypes.c_void_p
+        lib.xbo_run_masked.argtypes = [ctypes.POINTER(XbParams), ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]
         lib.xbo_get_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p,
                                       ctypes.c_void_p, ctypes.c_size_t,
                                       ctypes.POINTER(ctypes.c_size_t)]
@@ -131,14 +136,21 @@ class Oracle:
                 setattr(p, k, v)
         return p
 
-    def run(self, params, T, S, nthreads=0, keep_w=False):
+    def run(self, params, T, S, nthreads=0, keep_w=False, mask=None):
+        """mask: optional (h, w) input mask, nonzero = excluded."""
         T = np.ascontiguousarray(T, dtype=np.float64)
         S = np.ascontiguousarray(S, dtype=np.float64)
         h, w = T.shape
         st = ctypes.c_int(-1)
-        hd = self.lib.xbo_run(ctypes.byref(params), T.ctypes.data,
-                              S.ctypes.data, w, h, nthreads, int(keep_w),
-                              ctypes.byref(st))
+        if mask is None:
+            hd = self.lib.xbo_run(ctypes.byref(params), T.ctypes.data,
+                                  S.ctypes.data, w, h, nthreads, int(keep_w),
+                                  ctypes.byref(st))
+        else:
+            m = np.ascontiguousarray(np.asarray(mask) != 0, dtype=np.uint8)
+            hd = self.lib.xbo_run_masked(ctypes.byref(params), T.ctypes.data,
+                                         S.ctypes.data, m.ctypes.data, w, h, nthreads,
+                                         int(keep_w), ctypes.byref(st))
         return OracleResult(self.lib, hd, st.value, w, h)
 
 
