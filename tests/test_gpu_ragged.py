@@ -76,3 +76,38 @@ def test_mixed_within_1e3_sigma_and_graph_replays(frame):
         g.run(T, S)
         assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False),
                               mixed.image(xbach.XB_IMG_DIFF, f64=False)), name
+
+
+def test_plain_other_widths_match_oracle(oracle):
+    """Kernel and substamp widths other than the reference's 21 / 31 px
+    (hKernelWidth 12, hSStampWidth 18): plain mode still equals the oracle on
+    every decision, the chi^2 and the solution."""
+    import xbach
+    from xbach.synth import make_pair
+    T, S, info = make_pair(1)
+    kw = dict(hKernelWidth=12, hSStampWidth=18, stampsx=info["stamps"], stampsy=info["stamps"],
+              threshHigh=info["threshHigh"])
+    ref = oracle.run(oracle.default_params(**kw), T.astype(np.float64), S.astype(np.float64))
+    assert ref.status == 0
+    ctx = xbach.Context(xbach.default_params(**kw), trace=True)
+    ctx.run_all(T, S)
+    for k in ("ss_xy0", "ss_xy1", "ksc_rejects", "cur"):
+        assert np.array_equal(ctx.array(k, np.int32), ref.array(k, np.int32)), k
+    for k in ("ksc_sig_last", "solution"):
+        assert np.array_equal(_bits(ctx.array(k, np.float64)), _bits(ref.array(k, np.float64))), k
+    assert np.array_equal(ctx.array("mask", np.uint16), ref.array("mask", np.uint16))
+
+
+def test_mixed_refuses_other_kernel_widths_cleanly():
+    """The mixed convolution is built for 21-px kernels: another width is an
+    XB_ERR_UNSUPPORTED status, and the context stays usable."""
+    import xbach
+    from xbach.synth import make_pair
+    T, S, info = make_pair(1)
+    ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED, hKernelWidth=12,
+                                             threshHigh=info["threshHigh"]))
+    with pytest.raises(xbach.XbError) as e:
+        ctx.run_all(T, S)
+    assert e.value.code == 10
+    ok = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED, threshHigh=info["threshHigh"]))
+    ok.run_all(T, S)
