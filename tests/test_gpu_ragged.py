@@ -98,16 +98,29 @@ def test_plain_other_widths_match_oracle(oracle):
     assert np.array_equal(ctx.array("mask", np.uint16), ref.array("mask", np.uint16))
 
 
-def test_mixed_refuses_other_kernel_widths_cleanly():
-    """The mixed convolution is built for 21-px kernels: another width is an
-    XB_ERR_UNSUPPORTED status, and the context stays usable."""
+def test_mixed_other_kernel_width_within_1e3_sigma():
+    """The mixed path's FP32 conv tile is built for 21-px kernels; a mixed
+    frame with another width (25 px) runs the FP64 block conv and stays within
+    1e-3 sigma of plain mode, stage by stage and as a replayed frame graph."""
     import xbach
+    from xbach.accuracy import diff_error
     from xbach.synth import make_pair
     T, S, info = make_pair(1)
-    ctx = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED, hKernelWidth=12,
-                                             threshHigh=info["threshHigh"]))
-    with pytest.raises(xbach.XbError) as e:
-        ctx.run_all(T, S)
-    assert e.value.code == 10
-    ok = xbach.Context(xbach.default_params(mode=xbach.XB_MODE_MIXED, threshHigh=info["threshHigh"]))
-    ok.run_all(T, S)
+    kw = dict(hKernelWidth=12, stampsx=info["stamps"], stampsy=info["stamps"],
+              threshHigh=info["threshHigh"])
+    plain = xbach.Context(xbach.default_params(**kw))
+    plain.run_all(T, S)
+    params = xbach.default_params(mode=xbach.XB_MODE_MIXED, **kw)
+    mixed = xbach.Context(params)
+    mixed.run_all(T, S)
+    ct = plain.scalar("convTemplate")
+    assert mixed.scalar("convTemplate") == ct
+    e = diff_error(mixed.image(xbach.XB_IMG_DIFF), plain.image(xbach.XB_IMG_DIFF),
+                   plain.image(xbach.XB_IMG_CONV), S if ct == 1 else T)
+    assert e["pixels"] > 0.5 * T.size and e["max_sigma"] <= 1e-3, e
+    g = xbach.Context(params)
+    g.set_option("graph", 1)
+    for _ in range(2):
+        g.run(T, S)
+        assert np.array_equal(g.image(xbach.XB_IMG_DIFF, f64=False),
+                              mixed.image(xbach.XB_IMG_DIFF, f64=False))

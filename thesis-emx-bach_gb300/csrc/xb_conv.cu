@@ -332,7 +332,9 @@ void stageConvSub(xb_ctx* c, bool doSub) {
     const double xf = (c->w / 2 - hx) / hx, yf = (c->h / 2 - hy) / hy;
     kernelSumLaunch(c, c->dSol, xf, yf, 0, ks);
   }
-  if(mixedMode(c)) {
+  // the FP32 conv tile is built for 21-px kernels; mixed frames with another
+  // kernel width take the FP64 block conv below
+  if(mixedMode(c) && g.fK == 21) {
     c->convD = nullptr;
     c->diffD = nullptr;
     convSubMixed(c, ks);
@@ -420,6 +422,7 @@ void stageConvSub(xb_ctx* c, bool doSub) {
         c->diffD, c->diffF);
   }
   XB_LAUNCHED(c);
+  if(c->capturing) return;  // a frame graph records the kernel sum on the device
   c->kernSum = toHost(c, ks, 1)[0];
   c->scalars["kernSum"] = c->kernSum;
   if(c->trace) {
