@@ -258,9 +258,14 @@ int xb_get_stream(xb_ctx* ctx, void** stream);
  * same kernel as xb_sss, with all scratch taken from a 32 MiB device array
  * built into the library (held on every GPU that loads it until exit).
  *   dImg   w*h FP32 image, device memory
- *   dMask  w*h mask words (in/out: NaN pixels get NAN_PIXEL|BAD_INPUT, as in
- *          xb_sss)
- *   dGeom  nStamps x {x, y, width, height} ints, 16-byte aligned, device
+ *   dMask  w*h mask words (in/out: NaN pixels inside a stamp's fStampWidth^2
+ *          area get NAN_PIXEL|BAD_INPUT, as in xb_sss)
+ *   dGeom  nStamps x {x, y, width, height} ints, 16-byte aligned, device.
+ *          Each stamp must have the form of the reference's stamp grid
+ *          (createStampBounds, cl_kern/sss.cl:19-40): 0 <= x < w, 0 <= y < h,
+ *          width = min(fStampWidth, w - x), height = min(fStampWidth, h - y),
+ *          as every stamp xb_sss builds does.  A stamp that does not gets
+ *          NaN in dSky and dFwhm, and none of its pixels is read.
  *   dSky, dFwhm  nStamps doubles each, device memory
  *   stream cudaStream_t to launch on (NULL = legacy default stream); the call
  *          returns after the launch, results are ready when the stream is
@@ -268,9 +273,14 @@ int xb_get_stream(xb_ctx* ctx, void** stream);
  * must fit in 32 MiB (2048^2 with 16x16 stamps of 107 px needs 27 MiB);
  * larger requests return XB_ERR_UNSUPPORTED and nothing runs.  The first call
  * on each device looks up the array's device address, so make that first call
- * before capturing a stream.  All calls share the one array: calls whose
- * launches overlap on the GPU race with each other; the kernel needs nothing
- * cleared, it writes every scratch byte before reading it.  `err` (may be
+ * before capturing a stream; the address is kept for the device's context,
+ * so do not use the entry point across a cudaDeviceReset.  All calls share
+ * the one array: calls whose launches overlap on the GPU race with each
+ * other; the kernel needs nothing cleared, it writes every scratch byte
+ * before reading it.  Errors: XB_ERR_ARG (null pointer, non-positive size,
+ * unaligned dGeom), XB_ERR_UNSUPPORTED (beyond the limit), XB_ERR_CUDA (a
+ * CUDA error was already pending when the call began -- reported and left in
+ * place, nothing launched -- or the launch itself failed).  `err` (may be
  * NULL) receives a message on failure.  Calls no allocation routine. */
 int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w, int h,
                            const int* dGeom, int nStamps, int fStampWidth,

@@ -1703,6 +1703,35 @@ int xbo_get_scalar(const xbo_handle* h, const char* name, double* out) {
 
 void xbo_free(xbo_handle* h) { delete h; }
 
+int xbo_stamp_stats(const double* img, uint16_t* mask, int w, int h, const int* geom,
+                    int n, int fStampWidth, double sigClipAlpha, double iqRange, double* sky,
+                    double* fwhm) {
+  xbo_handle o;
+  xb_params_default(&o.p);
+  o.p.sigClipAlpha = sigClipAlpha;
+  o.p.iqRange = iqRange;
+  o.w = w;
+  o.h = h;
+  o.fStampWidth = fStampWidth;
+  o.img[0].assign(img, img + (size_t)w * h);
+  o.mask.assign(mask, mask + (size_t)w * h);
+  AllStamps st;
+  st.n = n;
+  for(int i = 0; i < n; i++) {
+    st.cx.push_back(geom[4 * i]);
+    st.cy.push_back(geom[4 * i + 1]);
+    st.sx.push_back(geom[4 * i + 2]);
+    st.sy.push_back(geom[4 * i + 3]);
+  }
+  std::vector<double> sk, fw;
+  const int rc = calcStats(o, st, 0, sk, fw);
+  if(rc != XB_OK) return rc;
+  std::copy(sk.begin(), sk.end(), sky);
+  std::copy(fw.begin(), fw.end(), fwhm);
+  std::copy(o.mask.begin(), o.mask.end(), mask);
+  return XB_OK;
+}
+
 void xbo_sigma_clip(const double* data, int n, int maxIter, double alpha,
                     double* mean, double* stdDev) {
   sigmaClip(data, n, mean, stdDev, maxIter, alpha);

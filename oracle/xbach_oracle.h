@@ -48,6 +48,14 @@ void xbo_free(xbo_handle* h);
  * cl_kern/bach.cl:135-170. */
 void xbo_sigma_clip(const double* data, int n, int maxIter, double alpha,
                     double* mean, double* stdDev);
+/* calcStats of src/bachUtil.cpp:130-280 (sampling, maskStamp, sigmaClip,
+ * createHistogram) for caller-given stamps: geom holds n x {x, y, width,
+ * height}, every stamp inside the image with width*height >= 100 (else
+ * XB_ERR_STAMP_TOO_SMALL); mask is in/out (NaN pixels get
+ * NAN_PIXEL|BAD_INPUT). */
+int xbo_stamp_stats(const double* img, uint16_t* mask, int w, int h, const int* geom,
+                    int n, int fStampWidth, double sigClipAlpha, double iqRange, double* sky,
+                    double* fwhm);
 /* Numerical-Recipes ran1 of cl_kern/sss.cl:52-79, seeded with idum; writes
  * n deviates. */
 void xbo_ran1_seq(int idum, int n, double* out);

@@ -122,6 +122,10 @@ class Oracle:
                                      ctypes.c_void_p]
         lib.xbo_lu_solve.argtypes = [ctypes.c_void_p, ctypes.c_int,
                                      ctypes.c_void_p]
+        lib.xbo_stamp_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_void_p, ctypes.c_void_p]
         self.lib = lib
 
     def default_params(self, **kw):
@@ -135,6 +139,21 @@ class Oracle:
             else:
                 setattr(p, k, v)
         return p
+
+    def stamp_stats(self, img, mask, geom, fsw, alpha, iq_range):
+        """calcStats for the stamps geom (n x {x, y, width, height}); returns
+        (sky, fwhm, mask after NaN flagging)."""
+        img = np.ascontiguousarray(img, dtype=np.float64)
+        h, w = img.shape
+        m = np.ascontiguousarray(mask, dtype=np.uint16).copy()
+        g = np.ascontiguousarray(geom, dtype=np.int32)
+        n = len(g)
+        sky, fwhm = np.zeros(n), np.zeros(n)
+        rc = self.lib.xbo_stamp_stats(img.ctypes.data, m.ctypes.data, w, h, g.ctypes.data, n,
+                                      fsw, alpha, iq_range, sky.ctypes.data, fwhm.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("xbo_stamp_stats status %d" % rc)
+        return sky, fwhm, m
 
     def run(self, params, T, S, nthreads=0, keep_w=False, mask=None):
         """mask: optional (h, w) input mask, nonzero = excluded."""

@@ -170,6 +170,22 @@ __global__ void __launch_bounds__(ST_THREADS)
   const int4 gm = geom[s];  // cx, cy, sx, sy
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr bool F32 = sizeof(T) == 4;
+  // A stamp must have the form of the reference's grid (createStampBounds,
+  // cl_kern/sss.cl:19-40): its origin inside the image and its size the full
+  // stamp width clipped by the image edge.  Its histogram is then taken over
+  // the good pixels of the clipped fSW^2 window (phase D), which are exactly
+  // the stamp's pixels.  The grid that xb_sss builds always has this form;
+  // geometry passed in from outside (xb_stamp_stats_noalloc) that does not
+  // gets NaN statistics and no pixel of it is read (the test is uniform over
+  // the CTA, before any barrier).
+  if(gm.x < 0 || gm.y < 0 || gm.x >= w || gm.y >= h || gm.z != min(fSW, w - gm.x) ||
+     gm.w != min(fSW, h - gm.y)) {
+    if(tid == 0) {
+      skyOut[s] = __longlong_as_double(0x7ff8000000000000ll);
+      fwhmOut[s] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+    return;
+  }
   __shared__ double samples[PADDED];
   __shared__ double rtab[98];
   __shared__ int cand[32];
@@ -1696,6 +1712,11 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
     return noallocFail(err, errCap, XB_ERR_UNSUPPORTED,
                        "stamps need more than the 32 MiB scratch: nStamps * (9 * fStampWidth^2 "
                        "+ 16 * ceil(fStampWidth^2 / 32)) bytes must fit");
+  // An error left pending by the caller's own work is reported as such and
+  // left in place (not cleared), so it is not mistaken for this call's.
+  const cudaError_t pending = cudaPeekAtLastError();
+  if(pending != cudaSuccess)
+    return noallocFail(err, errCap, XB_ERR_CUDA, "a CUDA error was already pending; nothing launched");
   int dev = -1;
   if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return noallocFail(err, errCap, XB_ERR_CUDA, "no usable current CUDA device");
@@ -1703,6 +1724,9 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
   {
     // The array's device address is looked up once per device, with that
     // device current; host code must not use the symbol itself as an address.
+    // The cached address belongs to the device's current context: after a
+    // cudaDeviceReset the module is reloaded elsewhere, so the entry point
+    // must not be used across a reset.
     std::lock_guard<std::mutex> lock(g_statsScratchMutex);
     if(!g_statsScratchAddr[dev]) {
       void* p = nullptr;
@@ -1724,6 +1748,7 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
       dImg, dMask, reinterpret_cast<const int4*>(dGeom), w, h, fStampWidth,
       reinterpret_cast<float*>(good), clip, chunks,
       maxChunks, sigClipAlpha, iqRange, dSky, dFwhm, nullptr);
+  // no error was pending before the launch, so any error now is the launch's
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
   return XB_OK;
