@@ -5,7 +5,7 @@ Plain mode: every decision, the stamp chi^2 and the solution bit-identical;
 the per-pixel convolution is an FMA chain in the oracle's order, so its
 images are bit-identical too (the per-block images keep the parity suite's
 1e-11 tolerance).  Mixed mode: the per-pixel FP32 convolution within the
-mixed path's bars (1e-3 sigma; 1e-2 on test01) of the plain per-pixel one,
+mixed path's bar (1e-3 sigma) of the plain per-pixel one,
 and a frame graph replays it bit for bit.
 The defaults reproduce the reference (the parity suite runs with them)."""
 import numpy as np
@@ -88,10 +88,7 @@ def test_gain_alone_scales_the_chi2(field):
     assert _same(out[1].image(xbach.XB_IMG_DIFF), out[0].image(xbach.XB_IMG_DIFF))
 
 
-# test01's global system has cond ~6e13: FP32 storage of W alone moves its
-# difference image by 1.2e-3 sigma, so it keeps the 1e-2 bar the block-kernel
-# mixed path is held to there; the synthetic field is held to 1e-3 sigma.
-SIGMA_BAR = {"config1": 1e-3, "test01": 1e-2}
+SIGMA_BAR = {"config1": 1e-3, "test01": 1e-3}
 
 
 @pytest.mark.parametrize("src", ["config1", "test01"])

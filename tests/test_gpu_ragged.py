@@ -2,8 +2,7 @@
 kernel blocks nor the stamp grid, so every tiled kernel meets partial blocks
 at the right and bottom edges.  Plain mode against the oracle (decisions,
 chi^2, solution and kernel sum bit-exact, masks identical, images within
-1e-11 of their scale); mixed mode within 1e-3 sigma of plain (2e-3 and 1e-2
-for two crops, below); a frame graph replays the stage-by-stage run bit for
+1e-11 of their scale); mixed mode within 1e-3 sigma of plain; a frame graph replays the stage-by-stage run bit for
 bit."""
 import numpy as np
 import pytest
@@ -12,13 +11,10 @@ pytestmark = pytest.mark.gpu
 
 CROPS = {"wide": (437, 611), "tall": (611, 437), "small": (173, 300)}
 # The 173 x 300 frame holds 15 stamps (5 x 3 of 51 px) for 292 unknowns, a fit
-# as loosely constrained as test01's, where FP32 storage of W alone moves the
-# difference image by ~1e-3 sigma: it keeps test01's 1e-2 bar.  On the
-# 437 x 611 frame the two modes' solutions differ by 3.7e-4 (relative) and
-# the spatial kernel polynomial, extrapolated to a bright star 17 px from the
-# bottom edge, turns that into 1.17e-3 sigma there (6.9e-4 in the interior,
-# rms 5.4e-5): 2e-3.
-SIGMA_BAR = {"wide": 2e-3, "tall": 1e-3, "small": 1e-2}
+# as loosely constrained as test01's; the 437 x 611 frame extrapolates the
+# spatial kernel polynomial to a bright star 17 px from its bottom edge.  Both
+# are where W's precision shows, and both are held to 1e-3 sigma.
+SIGMA_BAR = {"wide": 1e-3, "tall": 1e-3, "small": 1e-3}
 
 
 def _bits(a):

@@ -300,6 +300,7 @@ void stageCmv(xb_ctx* c) {
     const std::string sfx = std::to_string(si);
     if(mixedMode(c)) {
       S.Wf = buf<float>(c, "Wf" + sfx, (size_t)std::max(S.n, 1) * g.wRows * mixedLd(g));
+      S.Wlo = buf<float>(c, "Wlo" + sfx, (size_t)std::max(S.n, 1) * g.wRows * mixedLd(g));
       S.dots = buf<double>(c, "dots" + sfx, (size_t)std::max(S.n, 1) * mixedDotStride(g));
     } else {
       S.W = buf<double>(c, "W" + sfx, (size_t)std::max(S.n, 1) * g.wRows * g.wCols);
@@ -320,8 +321,10 @@ void stageCmv(xb_ctx* c) {
       const std::string sfx = std::to_string(si);
       c->put("Q" + sfx, toHost(c, S.Q, (size_t)S.n * g.qCount * g.qCount));
       c->put("B" + sfx, toHost(c, S.B, (size_t)S.n * g.bCount));
-      if(mixedMode(c))
+      if(mixedMode(c)) {
         c->put("Wf" + sfx, toHost(c, S.Wf, (size_t)S.n * g.wRows * mixedLd(g)));
+        c->put("Wlo" + sfx, toHost(c, S.Wlo, (size_t)S.n * g.wRows * mixedLd(g)));
+      }
       else
         c->put("W" + sfx, toHost(c, (const double*)S.W, (size_t)S.n * g.wRows * g.wCols));
     }

@@ -76,7 +76,8 @@ struct StampSetDev {
   void* W = nullptr;         // n * wRows * wCols (double or float)
   double* Q = nullptr;       // n * qCount^2
   double* B = nullptr;       // n * bCount
-  float* Wf = nullptr;       // mixed mode: FP32 W [n][wRows][ld], ld = wCols padded to 32
+  float* Wf = nullptr;       // mixed mode: W [n][wRows][ld] as hi + lo floats, ld = wCols
+  float* Wlo = nullptr;      //   padded to 32 (Wf the hi parts, Wlo the lo parts)
   double* dots = nullptr;    // mixed mode: per-stamp dot table of the global matrix
   double* omega = nullptr;   // plain mode, weighted fit: n * wCols pixel weights 1 / sigma^2
   const int* dN = nullptr;   // frame graphs: the kept count on the device (n is its bound)

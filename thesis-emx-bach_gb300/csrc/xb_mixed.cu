@@ -37,7 +37,54 @@ __device__ __forceinline__ float floatNormF(int x, int w) {
   return ((float)x - hw) / hw;
 }
 
-// ------------------------------------------------------------ W in FP32 ---
+// -------------------------------------------------- W as an FP32 pair ---
+// The normal matrices are ill-conditioned enough that a W rounded to FP32
+// (2^-24 per element) moves the difference image of the reference's own
+// test case (cond ~6e13) by ~1e-3 of the pixel noise.  So W is kept as an
+// unevaluated sum hi + lo of two floats (~48 bits), computed on the FP32 pipe
+// (GB300's FP64 rate is 1/64 of FP32) with error-free transformations; the
+// library is built without FMA contraction, so the two-sums below are exact.
+//   * Y pass (convStampY, cl_kern/cmv.cl:70-106): the reference accumulates
+//     in float over FP64 products, v = (float)((double)v + img * fy), and
+//     the rounding of every step is part of its result.  It is reproduced:
+//     fy = fh + fl as floats, img*fh split exactly by an FMA, the sum
+//     v + product formed exactly (two-sum) and rounded once to float.  The
+//     result equals the reference's except when v + product lies within
+//     ~2^-47 of a float rounding boundary (~1 step in 10^7).
+//   * X pass (convStampX, :108-135, FP64 there): double-float accumulation.
+//   * convStampOdd (:137-154): W[n] - W[0] as a double-float difference.
+//   * convStampBg (:156-193): FP64, split into hi + lo.
+__device__ __forceinline__ float refStepY(float v, float a, float fh, float fl) {
+  const float ph = a * fh;
+  const float pe = fmaf(a, fh, -ph);  // a*fh = ph + pe exactly
+  const float pl = a * fl;
+  const float s = v + ph;             // two-sum: v + ph = s + e exactly
+  const float bb = s - v;
+  const float e = (v - (s - bb)) + (ph - bb);
+  return s + (e + (pe + pl));
+}
+// (sh, sl) += t * (fh + fl)
+__device__ __forceinline__ void dfAccum(float& sh, float& sl, float t, float fh, float fl) {
+  const float ph = t * fh;
+  const float pe = fmaf(t, fh, -ph);
+  const float s = sh + ph;
+  const float bb = s - sh;
+  const float e = (sh - (s - bb)) + (ph - bb);
+  sh = s;
+  sl += e + (pe + t * fl);
+}
+// renormalised hi + lo of sh + sl
+__device__ __forceinline__ void dfNorm(float sh, float sl, float& hi, float& lo) {
+  const float s = sh + sl;
+  const float bb = s - sh;
+  hi = s;
+  lo = (sh - (s - bb)) + (sl - bb);
+}
+__device__ __forceinline__ void splitF64(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
 // One CTA per (stamp, group of basis functions sharing a Y filter).
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
@@ -46,7 +93,7 @@ __global__ void __launch_bounds__(MX_THREADS)
                  const int2* __restrict__ ssxy, int maxSS, const double* __restrict__ fX,
                  const double* __restrict__ fY, const int* __restrict__ gStart,
                  const int* __restrict__ gMembers, int hSS, int hK, int wRows, int ldW,
-                 float* __restrict__ W) {
+                 float* __restrict__ W, float* __restrict__ Wlo) {
   extern __shared__ float fw_s[];
   if(liveN && (int)blockIdx.x >= *liveN) return;
   const int s = list[blockIdx.x], gi = blockIdx.y, tid = threadIdx.x;
@@ -54,19 +101,25 @@ __global__ void __launch_bounds__(MX_THREADS)
   const int xHalf = hSS + hK, tw = 2 * xHalf + 1, th = fSS;
   const int m0 = gStart[gi], m1 = gStart[gi + 1];
   float* Ws = W + (size_t)s * wRows * ldW;
+  float* Wl = Wlo + (size_t)s * wRows * ldW;
   const bool live = cur[s] < count[s];
   if(!live) {
     for(int m = m0; m < m1; m++)
-      for(int p = tid; p < ldW; p += MX_THREADS) Ws[(size_t)gMembers[m] * ldW + p] = 0.f;
+      for(int p = tid; p < ldW; p += MX_THREADS) {
+        Ws[(size_t)gMembers[m] * ldW + p] = 0.f;
+        Wl[(size_t)gMembers[m] * ldW + p] = 0.f;
+      }
     return;
   }
   const int2 c = ssxy[(size_t)s * maxSS + cur[s]];
   float* win = fw_s;              // tw * tw
   float* tmp = win + tw * tw;     // th * tw
-  float* fy = tmp + th * tw;      // fK
-  float* fx = fy + fK;            // fK
+  float* fyh = tmp + th * tw;     // fK
+  float* fyl = fyh + fK;          // fK
+  float* fxh = fyl + fK;          // fK
+  float* fxl = fxh + fK;          // fK
   const int n0 = gMembers[m0];
-  for(int i = tid; i < fK; i += MX_THREADS) fy[i] = (float)fY[(size_t)n0 * fK + i];
+  for(int i = tid; i < fK; i += MX_THREADS) splitF64(fY[(size_t)n0 * fK + i], fyh[i], fyl[i]);
   for(int i = tid; i < tw * tw; i += MX_THREADS) {
     int gx = min(max(c.x - xHalf + i % tw, 0), w - 1);
     int gy = min(max(c.y - xHalf + i / tw, 0), h - 1);
@@ -77,38 +130,42 @@ __global__ void __launch_bounds__(MX_THREADS)
     const int row = p / tw, col = p % tw;
     float v = 0.f;
 #pragma unroll 7
-    for(int y = -hK; y <= hK; y++) v = fmaf(win[(row + hK + y) * tw + col], fy[hK - y], v);
+    for(int y = -hK; y <= hK; y++) v = refStepY(v, win[(row + hK + y) * tw + col], fyh[hK - y], fyl[hK - y]);
     tmp[p] = v;
   }
   for(int m = m0; m < m1; m++) {
     const int n = gMembers[m];
     __syncthreads();
-    for(int i = tid; i < fK; i += MX_THREADS) fx[i] = (float)fX[(size_t)n * fK + i];
+    for(int i = tid; i < fK; i += MX_THREADS) splitF64(fX[(size_t)n * fK + i], fxh[i], fxl[i]);
     __syncthreads();
     for(int p = tid; p < ldW; p += MX_THREADS) {
-      float w0 = 0.f;
+      float hi = 0.f, lo = 0.f;
       if(p < wCols) {
         const int row = p / fSS, ii = p % fSS;
+        float sh = 0.f, sl = 0.f;
 #pragma unroll 7
-        for(int x = -hK; x <= hK; x++) w0 = fmaf(tmp[row * tw + ii + x + hK], fx[hK - x], w0);
+        for(int x = -hK; x <= hK; x++) dfAccum(sh, sl, tmp[row * tw + ii + x + hK], fxh[hK - x], fxl[hK - x]);
+        dfNorm(sh, sl, hi, lo);
       }
-      Ws[(size_t)n * ldW + p] = w0;
+      Ws[(size_t)n * ldW + p] = hi;
+      Wl[(size_t)n * ldW + p] = lo;
     }
   }
 }
 
-// convStampOdd and convStampBg in FP32; pads the background rows.
+// convStampOdd and convStampBg on the hi + lo pair; pads the background rows.
 __global__ void __launch_bounds__(MX_THREADS)
     k_fill_finish_f32(const int* __restrict__ list, const int* __restrict__ liveN,
                       const int* __restrict__ count,
                       const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                       const int* __restrict__ kx, const int* __restrict__ ky, int nPSF,
                       const int2* __restrict__ bgXY, int nBG, int hSS, int w, int h, int wRows,
-                      int ldW, float* __restrict__ W) {
+                      int ldW, float* __restrict__ W, float* __restrict__ Wlo) {
   if(liveN && (int)blockIdx.x >= *liveN) return;
   const int s = list[blockIdx.x], tid = threadIdx.x;
   const int fSS = 2 * hSS + 1, wCols = fSS * fSS;
   float* Ws = W + (size_t)s * wRows * ldW;
+  float* Wl = Wlo + (size_t)s * wRows * ldW;
   const bool live = cur[s] < count[s];
   // W[n] -= W[0] for the even/even rows: each thread takes its pixels
   // through all such rows (independent loads in flight, not one pass per row)
@@ -123,34 +180,49 @@ __global__ void __launch_bounds__(MX_THREADS)
   __syncthreads();
   const int ne = nEven;
   for(int p = tid; p < wCols; p += MX_THREADS) {
-    const float w0 = Ws[p];
-#pragma unroll 8
-    for(int e = 0; e < ne; e++) Ws[(size_t)evenRows[e] * ldW + p] -= w0;
+    const float bh = Ws[p], bl = Wl[p];
+#pragma unroll 4
+    for(int e = 0; e < ne; e++) {
+      const size_t i = (size_t)evenRows[e] * ldW + p;
+      const float ah = Ws[i], al = Wl[i];
+      const float s = ah - bh;  // two-sum of ah and -bh
+      const float bb = s - ah;
+      const float er = (ah - (s - bb)) + (-bh - bb);
+      float hi, lo;
+      dfNorm(s, er + (al - bl), hi, lo);
+      Ws[i] = hi;
+      Wl[i] = lo;
+    }
   }
   int2 c = make_int2(0, 0);
   if(live) c = ssxy[(size_t)s * maxSS + cur[s]];
   for(int b = 0; b < nBG; b++)
     for(int p = tid; p < ldW; p += MX_THREADS) {
-      float a = 0.f;
+      double a = 0.0;
       if(live && p < wCols) {
-        const float xf = floatNormF(c.x - hSS + p % fSS, w), yf = floatNormF(c.y - hSS + p / fSS, h);
-        float ax = 1.f, ay = 1.f;
+        // the reference's form: float-normalised coordinates, FP64 powers
+        const double xf = (double)floatNormF(c.x - hSS + p % fSS, w);
+        const double yf = (double)floatNormF(c.y - hSS + p / fSS, h);
+        double ax = 1.0, ay = 1.0;
         for(int i = 0; i < bgXY[b].x; i++) ax *= xf;
         for(int i = 0; i < bgXY[b].y; i++) ay *= yf;
         a = ax * ay;
       }
-      Ws[(size_t)(nPSF + b) * ldW + p] = a;
+      float hi, lo;
+      splitF64(a, hi, lo);
+      Ws[(size_t)(nPSF + b) * ldW + p] = hi;
+      Wl[(size_t)(nPSF + b) * ldW + p] = lo;
     }
 }
 
 // ------------------------------------------------------------------ Gram ---
-// G = X X^T with X = [W rows; image row] over the substamp pixels.  The
-// products of two FP32 values are exact in FP64 and are accumulated in FP64:
-// the normal matrices are ill-conditioned (cond ~1e14), and an FP32
-// accumulation moves the fitted kernel sum by up to 9 %, while FP32 storage of
-// W itself (a consistent design matrix) moves it by ~1e-7.  Each stamp's
-// lower triangle is split over gridDim.y CTAs; k_gram_scatter then fills Q
-// (createQ), B (createB) and the global-matrix dot table.
+// G = X X^T with X = [W rows; image row] over the substamp pixels, on the
+// CUDA cores in FP64 (the weighted fit and shapes beyond the tensor-core
+// kernel).  Each W element hi + lo is exact in FP64; the normal matrices are
+// ill-conditioned (cond ~1e14), and an FP32 accumulation moves the fitted
+// kernel sum by up to 9 %.  Each stamp's lower triangle is split over
+// gridDim.y CTAs; k_gram_scatter then fills Q (createQ), B (createB) and the
+// global-matrix dot table.
 constexpr int GM_KT = 32, GM_SPLIT = 6;
 template <class T>
 __global__ void __launch_bounds__(MX_THREADS)
@@ -158,8 +230,8 @@ __global__ void __launch_bounds__(MX_THREADS)
                  const int* __restrict__ list,
                  const int* __restrict__ liveN, const int* __restrict__ count, const int* __restrict__ cur,
                  const int2* __restrict__ ssxy, int maxSS, int hSS, int wRows, int ldW,
-                 const float* __restrict__ W, double* __restrict__ Gout, int weighted,
-                 double invGain, double rn2x2) {
+                 const float* __restrict__ W, const float* __restrict__ Wlo,
+                 double* __restrict__ Gout, int weighted, double invGain, double rn2x2) {
   extern __shared__ double gm_s[];
   __shared__ double omT[GM_KT];  // pixel weights of the tile (weighted fit)
   if(liveN && (int)blockIdx.x >= *liveN) return;
@@ -169,6 +241,7 @@ __global__ void __launch_bounds__(MX_THREADS)
   const int per = (nEnt + gridDim.y - 1) / gridDim.y, e0 = blockIdx.y * per;
   double* tile = gm_s;  // R x (GM_KT + 1)
   const float* Ws = W + (size_t)s * wRows * ldW;
+  const float* Wl = Wlo + (size_t)s * wRows * ldW;
   const bool live = cur[s] < count[s];
   int2 c = make_int2(0, 0);
   if(live) c = ssxy[(size_t)s * maxSS + cur[s]];
@@ -186,18 +259,18 @@ __global__ void __launch_bounds__(MX_THREADS)
     const int kt = min(GM_KT, wCols - k0);
     for(int i = tid; i < R * GM_KT; i += MX_THREADS) {
       const int r = i / GM_KT, kk = i % GM_KT;
-      float v = 0.f;
+      double v = 0.0;
       if(kk < kt) {
         if(r < wRows) {
-          v = Ws[(size_t)r * ldW + k0 + kk];
+          v = (double)Ws[(size_t)r * ldW + k0 + kk] + (double)Wl[(size_t)r * ldW + k0 + kk];
         } else if(live) {
           const int k = k0 + kk;
           const int gx = min(max(c.x - hSS + k % fSS, 0), w - 1);
           const int gy = min(max(c.y - hSS + k / fSS, 0), h - 1);
-          v = (float)other[(size_t)gx + (size_t)gy * w];
+          v = (double)(float)other[(size_t)gx + (size_t)gy * w];
         }
       }
-      tile[r * (GM_KT + 1) + kk] = (double)v;
+      tile[r * (GM_KT + 1) + kk] = v;
     }
     if(weighted && tid < GM_KT) {
       double v = 0.0;
@@ -1205,7 +1278,7 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
   const int ldW = mixedLd(g);
   const int nGroups = (int)c->basis.yGroupStart.size() - 1;
   const int tw = 2 * (g.hSS + g.hK) + 1, th = g.fSS;
-  const size_t smemFill = (size_t)(tw * tw + th * tw + 2 * g.fK) * sizeof(float);
+  const size_t smemFill = (size_t)(tw * tw + th * tw + 4 * g.fK) * sizeof(float);
   const int other = 1 - imgConv;
   {
     KT_SCOPE(c, "fill_w");
@@ -1213,18 +1286,20 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     if(c->imgIsF64)
       k_fill_w_f32<double><<<grid, MX_THREADS, smemFill, c->stream>>>(
           (const double*)c->img[imgConv], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy,
-          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf,
+          S.Wlo);
     else
       k_fill_w_f32<float><<<grid, MX_THREADS, smemFill, c->stream>>>(
           (const float*)c->img[imgConv], c->w, c->h, dList, liveN, S.count, S.cur, S.ssxy,
-          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf);
+          g.maxSS, c->dFX, c->dFY, c->dYGroupStart, c->dYGroupMembers, g.hSS, g.hK, g.wRows, ldW, S.Wf,
+          S.Wlo);
     XB_LAUNCHED(c);
   }
   {
     KT_SCOPE(c, "fill_finish");
     k_fill_finish_f32<<<nList, MX_THREADS, 0, c->stream>>>(
         dList, liveN, S.count, S.cur, S.ssxy, g.maxSS, c->dKx, c->dKy, g.nPSF, buf<int2>(c, "bgXY", g.nBG),
-        g.nBG, g.hSS, c->w, c->h, g.wRows, ldW, S.Wf);
+        g.nBG, g.hSS, c->w, c->h, g.wRows, ldW, S.Wf, S.Wlo);
     XB_LAUNCHED(c);
   }
   {
@@ -1240,12 +1315,12 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
     } else if(c->imgIsF64)
       k_gram_mixed<double><<<grid, MX_THREADS, smem, c->stream>>>(
           (const double*)c->img[other], (const double*)c->img[imgConv], c->w, c->h, dList, liveN,
-          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, G, c->p.fitWeighted,
+          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, S.Wlo, G, c->p.fitWeighted,
           noiseInvGain(c->p), noiseRn2x2(c->p));
     else
       k_gram_mixed<float><<<grid, MX_THREADS, smem, c->stream>>>(
           (const float*)c->img[other], (const float*)c->img[imgConv], c->w, c->h, dList, liveN,
-          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, G, c->p.fitWeighted,
+          S.count, S.cur, S.ssxy, g.maxSS, g.hSS, g.wRows, ldW, S.Wf, S.Wlo, G, c->p.fitWeighted,
           noiseInvGain(c->p), noiseRn2x2(c->p));
     XB_LAUNCHED(c);
     k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, liveN, S.count, S.cur, g.wRows,
