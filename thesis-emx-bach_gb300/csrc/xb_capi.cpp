@@ -168,6 +168,22 @@ int xb_ctx_create(const xb_params* p, int device, xb_ctx** out) {
     toDevice(c, c->dYGroupMembers, b.yGroupMembers);
     toDevice(c, c->dKx, b.kx);
     toDevice(c, c->dKy, b.ky);
+    {
+      const int fK = c->g.fK, nPSF = c->g.nPSF, nG = (int)b.yGroupStart.size() - 1;
+      std::vector<float> fs((size_t)2 * (nPSF + nG) * fK);
+      auto split = [&](double v, float& hi, float& lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+      };
+      for(int i = 0; i < nPSF * fK; i++) split(b.fX[i], fs[i], fs[(size_t)nPSF * fK + i]);
+      float* fy = fs.data() + (size_t)2 * nPSF * fK;
+      for(int gi = 0; gi < nG; gi++)
+        for(int k = 0; k < fK; k++)
+          split(b.fY[(size_t)b.yGroupMembers[b.yGroupStart[gi]] * fK + k], fy[gi * fK + k],
+                fy[(size_t)nG * fK + gi * fK + k]);
+      c->dFSplit = buf<float>(c, "fSplit", fs.size());
+      toDevice(c, c->dFSplit, fs);
+    }
     XB_CUDA(cudaStreamSynchronize(c->stream));
   });
   if(rc != XB_OK) {
@@ -232,6 +248,10 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->kt.total.clear();
   } else if(n == "gram_fp64") {
     c->gramFp64 = value != 0;
+  } else if(n == "fill_gram") {
+    c->fillGram = value != 0;
+  } else if(n == "fill_gram_tma") {
+    c->fillGramTma = value != 0;
   } else if(n == "ldl_panel") {
     c->ldlPanel = value != 0;
   } else if(n == "ldl_cluster") {

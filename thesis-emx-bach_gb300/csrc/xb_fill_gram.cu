@@ -1,0 +1,471 @@
+// xb_fill_gram.cu — the mixed path's substamp fill and its exact tensor-core
+// Gram matrix in one kernel, one CTA per stamp.
+//
+// For the common shapes it replaces three launches (k_fill_w_f32 ->
+// k_fill_finish_f32 -> k_gram_tc) that passed W through HBM: the separate
+// fill wrote W (hi and lo, 412 KB per stamp at 49 basis functions) and the
+// Gram read it back after every other stamp's fill had pushed it out of L2.
+// Here one CTA runs, for its stamp,
+//   1. the 51 x 51 window (substamp + kernel half-width on each side) from
+//      the image into shared memory with one TMA tile copy
+//      (cp.async.bulk.tensor.2d, completion on an mbarrier) when the window
+//      lies inside the frame and the frame's rows are 16-byte multiples, else
+//      with clamped loads (the reference clamps at the edge);
+//   2. the Y pass of every unique Y filter (convStampY, cl_kern/cmv.cl:70-106)
+//      into shared memory, eight output rows per thread from one sliding
+//      column of the window, the filter in registers;
+//   3. the X pass of every basis function (convStampX, :108-135), eight
+//      output pixels per thread from one sliding row, the even/even
+//      subtraction (convStampOdd, :137-154) against W[0] kept in shared
+//      memory, the background rows (convStampBg, :156-193) and the image row
+//      of createB (:218-248); W goes to global memory (hi for the chi^2 of
+//      k_sigs_f32, lo as scratch for step 4) while each row's largest |hi|
+//      is collected;
+//   4. the exact sliced Gram of xb_tc.cuh: the CTA's own W comes back from L2
+//      chunk by chunk, is sliced with the row exponents into BF16 digits and
+//      multiplied by tcgen05.mma into TMEM; the int64 epilogue writes G.
+// The arithmetic of steps 2-3 is that of the separate kernels (xb_df.cuh,
+// same operations in the same order) and step 4 is the same code, so G and W
+// are theirs bit for bit (tests/test_gpu_fill_gram.py).
+//
+// Limits (else the separate kernels run): FP32 images, kernel half-width 10
+// (the filter loops are unrolled for 21 taps), substamps up to 31 x 31,
+// R = basis + background + 1 <= 64 rows, background order <= 2 (its values
+// are then exact products of two floats), no weighted fit.
+#include <cuda.h>
+
+#include "xb_df.cuh"
+#include "xb_internal.h"
+#include "xb_tc.cuh"
+
+namespace xb {
+
+namespace {
+
+constexpr int FG_THREADS = 512;
+constexpr int FG_HK = 10;  // the kernel half-width the fused kernel is built for
+constexpr int FG_R8 = 8;   // outputs per thread item (rows of the Y pass, pixels of the X pass)
+
+// Shared-memory layout of the fill (steps 1-3); the Gram (step 4) and the
+// epilogue reuse the same area from offset 0.
+struct FgLayout {
+  int tw, fSS, ldWin, winRows, ldY;
+  size_t oWin, oFy, oFx, oY, oW0, fill, total;
+};
+__host__ __device__ inline FgLayout fgLayout(int hSS, int hK, int nGroups, int nPSF) {
+  FgLayout L;
+  L.fSS = 2 * hSS + 1;
+  L.tw = L.fSS + 2 * hK;
+  L.ldWin = (L.tw + 3 + 3) / 4 * 4;   // TMA box width: 16-byte rows, room for the x offset
+  L.winRows = L.tw + FG_R8;           // rows past tw are read only by discarded outputs
+  L.ldY = L.tw + FG_R8;               // odd stride: the X items' rows fall on distinct banks
+  if(L.ldY % 2 == 0) L.ldY++;
+  const int fK = 2 * hK + 1;
+  auto al = [](size_t v) { return (v + 127) / 128 * 128; };
+  L.oWin = 0;
+  L.oFy = al(L.oWin + (size_t)L.ldWin * L.winRows * 4);
+  L.oFx = al(L.oFy + (size_t)2 * nGroups * fK * 4);
+  L.oY = al(L.oFx + (size_t)2 * nPSF * fK * 4);
+  L.oW0 = al(L.oY + (size_t)nGroups * L.fSS * L.ldY * 4);
+  L.fill = al(L.oW0 + (size_t)2 * L.fSS * L.fSS * 4);
+  size_t m = L.fill;
+  if((size_t)tc::CHUNK_SMEM > m) m = tc::CHUNK_SMEM;
+  if((size_t)tc::EPI_BYTES > m) m = tc::EPI_BYTES;
+  L.total = m + 1024;  // 1024-byte alignment of the operand buffers
+  return L;
+}
+
+struct FillGramArgs {
+  const float* conv;   // the image whose substamps are convolved
+  const float* other;  // the image of createB's target row
+  int w, h;
+  const int* list;
+  const int* liveN;
+  const int* count;
+  const int* cur;
+  const int2* ssxy;
+  int maxSS;
+  const float* fSplit;  // the filters as float pairs (xb_ctx::dFSplit)
+  const int* gStart;    // unique Y filters: members gMembers[gStart[g] .. gStart[g+1])
+  const int* gMembers;
+  int nGroups, g0;      // g0: the group of basis function 0
+  const int* kx;
+  const int* ky;
+  int nPSF;
+  const int2* bgXY;
+  int nBG;
+  int hSS, wRows, ldW;
+  int useTma;
+  float* W;    // [stamp][wRows][ldW] hi
+  float* Wlo;  // [stamp][wRows][ldW] lo
+  double* G;   // [list entry][R][R]
+  int* timeout;
+};
+
+// Y pass, 8 consecutive output rows of one window column: v[j] is the
+// reference's float accumulation over taps t = 0..FK-1 (window row j + t,
+// filter entry FK-1-t), in that order.  The tap loop is not unrolled (eight
+// independent chains per tap keep the FP32 pipe busy; small code keeps the
+// instruction cache warm); ld is the window's row stride.
+template <int FK>
+__device__ __forceinline__ void yPass8(const float* wp, int ld, const float* fh, const float* fl,
+                                       float (&v)[FG_R8]) {
+#pragma unroll
+  for(int j = 0; j < FG_R8; j++) v[j] = 0.f;
+#pragma unroll 1
+  for(int t = 0; t < FK; t++) {
+    const float h = fh[FK - 1 - t], l = fl[FK - 1 - t];
+    const float* p = wp + t * ld;
+#pragma unroll
+    for(int j = 0; j < FG_R8; j++) v[j] = df::refStepY(v[j], p[j * ld], h, l);
+  }
+}
+// X pass, 8 consecutive output pixels of one row: the double-float sum over
+// taps t = 0..FK-1 (Y-pass value j + t, filter entry FK-1-t), in that order.
+template <int FK>
+__device__ __forceinline__ void xPass8(const float* yp, const float* fh, const float* fl,
+                                       float (&hi)[FG_R8], float (&lo)[FG_R8]) {
+  float sh[FG_R8], sl[FG_R8];
+#pragma unroll
+  for(int j = 0; j < FG_R8; j++) sh[j] = sl[j] = 0.f;
+#pragma unroll 1
+  for(int t = 0; t < FK; t++) {
+    const float h = fh[FK - 1 - t], l = fl[FK - 1 - t];
+#pragma unroll
+    for(int j = 0; j < FG_R8; j++) df::dfAccum(sh[j], sl[j], yp[t + j], h, l);
+  }
+#pragma unroll
+  for(int j = 0; j < FG_R8; j++) df::dfNorm(sh[j], sl[j], hi[j], lo[j]);
+}
+
+__device__ __forceinline__ void maxBits(unsigned* slot, float m) {
+  atomicMax(slot, __float_as_uint(m));  // m >= 0: the bit patterns are ordered
+}
+
+__global__ void __launch_bounds__(FG_THREADS, 1)
+    k_fill_gram(const __grid_constant__ CUtensorMap tmap, const FillGramArgs a) {
+  using namespace tc;
+  constexpr int HK = FG_HK, FK = 2 * HK + 1;
+  extern __shared__ __align__(1024) unsigned char fg_s[];
+  __shared__ float imgRow[1024];  // K <= 961 pixels, padded to whole chunks
+  __shared__ int expo[RB];
+  __shared__ unsigned rowMax[RB];
+  __shared__ unsigned char evenRow[MAX_NPSF];
+  __shared__ unsigned char groupOf[MAX_NPSF];
+  __shared__ unsigned long long bars[3];  // two operand buffers, the window copy
+  __shared__ uint32_t tmemBase;
+  if(a.liveN && (int)blockIdx.x >= *a.liveN) return;  // before any barrier or TMEM allocation
+  const int t = blockIdx.x, s = a.list[t], tid = threadIdx.x, warp = tid >> 5;
+  const int fSS = 2 * a.hSS + 1, K = fSS * fSS, R = a.wRows + 1, nPSF = a.nPSF;
+  const int ldW = a.ldW;
+  float* Ws = a.W + (size_t)s * a.wRows * ldW;
+  float* Wl = a.Wlo + (size_t)s * a.wRows * ldW;
+  double* Gs = a.G + (size_t)t * R * R;
+  if(!(a.cur[s] < a.count[s])) {
+    // no substamp left: W and G are zero (what the separate kernels give)
+    for(int i = tid; i < a.wRows * ldW; i += FG_THREADS) {
+      Ws[i] = 0.f;
+      Wl[i] = 0.f;
+    }
+    for(int i = tid; i < R * R; i += FG_THREADS) Gs[i] = 0.0;
+    return;
+  }
+  const unsigned long long deadline = timerNs() + WAIT_NS;
+  unsigned char* buf = (unsigned char*)(((uintptr_t)fg_s + 1023) & ~(uintptr_t)1023);
+  const FgLayout L = fgLayout(a.hSS, HK, a.nGroups, nPSF);
+  const int tw = L.tw, ldWin = L.ldWin, ldY = L.ldY;
+  float* win = (float*)(buf + L.oWin);
+  float* fyh = (float*)(buf + L.oFy);
+  float* fyl = fyh + a.nGroups * FK;
+  float* fxh = (float*)(buf + L.oFx);
+  float* fxl = fxh + nPSF * FK;
+  float* ytmp = (float*)(buf + L.oY);
+  float* w0h = (float*)(buf + L.oW0);
+  float* w0l = w0h + K;
+
+  const int2 c = a.ssxy[(size_t)s * a.maxSS + a.cur[s]];
+  const int xHalf = a.hSS + HK, wx0 = c.x - xHalf, wy0 = c.y - xHalf;
+  const bool tma = a.useTma && wx0 >= 0 && wy0 >= 0 && wx0 + tw <= a.w && wy0 + tw <= a.h;
+  const int x0 = wx0 & ~3;              // 16-byte aligned start of the TMA box
+  const int dx = tma ? wx0 - x0 : 0;    // window column 0 in the staged rows
+  const uint32_t winBar = smemU32(&bars[2]);
+  if(tid == 0) {
+    barInit(smemU32(&bars[0]), 1);
+    barInit(smemU32(&bars[1]), 1);
+    barInit(winBar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if(tma) {
+      const uint32_t bytes = (uint32_t)(ldWin * tw * 4);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(winBar), "r"(bytes)
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+          " [%0], [%1, {%2, %3}], [%4];" ::"r"(smemU32(win)),
+          "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x0), "r"(wy0), "r"(winBar)
+          : "memory");
+    }
+  }
+  // filters (hi + lo), basis tables, row maxima; the window by plain loads
+  // when TMA does not apply
+  // the filters as float pairs: X [nPSF][FK] hi, lo; Y [group][FK] hi, lo
+  for(int i = tid; i < nPSF * FK; i += FG_THREADS) {
+    fxh[i] = a.fSplit[i];
+    fxl[i] = a.fSplit[nPSF * FK + i];
+  }
+  for(int i = tid; i < a.nGroups * FK; i += FG_THREADS) {
+    fyh[i] = a.fSplit[2 * nPSF * FK + i];
+    fyl[i] = a.fSplit[(2 * nPSF + a.nGroups) * FK + i];
+  }
+  for(int n = tid; n < nPSF; n += FG_THREADS)
+    evenRow[n] = (n > 0 && a.kx[n] % 2 == 0 && a.ky[n] % 2 == 0) ? 1 : 0;
+  for(int g = tid; g < a.nGroups; g += FG_THREADS)
+    for(int m = a.gStart[g]; m < a.gStart[g + 1]; m++) groupOf[a.gMembers[m]] = (unsigned char)g;
+  if(tid < RB) rowMax[tid] = 0u;
+  if(!tma) {
+    for(int i = tid; i < tw * tw; i += FG_THREADS) {
+      const int gx = min(max(wx0 + i % tw, 0), a.w - 1);
+      const int gy = min(max(wy0 + i / tw, 0), a.h - 1);
+      win[(i / tw) * ldWin + i % tw] = a.conv[(size_t)gx + (size_t)gy * a.w];
+    }
+  }
+  __syncthreads();  // barrier inits and the tables before any wait or use
+  bool ok = true;
+  if(tma) {
+    int late = 0;
+    if(!waitUntil(winBar, 0, deadline)) {
+      late = 1;
+      waitUntil(winBar, 0, timerNs() + WAIT_NS);  // the copy in flight gets a second chance
+    }
+    ok = __syncthreads_or(late) == 0;
+  }
+
+  // ---- Y pass: item (group, block of 8 output rows, window column) ----------
+  const int nRB = (fSS + FG_R8 - 1) / FG_R8;
+  auto yItem = [&](int g, int rb, int col) {
+    const int r0 = rb * FG_R8;
+    float v[FG_R8];
+    yPass8<FK>(win + r0 * ldWin + col + dx, ldWin, fyh + g * FK, fyl + g * FK, v);
+    float* yo = ytmp + ((size_t)g * fSS + r0) * ldY + col;
+#pragma unroll
+    for(int j = 0; j < FG_R8; j++)
+      if(r0 + j < fSS) yo[j * ldY] = v[j];
+  };
+  // ---- X pass: item (basis function, output row, block of 8 pixels) ----------
+  const int nXB = (fSS + FG_R8 - 1) / FG_R8;
+  auto xItem = [&](int n, int row, int xb, float (&hi)[FG_R8], float (&lo)[FG_R8]) {
+    xPass8<FK>(ytmp + ((size_t)groupOf[n] * fSS + row) * ldY + xb * FG_R8, fxh + n * FK,
+               fxl + n * FK, hi, lo);
+  };
+  // stores 8 outputs of row n starting at pixel p0 (nv of them valid) and
+  // folds their largest |hi| into the row maximum
+  auto putRow = [&](int n, int p0, int nv, const float (&hi)[FG_R8], const float (&lo)[FG_R8]) {
+    float m = 0.f;
+#pragma unroll
+    for(int j = 0; j < FG_R8; j++)
+      if(j < nv) {
+        Ws[(size_t)n * ldW + p0 + j] = hi[j];
+        Wl[(size_t)n * ldW + p0 + j] = lo[j];
+        m = fmaxf(m, fabsf(hi[j]));  // NaN is skipped, as in the separate Gram
+      }
+    maxBits(&rowMax[n], m);
+  };
+
+  // list A: the Y pass of basis function 0's filter
+  for(int it = tid; it < nRB * tw; it += FG_THREADS) yItem(a.g0, it / tw, it % tw);
+  __syncthreads();
+  // list B: W[0] (kept in shared memory for the even/even rows), and the Y
+  // pass of every other filter
+  {
+    const int nX0 = fSS * nXB, nYo = (a.nGroups - 1) * nRB * tw;
+    for(int it = tid; it < nX0 + nYo; it += FG_THREADS) {
+      if(it < nX0) {
+        const int row = it / nXB, xb = it % nXB;
+        float hi[FG_R8], lo[FG_R8];
+        xItem(0, row, xb, hi, lo);
+        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+#pragma unroll
+        for(int j = 0; j < FG_R8; j++)
+          if(j < nv) {
+            w0h[p0 + j] = hi[j];
+            w0l[p0 + j] = lo[j];
+          }
+        putRow(0, p0, nv, hi, lo);
+      } else {
+        const int i = it - nX0, col = i % tw, rb = (i / tw) % nRB;
+        int g = i / (tw * nRB);
+        if(g >= a.g0) g++;
+        yItem(g, rb, col);
+      }
+    }
+  }
+  __syncthreads();
+  // list C: every other basis function, the background rows, the image row,
+  // and the zero padding of the W rows
+  {
+    const int nX = (nPSF - 1) * fSS * nXB, nB = a.nBG * fSS * nXB, nI = fSS * nXB;
+    for(int it = tid; it < nX + nB + nI; it += FG_THREADS) {
+      if(it < nX) {
+        const int n = 1 + it / (fSS * nXB), row = (it / nXB) % fSS, xb = it % nXB;
+        float hi[FG_R8], lo[FG_R8];
+        xItem(n, row, xb, hi, lo);
+        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+        if(evenRow[n]) {
+#pragma unroll
+          for(int j = 0; j < FG_R8; j++)
+            if(j < nv) df::dfSub(hi[j], lo[j], w0h[p0 + j], w0l[p0 + j], hi[j], lo[j]);
+        }
+        putRow(n, p0, nv, hi, lo);
+      } else if(it < nX + nB) {
+        // the reference's form: float-normalised coordinates, FP64 powers,
+        // each an exact product of at most two floats at background order <= 2
+        const int i = it - nX, b = i / (fSS * nXB), row = (i / nXB) % fSS, xb = i % nXB;
+        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+        const int ex = a.bgXY[b].x, ey = a.bgXY[b].y;
+        const float yf = df::floatNormF(c.y - a.hSS + row, a.h);
+        float hi[FG_R8], lo[FG_R8];
+#pragma unroll
+        for(int j = 0; j < FG_R8; j++) {
+          const float xf = df::floatNormF(c.x - a.hSS + ii0 + j, a.w);
+          float u = 1.f, v = 1.f;  // the two float factors
+          if(ex == 2) u = v = xf;
+          else if(ey == 2) u = v = yf;
+          else {
+            if(ex == 1) u = xf;
+            if(ey == 1) v = yf;
+          }
+          hi[j] = u * v;
+          lo[j] = fmaf(u, v, -hi[j]);  // exact: u v = hi + lo
+        }
+        putRow(nPSF + b, p0, nv, hi, lo);
+      } else {
+        const int i = it - nX - nB, row = i / nXB, xb = i % nXB;
+        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+        const int gy = min(max(c.y - a.hSS + row, 0), a.h - 1);
+        float m = 0.f;
+        for(int j = 0; j < nv; j++) {
+          const int gx = min(max(c.x - a.hSS + ii0 + j, 0), a.w - 1);
+          const float v = a.other[(size_t)gx + (size_t)gy * a.w];
+          imgRow[p0 + j] = v;
+          m = fmaxf(m, fabsf(v));
+        }
+        maxBits(&rowMax[a.wRows], m);
+      }
+    }
+    // zero padding: W columns K..ldW-1 and the image row up to whole chunks
+    const int padW = ldW - K, nChunkK = (K + KC - 1) / KC * KC;
+    for(int i = tid; i < a.wRows * padW; i += FG_THREADS) {
+      const size_t o = (size_t)(i / padW) * ldW + K + i % padW;
+      Ws[o] = 0.f;
+      Wl[o] = 0.f;
+    }
+    for(int k = K + tid; k < nChunkK; k += FG_THREADS) imgRow[k] = 0.f;
+  }
+  // the CTA's W stores before its own cp.async reads of them (step 4)
+  __syncthreads();
+  if(tid < RB) expo[tid] = tid < R ? rowExponent(__uint_as_float(rowMax[tid])) : 0;
+  if(warp == 0) tmemAlloc512(&tmemBase);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmemBase;
+  if(!gramChunks<FG_THREADS>(Ws, Wl, a.wRows, ldW, R, K, imgRow, expo, buf, bars, tmem, deadline))
+    ok = false;
+  epilogue(tmem, (long long*)buf, expo, R, Gs);
+  if(tid == 0 && !ok) atomicOr(a.timeout, 1);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so the
+// library has no link-time dependence on the driver library.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encodeTiled() {
+  static const EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+           cudaSuccess ||
+       q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (EncodeTiledFn)p;
+  }();
+  return fn;
+}
+
+}  // namespace
+
+bool fillGramFits(const xb_ctx* c) {
+  const Geo& g = c->g;
+  if(!c->fillGram || c->imgIsF64 || c->p.fitWeighted || c->gramFp64) return false;
+  if(g.hK != FG_HK || g.fSS > 31 || g.wRows + 1 > tc::RB || g.nPSF > MAX_NPSF) return false;
+  if(c->p.backgroundOrder > 2) return false;
+  const int nGroups = (int)c->basis.yGroupStart.size() - 1;
+  if(nGroups < 1 || nGroups > 255) return false;
+  int optin = 0;
+  if(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess)
+    return false;
+  // the static arrays of the kernel take ~5 KB beside the dynamic area
+  return fgLayout(g.hSS, g.hK, nGroups, g.nPSF).total + 8 * 1024 <= (size_t)optin;
+}
+
+void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv, double* G,
+                    const int* liveN) {
+  const Geo& g = c->g;
+  StampSetDev& S = c->set[si];
+  const int nGroups = (int)c->basis.yGroupStart.size() - 1;
+  int g0 = 0;
+  for(int gi = 0; gi < nGroups; gi++)
+    for(int m = c->basis.yGroupStart[gi]; m < c->basis.yGroupStart[gi + 1]; m++)
+      if(c->basis.yGroupMembers[m] == 0) g0 = gi;
+  const FgLayout L = fgLayout(g.hSS, g.hK, nGroups, g.nPSF);
+  FillGramArgs a{};
+  a.conv = (const float*)c->img[imgConv];
+  a.other = (const float*)c->img[1 - imgConv];
+  a.w = c->w;
+  a.h = c->h;
+  a.list = dList;
+  a.liveN = liveN;
+  a.count = S.count;
+  a.cur = S.cur;
+  a.ssxy = S.ssxy;
+  a.maxSS = g.maxSS;
+  a.fSplit = c->dFSplit;
+  a.gStart = c->dYGroupStart;
+  a.gMembers = c->dYGroupMembers;
+  a.nGroups = nGroups;
+  a.g0 = g0;
+  a.kx = c->dKx;
+  a.ky = c->dKy;
+  a.nPSF = g.nPSF;
+  a.bgXY = buf<int2>(c, "bgXY", g.nBG);
+  a.nBG = g.nBG;
+  a.hSS = g.hSS;
+  a.wRows = g.wRows;
+  a.ldW = mixedLd(g);
+  a.W = S.Wf;
+  a.Wlo = S.Wlo;
+  a.G = G;
+  a.timeout = deviceStatus(c) + 1;  // the context's device-timeout word
+  // the window's tile copy: rows of the frame in 16-byte multiples, box
+  // ldWin x tw floats (its x start is rounded down to 4 floats in the kernel)
+  CUtensorMap tm;
+  memset(&tm, 0, sizeof(tm));
+  a.useTma = 0;
+  const EncodeTiledFn enc = encodeTiled();
+  if(enc && c->w % 4 == 0 && ((uintptr_t)a.conv & 15) == 0) {
+    const cuuint64_t dims[2] = {(cuuint64_t)c->w, (cuuint64_t)c->h};
+    const cuuint64_t strides[1] = {(cuuint64_t)c->w * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)L.ldWin, (cuuint32_t)L.tw};
+    const cuuint32_t es[2] = {1, 1};
+    if(enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)a.conv, dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+      a.useTma = c->fillGramTma;
+  }
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_fill_gram, c->device));
+  k_fill_gram<<<nList, FG_THREADS, L.total, c->stream>>>(tm, a);
+  XB_LAUNCHED(c);
+}
+
+}  // namespace xb

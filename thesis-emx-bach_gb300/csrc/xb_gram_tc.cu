@@ -11,16 +11,8 @@ namespace xb {
 namespace {
 
 constexpr int GT_THREADS = 256;
-constexpr int GT_STAGE = tc::RB * tc::KC * 4;          // one FP32 W chunk (16 KB)
-constexpr int GT_DYN = 2 * tc::OPBUF + 4 * GT_STAGE;   // operands + hi/lo staging
-constexpr size_t GT_SMEM = (size_t)(GT_DYN > tc::EPI_BYTES ? GT_DYN : tc::EPI_BYTES) + 1024;
-
-__device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cpAsyncWaitOne() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+constexpr size_t GT_SMEM =
+    (size_t)(tc::CHUNK_SMEM > tc::EPI_BYTES ? tc::CHUNK_SMEM : tc::EPI_BYTES) + 1024;
 
 }  // namespace
 
@@ -39,7 +31,6 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
   __shared__ int expo[RB];
   __shared__ unsigned long long bars[2];
   __shared__ uint32_t tmemBase;
-  __shared__ int sErr;
   if(liveN && (int)blockIdx.x >= *liveN) return;  // before any barrier or TMEM allocation
   const int t = blockIdx.x, s = list[t], tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int fSS = 2 * hSS + 1, K = fSS * fSS, R = wRows + 1;
@@ -63,7 +54,6 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
     imgRow[k] = v;
   }
   if(tid == 0) {
-    sErr = 0;
     barInit(smemU32(&bars[0]), 1);
     barInit(smemU32(&bars[1]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -89,85 +79,16 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
     }
 #pragma unroll
     for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if(lane == 0) {
-      int e = 0;
-      if(m > 0.f) frexpf(m, &e);
-      expo[r] = e;
-    }
+    if(lane == 0) expo[r] = rowExponent(m);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
-
-  // W chunks (hi and lo) arrive one ahead through cp.async into FP32
-  // staging buffers behind the operand buffers (the epilogue reuses the area
-  // later); columns at or past ldW are not copied (the slicer zeroes k >= K).
-  float* stage = (float*)(buf + 2 * OPBUF);
-  auto fetch = [&](int ch) {
-    float* st = stage + (ch & 1) * (GT_STAGE / 4);
-    float* stl = st + 2 * (GT_STAGE / 4);
-    for(int u = tid; u < RB * (KC / 4); u += GT_THREADS) {
-      const int r = u / (KC / 4), k = ch * KC + (u % (KC / 4)) * 4;
-      if(r < wRows && k < ldW) {
-        cpAsync16(smemU32(st + r * KC + (k - ch * KC)), Ws + (size_t)r * ldW + k);
-        cpAsync16(smemU32(stl + r * KC + (k - ch * KC)), Wl + (size_t)r * ldW + k);
-      }
-    }
-    cpAsyncCommit();
-  };
-  fetch(0);
-  for(int ch = 0; ch < nChunk; ch++) {
-    const int b = ch & 1;
-    unsigned char* B = buf + b * OPBUF;
-    if(ch + 1 < nChunk) {
-      fetch(ch + 1);
-      cpAsyncWaitOne();
-    } else {
-      cpAsyncWaitAll();
-    }
-    if(ch >= 2 && !waitUntil(smemU32(&bars[b]), ((ch - 2) >> 1) & 1, deadline)) sErr = 1;
-    __syncthreads();
-    const float* stc = stage + (ch & 1) * (GT_STAGE / 4);
-    const float* stl = stc + 2 * (GT_STAGE / 4);
-    // 16-byte units: (row, 8 consecutive k) -> 5 slice units
-    for(int u = tid; u < RB * (KC / 8); u += GT_THREADS) {
-      const int r = u % RB, kg = u / RB, k0 = ch * KC + kg * 8;  // rows fastest
-      float xh[8], xl[8];
-#pragma unroll
-      for(int e = 0; e < 8; e++) {
-        const int k = k0 + e;
-        xh[e] = xl[e] = 0.f;
-        if(r < R && k < K) {
-          if(r < wRows) {
-            xh[e] = stc[r * KC + (k - ch * KC)];
-            xl[e] = stl[r * KC + (k - ch * KC)];
-          } else {
-            xh[e] = imgRow[k];
-          }
-        }
-      }
-      uint32_t q[NS][4];
-      slice8(xh, xl, r < R ? expo[r] : 0, q);
-      storeSlices(B, r, kg, q);
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if(tid == 0) issueChunk(tmem, B, ch == 0, smemU32(&bars[b]));
-  }
-  // the last commit covers every product issued before it
-  {
-    const int last = nChunk - 1;
-    if(!waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, deadline)) {
-      sErr = 1;
-      // give products still in flight a second bounded chance before TMEM is freed
-      waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, timerNs() + WAIT_NS);
-    }
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool ok = gramChunks<GT_THREADS>(Ws, Wl, wRows, ldW, R, K, imgRow, expo, buf, bars, tmem,
+                                         deadline);
   epilogue(tmem, (long long*)buf, expo, R, Gout + (size_t)t * R * R);
-  if(tid == 0 && sErr) atomicOr(timeout, 1);
+  if(tid == 0 && !ok) atomicOr(timeout, 1);
 }
 
 template __global__ void k_gram_tc<float>(const float*, int, int, const int*, const int*,

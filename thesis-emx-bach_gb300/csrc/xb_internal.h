@@ -136,6 +136,10 @@ struct xb_ctx {
   int* dYGroupMembers = nullptr;
   int* dKx = nullptr;
   int* dKy = nullptr;
+  // the filters as float pairs (hi = (float)f, lo = (float)(f - hi)) for the
+  // fused fill: X filters [nPSF][fK] hi then lo, then the unique Y filters
+  // [group][fK] hi then lo
+  float* dFSplit = nullptr;
   // cd / ksc
   int convTemplate = 0, chosen = 0;
   double merit[2] = {0, 0};
@@ -163,6 +167,8 @@ struct xb_ctx {
   int trace = 0;
   int timeKernels = 0;
   int gramFp64 = 0;  // mixed mode: FP64 CUDA-core Gram instead of the tensor cores (checks)
+  int fillGram = 1;     // mixed mode: fused fill + tensor-core Gram where the shape allows
+  int fillGramTma = 1;  // the fused kernel stages its windows by TMA tile copies
   int rank = 0;          // learned substamp order after sss: 1 demote, 2 sort
   int rankTau = 500;     // demotion threshold of the accept probability, 1/1000
   int autotune = 1;      // time the variants of tunable kernels on first use
@@ -331,6 +337,13 @@ int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
                  const std::function<void(int)>& launch);
 // Learned substamp ranking (xb_ranker.cu): reorder both sets' substamps.
 void rankSubstamps(xb_ctx* c);
+// Fused fill + tensor-core Gram of the mixed path (xb_fill_gram.cu): W (hi,
+// lo) of the listed stamps and their Gram matrices G (nList x R x R), the
+// results of fill + finish + gramTensorCores bit for bit; fillGramFits says
+// whether the context's shape and options allow it.
+bool fillGramFits(const xb_ctx* c);
+void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv, double* G,
+                    const int* liveN);
 // Tensor-core Gram of the mixed path (xb_gram_tc.cu) into G (nList x R x R);
 // false when the shape is outside its limits.
 bool gramTensorCores(xb_ctx* c, int si, const int* dList, int nList, int other, double* G,

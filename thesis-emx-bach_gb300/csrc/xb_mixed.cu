@@ -21,6 +21,7 @@
 #include <atomic>
 #include <climits>
 
+#include "xb_df.cuh"
 #include "xb_device.cuh"
 #include "xb_internal.h"
 
@@ -32,58 +33,12 @@ namespace {
 
 constexpr int MX_THREADS = 256;
 
-__device__ __forceinline__ float floatNormF(int x, int w) {
-  float hw = (float)w * 0.5f;
-  return ((float)x - hw) / hw;
-}
-
-// -------------------------------------------------- W as an FP32 pair ---
-// The normal matrices are ill-conditioned enough that a W rounded to FP32
-// (2^-24 per element) moves the difference image of the reference's own
-// test case (cond ~6e13) by ~1e-3 of the pixel noise.  So W is kept as an
-// unevaluated sum hi + lo of two floats (~48 bits), computed on the FP32 pipe
-// (GB300's FP64 rate is 1/64 of FP32) with error-free transformations; the
-// library is built without FMA contraction, so the two-sums below are exact.
-//   * Y pass (convStampY, cl_kern/cmv.cl:70-106): the reference accumulates
-//     in float over FP64 products, v = (float)((double)v + img * fy), and
-//     the rounding of every step is part of its result.  It is reproduced:
-//     fy = fh + fl as floats, img*fh split exactly by an FMA, the sum
-//     v + product formed exactly (two-sum) and rounded once to float.  The
-//     result equals the reference's except when v + product lies within
-//     ~2^-47 of a float rounding boundary (~1 step in 10^7).
-//   * X pass (convStampX, :108-135, FP64 there): double-float accumulation.
-//   * convStampOdd (:137-154): W[n] - W[0] as a double-float difference.
-//   * convStampBg (:156-193): FP64, split into hi + lo.
-__device__ __forceinline__ float refStepY(float v, float a, float fh, float fl) {
-  const float ph = a * fh;
-  const float pe = fmaf(a, fh, -ph);  // a*fh = ph + pe exactly
-  const float pl = a * fl;
-  const float s = v + ph;             // two-sum: v + ph = s + e exactly
-  const float bb = s - v;
-  const float e = (v - (s - bb)) + (ph - bb);
-  return s + (e + (pe + pl));
-}
-// (sh, sl) += t * (fh + fl)
-__device__ __forceinline__ void dfAccum(float& sh, float& sl, float t, float fh, float fl) {
-  const float ph = t * fh;
-  const float pe = fmaf(t, fh, -ph);
-  const float s = sh + ph;
-  const float bb = s - sh;
-  const float e = (sh - (s - bb)) + (ph - bb);
-  sh = s;
-  sl += e + (pe + t * fl);
-}
-// renormalised hi + lo of sh + sl
-__device__ __forceinline__ void dfNorm(float sh, float sl, float& hi, float& lo) {
-  const float s = sh + sl;
-  const float bb = s - sh;
-  hi = s;
-  lo = (sh - (s - bb)) + (sl - bb);
-}
-__device__ __forceinline__ void splitF64(double v, float& hi, float& lo) {
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
-}
+using df::dfAccum;
+using df::dfNorm;
+using df::dfSub;
+using df::floatNormF;
+using df::refStepY;
+using df::splitF64;
 
 // One CTA per (stamp, group of basis functions sharing a Y filter).
 template <class T>
@@ -184,12 +139,8 @@ __global__ void __launch_bounds__(MX_THREADS)
 #pragma unroll 4
     for(int e = 0; e < ne; e++) {
       const size_t i = (size_t)evenRows[e] * ldW + p;
-      const float ah = Ws[i], al = Wl[i];
-      const float s = ah - bh;  // two-sum of ah and -bh
-      const float bb = s - ah;
-      const float er = (ah - (s - bb)) + (-bh - bb);
       float hi, lo;
-      dfNorm(s, er + (al - bl), hi, lo);
+      dfSub(Ws[i], Wl[i], bh, bl, hi, lo);
       Ws[i] = hi;
       Wl[i] = lo;
     }
@@ -1280,6 +1231,21 @@ void fillStampsMixed(xb_ctx* c, int si, const int* dList, int nList, int imgConv
   const int tw = 2 * (g.hSS + g.hK) + 1, th = g.fSS;
   const size_t smemFill = (size_t)(tw * tw + th * tw + 4 * g.fK) * sizeof(float);
   const int other = 1 - imgConv;
+  if(fillGramFits(c)) {
+    // one kernel: window by TMA, Y and X passes, W to global, exact Gram
+    const int R = g.wRows + 1;
+    double* G = buf<double>(c, "gram_scratch", (size_t)nList * R * R);
+    {
+      KT_SCOPE(c, "fill_gram");
+      fillGramLaunch(c, si, dList, nList, imgConv, G, liveN);
+    }
+    KT_SCOPE(c, "gram_scatter");
+    k_gram_scatter<<<nList, MX_THREADS, 0, c->stream>>>(dList, liveN, S.count, S.cur, g.wRows,
+                                                        g.nPSF, g.nBG, g.qCount, G, S.Q, S.B,
+                                                        S.dots, mixedDotStride(g));
+    XB_LAUNCHED(c);
+    return;
+  }
   {
     KT_SCOPE(c, "fill_w");
     dim3 grid(nList, nGroups);

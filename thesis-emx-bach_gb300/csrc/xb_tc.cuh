@@ -13,12 +13,13 @@
 // Exact slicing: each element x = hi + lo (two floats, ~48 bits) of row r is
 // scaled by 2^-e_r (e_r = the exponent just above the row's largest |hi|) and
 // rounded to a 35-bit fixed-point integer Z, written as five signed base-128
-// digits q_0..q_4 (|q| <= 127, exact in BF16):
+// digits q_0..q_4 (|q_0| <= 128, |q_t| <= 80 for t >= 1, exact in BF16;
+// slice8 below):
 //     x ~= 2^e_r * sum_t q_t 2^-7(t+1),   |error| <= 2^(e_r - 36).
 // Every slice-pair dot product P_tu[a][b] = sum_k q_{a,t,k} q_{b,u,k} is an
-// integer of magnitude <= 1024 * 127^2 < 2^24, so the tensor cores' FP32
-// accumulation of BF16 products is exact.  All pairs but (4, 4) are summed
-// exactly in int64 and rounded once:
+// integer of magnitude <= 961 * 128^2 < 2^24 (K <= 961: substamps up to
+// 31 x 31), so the tensor cores' FP32 accumulation of BF16 products is exact.
+// All pairs but (4, 4) are summed exactly in int64 and rounded once:
 //     G_ab = 2^(e_a + e_b - 63) * sum_{m<=7} 2^(7(7-m)) sum_{t+u=m} P_tu[a][b],
 // i.e. G is the Gram matrix of the rounded X up to the pair (4, 4) (2^-56 of
 // the leading pair) and the final FP64 rounding.  (On the reference's own
@@ -40,7 +41,6 @@
 // every wait is bounded by a global-timer deadline.
 #pragma once
 
-#include <cuda_bf16.h>
 #include <stdint.h>
 
 namespace xb {
@@ -131,41 +131,46 @@ __device__ __forceinline__ void tmemFree512(uint32_t tmem) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 }
 
-// round(x * 2^shift) as a signed integer, from the float's fields (exact
-// shifts; ties away from zero); |x| * 2^shift must stay below 2^62.
-__device__ __forceinline__ long long scaled(float x, int shift) {
-  const uint32_t xb = __float_as_uint(x);
-  const int ex = (int)((xb >> 23) & 0xFFu);
-  const uint32_t m = (xb & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
-  const int sh = (ex ? ex : 1) - 150 + shift;
-  unsigned long long mag;
-  if(sh >= 0) mag = (unsigned long long)m << sh;
-  else if(sh > -40) mag = ((unsigned long long)m + (1ull << (-sh - 1))) >> (-sh);
-  else mag = 0;
-  return (xb >> 31) ? -(long long)mag : (long long)mag;
+// 2^k as a float, -126 <= k <= 127
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+// nearest integer of |x| < 2^22 (ties to even): the sum's spacing is 1
+__device__ __forceinline__ float rintSmall(float x) {
+  const float big = 12582912.f;  // 1.5 * 2^23
+  return (x + big) - big;
 }
 
 // The five BF16 digits of 8 consecutive elements (hi[e] + lo[e]) of a row
-// with exponent er, as 16-byte core-matrix rows q[slice][0..3].
-// Z = round((hi + lo) 2^(35 - er)) in integers: both parts are scaled with
-// 16 guard bits (|hi| 2^(51 - er) < 2^51), summed exactly and rounded once.
-// |hi + lo| < 2^er (hi is the rounded sum, below 2^er by at least an ulp),
-// so |Z| < 2^35: five digits.
+// with exponent er (|hi| < 2^er on the whole row), as 16-byte core-matrix
+// rows q[slice][0..3].  With v = hi 2^(7 - er) (exact, |v| < 128):
+//     d0 = rint(v), r = (v - d0) 128, d1 = rint(r), r = (r - d1) 128,
+//     d2 = rint(r), r = (r - d2) 128 + lo 2^(28 - er), d3 = rint(r),
+//     r = (r - d3) 128, d4 = rint(r),
+// every step exact (each remainder is a multiple of ulp(v) below 1) except
+// the one addition of lo, which rounds at 2^-46 of the row maximum; so
+//     x ~= 2^(er - 35) Z,  Z = sum_t d_t 128^(4 - t),  |x - 2^(er-35) Z| <= 2^(er - 36),
+// and |d0| <= 128, |d1|, |d2|, |d4| <= 64, |d3| <= 80.  A digit is an integer
+// of at most 8 significant bits, so its BF16 form is the float's upper half.
 __device__ __forceinline__ void slice8(const float* hi, const float* lo, int er, uint32_t (&q)[NS][4]) {
+  const float s7 = pow2f(7 - er), s28 = pow2f(28 - er);
 #pragma unroll
-  for(int sl = 0; sl < NS; sl++) q[sl][0] = q[sl][1] = q[sl][2] = q[sl][3] = 0u;
+  for(int e = 0; e < 8; e += 2) {
+    float d[2][NS];
 #pragma unroll
-  for(int e = 0; e < 8; e++) {
-    const long long zx = scaled(hi[e], 51 - er) + scaled(lo[e], 51 - er);
-    const long long z = (zx + (1ll << 15)) >> 16;
-    const bool neg = z < 0;
-    const unsigned long long mag = (unsigned long long)(neg ? -z : z);
-#pragma unroll
-    for(int sl = 0; sl < NS; sl++) {
-      const int dgt = (int)((mag >> (7 * (NS - 1 - sl))) & 127u);
-      const __nv_bfloat16 hb = __float2bfloat16_rn((float)(neg ? -dgt : dgt));
-      q[sl][e >> 1] |= (uint32_t)__bfloat16_as_ushort(hb) << ((e & 1) * 16);
+    for(int i = 0; i < 2; i++) {
+      const float v = hi[e + i] * s7;
+      d[i][0] = rintSmall(v);
+      float r = (v - d[i][0]) * 128.f;
+      d[i][1] = rintSmall(r);
+      r = (r - d[i][1]) * 128.f;
+      d[i][2] = rintSmall(r);
+      r = (r - d[i][2]) * 128.f + lo[e + i] * s28;
+      d[i][3] = rintSmall(r);
+      r = (r - d[i][3]) * 128.f;
+      d[i][4] = rintSmall(r);
     }
+#pragma unroll
+    for(int sl = 0; sl < NS; sl++)
+      q[sl][e >> 1] = __byte_perm(__float_as_uint(d[0][sl]), __float_as_uint(d[1][sl]), 0x7632);
   }
 }
 // stores the digits of row r, K group kg (8 elements) into an operand buffer
@@ -197,6 +202,117 @@ __device__ __forceinline__ void issueChunk(uint32_t tmem, const unsigned char* B
   }
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                : "memory");
+}
+
+// The row exponent e (|hi| < 2^e on the row) from the row's largest |hi|;
+// rows of nothing but zeros (or values below 2^-90) take -90, which keeps
+// every scale factor of slice8 a normal float.
+__device__ __forceinline__ int rowExponent(float m) {
+  int e = 0;
+  if(m > 0.f) frexpf(m, &e);
+  return e < -90 ? -90 : e;
+}
+
+__device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitOne() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// FP32 W chunk staging: rows padded to KC + 4 floats, so that the slicing
+// loop's 16-byte reads of eight consecutive rows fall on distinct banks
+constexpr int SKC = KC + 4;
+constexpr int STAGE_F = RB * SKC;  // floats of one staging buffer (17 KB)
+// shared memory of the K-chunk loop: two operand buffers, then hi and lo
+// staging for two chunks (the epilogue reuses the area)
+constexpr int CHUNK_SMEM = 2 * OPBUF + 4 * STAGE_F * 4;
+
+// The K-chunk loop of one stamp, run by all NT threads of the CTA: W rows
+// r < wRows (hi at Ws, lo at Wl, row stride ldW, K valid columns) and the
+// image row imgRow (shared, zero-padded to a whole chunk) as row wRows are
+// staged by cp.async one chunk ahead, sliced with the row exponents expo[]
+// into the operand buffers at buf (1024-aligned, CHUNK_SMEM bytes), and
+// multiplied into TMEM by one thread; bars[0..1] are the operand buffers'
+// commit barriers (initialised, count 1).  Returns false, in every thread,
+// when a wait of any thread ran out of time (the products in flight were
+// then given a second bounded wait).
+template <int NT>
+__device__ __forceinline__ bool gramChunks(const float* __restrict__ Ws, const float* __restrict__ Wl,
+                                           int wRows, int ldW, int R, int K,
+                                           const float* imgRow, const int* expo,
+                                           unsigned char* buf, unsigned long long* bars,
+                                           uint32_t tmem, unsigned long long deadline) {
+  const int tid = threadIdx.x;
+  const int nChunk = (K + KC - 1) / KC;
+  bool ok = true;
+  float* stage = (float*)(buf + 2 * OPBUF);
+  auto fetch = [&](int ch) {
+    float* st = stage + (ch & 1) * STAGE_F;
+    float* stl = st + 2 * STAGE_F;
+    for(int u = tid; u < RB * (KC / 4); u += NT) {
+      const int r = u / (KC / 4), k = ch * KC + (u % (KC / 4)) * 4;
+      if(r < wRows && k < ldW) {
+        cpAsync16(smemU32(st + r * SKC + (k - ch * KC)), Ws + (size_t)r * ldW + k);
+        cpAsync16(smemU32(stl + r * SKC + (k - ch * KC)), Wl + (size_t)r * ldW + k);
+      }
+    }
+    cpAsyncCommit();
+  };
+  fetch(0);
+  for(int ch = 0; ch < nChunk; ch++) {
+    const int b = ch & 1;
+    unsigned char* B = buf + b * OPBUF;
+    if(ch + 1 < nChunk) {
+      fetch(ch + 1);
+      cpAsyncWaitOne();
+    } else {
+      cpAsyncWaitAll();
+    }
+    if(ch >= 2 && !waitUntil(smemU32(&bars[b]), ((ch - 2) >> 1) & 1, deadline)) ok = false;
+    __syncthreads();
+    const float* stc = stage + (ch & 1) * STAGE_F;
+    const float* stl = stc + 2 * STAGE_F;
+    // 16-byte units: (row, 8 consecutive k) -> 5 slice units
+    for(int u = tid; u < RB * (KC / 8); u += NT) {
+      const int r = u % RB, kg = u / RB, k0 = ch * KC + kg * 8;  // rows fastest
+      float xh[8], xl[8];
+      if(r < wRows) {
+        const float4* ph = (const float4*)(stc + r * SKC + kg * 8);
+        const float4* pl = (const float4*)(stl + r * SKC + kg * 8);
+        const float4 h0 = ph[0], h1 = ph[1], l0 = pl[0], l1 = pl[1];
+        xh[0] = h0.x; xh[1] = h0.y; xh[2] = h0.z; xh[3] = h0.w;
+        xh[4] = h1.x; xh[5] = h1.y; xh[6] = h1.z; xh[7] = h1.w;
+        xl[0] = l0.x; xl[1] = l0.y; xl[2] = l0.z; xl[3] = l0.w;
+        xl[4] = l1.x; xl[5] = l1.y; xl[6] = l1.z; xl[7] = l1.w;
+      } else {
+#pragma unroll
+        for(int e = 0; e < 8; e++) {
+          xh[e] = r < R ? imgRow[k0 + e] : 0.f;  // zero-padded past K
+          xl[e] = 0.f;
+        }
+      }
+#pragma unroll
+      for(int e = 0; e < 8; e++)
+        if(k0 + e >= K) xh[e] = xl[e] = 0.f;
+      uint32_t q[NS][4];
+      slice8(xh, xl, r < R ? expo[r] : 0, q);
+      storeSlices(B, r, kg, q);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if(tid == 0) issueChunk(tmem, B, ch == 0, smemU32(&bars[b]));
+  }
+  // the last commit covers every product issued before it
+  const int last = nChunk - 1;
+  if(!waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, deadline)) {
+    ok = false;
+    // give products still in flight a second bounded chance before TMEM is freed
+    waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, timerNs() + WAIT_NS);
+  }
+  const int failed = __syncthreads_or(ok ? 0 : 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return failed == 0;
 }
 
 // TMEM -> four int64 sum arrays in shared memory (sums: EPI_BYTES, 8-byte
@@ -239,7 +355,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, long long* sums, const i
 #pragma unroll
           for(int u = 0; u < 5; u++) {
             const int m = t1 + u;
-            const long long p = (long long)__float2ll_rn(p1[u][i]);
+            const long long p = (long long)__float2int_rn(p1[u][i]);  // |p| < 2^24: exact
             const long long v = p * (1ll << (m <= 3 ? 7 * (3 - m) : 7 * (7 - m)));
             if(m <= 3) xa += v; else xb += v;
             if(u >= 2) {
@@ -249,7 +365,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, long long* sums, const i
 #pragma unroll
           for(int j = 0; j < 3; j++) {
             const int m = t2 + 2 + j;  // >= 4
-            const long long v = (long long)__float2ll_rn(p2[j][i]) * (1ll << (7 * (7 - m)));
+            const long long v = (long long)__float2int_rn(p2[j][i]) * (1ll << (7 * (7 - m)));
             xb += v;
             if(j == 2) yb += v;
           }
