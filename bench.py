@@ -23,12 +23,22 @@ xbach/ranker_preset5.npy).  The process asks for 32 hardware work queues
 (CUDA_DEVICE_MAX_CONNECTIONS, set before CUDA starts): with the default 8,
 the workers' streams share queues and their graphs serialise.
 
-roofline: the conv kernel's HBM view (the contract's field); roofline_tensor:
-the exact-slice Gram on the tensor pipe; roofline_cuda_cores: the conv
-against the FP32 FMA peak and the global LDL^T against the FP64 FMA peak,
-both measured in the same run (xb_measure_fma_peaks).  cpu_baseline: the
-median of --cpu-runs FP64 oracle runs on all host threads, and one
-single-threaded run.
+roofline: the kernel with the most device time per frame (single-frame
+kernel timers) against the roof of the unit that bounds it, with the
+reference's algorithmic work (not the extra operations issued here for
+precision); rooflines: every hot kernel's views (conv+sub: HBM at 20 B/px and
+FP32 at 2 x 441 FLOP/px; fused fill + Gram: FP32 passes and tensor Gram per
+substamp; global solve: FP64 at 2/3 n^3).  Peaks: MEASURED_PEAKS.json for HBM
+and bf16, the FP32/FP64 FMA peaks measured in this run.  cpu_baseline: the
+median of --cpu-runs FP64 oracle runs on all host threads over the batch's
+first pairs, and one single-threaded run.
+
+Beside the headline (ranked, frame graphs): chosen_unranked (the same batch
+without the learned ranking), plain_gpu_batched (the plain FP64 pipeline
+through the same batch API, pairs and workers; chosen_over_plain divides by
+it) and plain_gpu_single; accuracy gives the chosen image against the plain
+one with the same ranking and without it, the unranked chosen image against
+the unranked plain one, and names the gate.
 
 --config 4: 64 pairs of mixed sizes per step (preset 4).  --files N: N
 2048^2 pairs per step streamed as FITS files through xb_pipeline.
@@ -181,24 +191,55 @@ def cpu_frames_per_s(T, S, info, runs, threads=None):
 
 
 def run_reference(args):
+    """The reference's CPU path on the GPU arm's frames: step k runs the
+    frame pairs of seeds k*f .. k*f+f-1 (mod --batch), f = ceil(batch /
+    steps), so the timed steps cover every seed the GPU arm runs."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    import build_native
+    build_native.build_oracle()
+    from xbach_testlib import Oracle
     from xbach.synth import make_pair
-    T, S, info = make_pair(2)
-    if args.warmup > 0:
-        cpu_frames_per_s(T, S, info, args.warmup)
-    fps, threads, times, _ = cpu_frames_per_s(T, S, info, args.steps)
+    B = max(1, args.batch)
+    per = -(-B // max(1, args.steps))
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    frames = {}
+
+    def frame(seed):
+        if seed not in frames:
+            T, S, info = make_pair(2, frame=seed)
+            frames[seed] = (T.astype("float64"), S.astype("float64"), frame_params(o, info))
+        return frames[seed]
+
+    def step(k):
+        seeds = [(k * per + i) % B for i in range(per)]
+        for sd in seeds:
+            frame(sd)  # generated outside the timed region
+        t0 = time.perf_counter()
+        for sd in seeds:
+            T64, S64, p = frames[sd]
+            r = o.run(p, T64, S64, nthreads=threads)
+            assert r.status == 0, r.status
+        return time.perf_counter() - t0
+    for k in range(args.warmup):
+        step(k)
+    times = [step(k) for k in range(args.steps)]
     total = sum(times)
+    fps = per * args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded 2048x2048 crowded field)",
-        "config": {"workload": WORKLOAD, "implementation": "FP64 C++ restatement of the reference "
+        "data": "synthetic (seeded 2048x2048 crowded fields, one seed per frame pair)",
+        "config": {"workload": WORKLOAD, "frames_per_step": per,
+                   "seeds": f"0..{B - 1} (the GPU arm's batch), {per} per step",
+                   "implementation": "FP64 C++ restatement of the reference "
                    "CPU path (the reference needs OpenCL + CCfits, absent here)"},
         "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full 2048x2048 frame pairs, one per step"},
+                         "sample": f"{per * args.steps} full 2048x2048 frame pairs, {per} per step, "
+                                   f"seeds cycling over the GPU arm's {B}"},
         "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -206,77 +247,71 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------- roofline --
-# DRAM bytes (read + write) of one k_conv_sub_f32 launch on the 2048^2
-# workload, from `ncu --set full` (profiles/mixed_kernels_2048_ncu.md):
-# 33.877 MB read + 1.665 MB written, cold cache.
-CONV_DRAM_BYTES_2048 = 33.876992e6 + 1.664512e6
+# Algorithmic work per unit (the reference's operations, not the extra ones
+# this implementation issues for precision):
+#   conv+sub: 2 x 441 FLOP and 20 B of HBM per pixel (T, S read FP32; conv
+#     and diff written FP32; mask 2 B read and written);
+#   cmv fill of one substamp: Y pass 15 filters x 1581 x 21 + X pass
+#     49 x 961 x 21 MAC (2.97 MFLOP, FP32 in mixed mode) and the Gram
+#     1275 x 961 + B 50 x 961 MAC (2.45 MFLOP, tensor cores);
+#   global solve: the reference's LU, 2/3 n^3 FLOP (n = 292); the LDL^T here
+#     executes n^3 / 3 of them.
+FILL_PASS_FLOP = 2.0 * (15 * 1581 * 21 + 49 * 961 * 21)
+FILL_GRAM_FLOP = 2.0 * (1275 * 961 + 50 * 961)
+CONV_BYTES_PER_PX = 20
 
 
-def roofline_for(name, ms_per_launch, n_pix, mode, hbm_peak):
-    """Algorithmic bytes of one launch of the frame-wide kernel and the
-    achieved bandwidth.  The conv reads I and O (FP32) and the mask (2 B) and
-    writes the mask, conv and diff (FP32; plain mode also FP64 copies)."""
-    if name == "conv_sub":
-        per_px = 4 + 4 + 2 + 4 + 4 + (16 if mode == "plain" else 0)
-        traffic_bytes = per_px * n_pix
-    else:
-        return None
-    achieved = traffic_bytes / (ms_per_launch * 1e-3) / 1e9
-    traffic = CONV_DRAM_BYTES_2048 if (mode == "mixed" and n_pix == 2048 * 2048) else None
-    return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": traffic, "kernel": name,
-            "algorithmic_bytes_per_launch": traffic_bytes, "ms_per_launch": ms_per_launch}
-
-
-def cuda_core_rooflines(kernels, params, n_pix, mode, fp32_peak, fp64_peak):
-    """The kernels bound by a CUDA-core pipe against that pipe's measured
-    FMA peak (xb_measure_fma_peaks in this run):
-    * conv_sub: 2 x 441 FLOP per pixel (one 21x21 kernel per pixel), FP32 in
-      mixed mode, FP64 in plain mode;
-    * global_ldl: the LDL^T of the n x n global system, n^3 / 3 FLOP per
-      launch (n = nComp + nBG + 1 = 292 here), FP64, one 16-CTA cluster: a
-      dependency chain of n pivots, latency-bound by design."""
+def rooflines(kernels, params, n_pix, mode, stamps, peaks):
+    """Per-kernel rooflines from the single-frame kernel timers (CUDA events
+    around each launch on the library's stream).  peaks: measured HBM GB/s
+    and bf16 TFLOP/s (MEASURED_PEAKS.json) and the FP32/FP64 FMA peaks
+    measured in this run (xb_measure_fma_peaks; MEASURED_PEAKS.json has no
+    CUDA-core entries)."""
     from xbach.accuracy import layout
-    out = {"peaks_tflops": {"fp32": fp32_peak, "fp64": fp64_peak,
-                            "source": "measured in this run (xb_measure_fma_peaks)"}}
+    out = {}
     fk = 2 * params.hKernelWidth + 1
+
+    def view(bound, work, ms, peak, unit, scale, **kw):
+        ach = work / (ms * 1e-3) / scale
+        d = {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+             "ms_per_launch": ms}
+        d.update(kw)
+        return d
     if "conv_sub" in kernels:
         k = kernels["conv_sub"]
         ms = k["ms_total"] / k["launches"]
+        byt = CONV_BYTES_PER_PX * n_pix + (16 * n_pix if mode == "plain" else 0)
         flop = 2.0 * fk * fk * n_pix
-        peak = fp32_peak if mode == "mixed" else fp64_peak
-        ach = flop / (ms * 1e-3) / 1e12
-        out["conv_sub"] = {"bound": "fp32" if mode == "mixed" else "fp64", "achieved": ach,
-                           "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                           "flop_per_launch": flop, "ms_per_launch": ms}
+        out["conv_sub"] = {
+            "hbm": view("hbm", byt, ms, peaks["hbm"], "GB/s", 1e9, bytes_per_launch=byt,
+                        peak_source=peaks["hbm_source"]),
+            "cuda_cores": view("fp32" if mode == "mixed" else "fp64", flop, ms,
+                               peaks["fp32"] if mode == "mixed" else peaks["fp64"], "TFLOP/s",
+                               1e12, flop_per_launch=flop, peak_source=peaks["fma_source"])}
+    if "fill_gram" in kernels:
+        k = kernels["fill_gram"]
+        ms = k["ms_total"]
+        out["fill_gram"] = {
+            "fp32_passes": view("fp32", FILL_PASS_FLOP * stamps, ms, peaks["fp32"], "TFLOP/s", 1e12,
+                                flop_per_substamp=FILL_PASS_FLOP, substamps_per_frame=stamps,
+                                ms_per_frame=ms, peak_source=peaks["fma_source"]),
+            "tensor_gram": view("tensor", FILL_GRAM_FLOP * stamps, ms, peaks["bf16"], "TFLOP/s",
+                                1e12, flop_per_substamp=FILL_GRAM_FLOP,
+                                mma_flop_per_substamp=16 * 4 * 2 * 128 * (256 + 64 + 192) * 16,
+                                substamps_per_frame=stamps, ms_per_frame=ms,
+                                peak_source=peaks["bf16_source"])}
+        for v in out["fill_gram"].values():
+            v.pop("ms_per_launch")
     if "global_ldl" in kernels:
         k = kernels["global_ldl"]
         ms = k["ms_total"] / k["launches"]
         n_comp, n_bg = layout(params)
         n = n_comp + n_bg + 1
-        flop = n ** 3 / 3.0
-        ach = flop / (ms * 1e-3) / 1e12
-        out["global_ldl"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak,
-                             "unit": "TFLOP/s", "frac": ach / fp64_peak, "n": n,
-                             "flop_per_launch": flop, "ms_per_launch": ms}
+        out["global_ldl"] = view("fp64", 2.0 * n ** 3 / 3.0, ms, peaks["fp64"], "TFLOP/s", 1e12,
+                                 n=n, flop_per_launch=2.0 * n ** 3 / 3.0,
+                                 flop_executed_per_launch=n ** 3 / 3.0,
+                                 peak_source=peaks["fma_source"])
     return out
-
-
-def gram_tensor_roofline(kernels, ctx, bf16_peak_tflops, wcols=961, rows=64, kc=64):
-    """BF16 tensor work of the exact-slice Gram (k_gram_tc) over one frame:
-    per stamp and 64-column chunk of W, four K-steps of three MMAs (M128 x
-    N256, N64, N128, K16), i.e. 2*128*(256+64+128)*16*4 FLOP per chunk, for
-    every stamp filled (both sets in cmv, then the ksc refills)."""
-    if "gram" not in kernels:
-        return None
-    chunks = -(-wcols // kc)
-    flop_stamp = chunks * 4 * 2 * 128 * (256 + 64 + 128) * 16
-    stamps = ctx.scalar("nstamps0") + ctx.scalar("nstamps1") + ctx.scalar("ksc_refills")
-    ms = kernels["gram"]["ms_total"]
-    achieved = flop_stamp * stamps / (ms * 1e-3) / 1e12
-    return {"bound": "tensor", "kernel": "gram_tc", "achieved": achieved,
-            "peak": bf16_peak_tflops, "unit": "TFLOP/s", "frac": achieved / bf16_peak_tflops,
-            "flop_per_stamp": flop_stamp, "stamps_per_frame": stamps, "ms_per_frame": ms}
 
 
 def run_result(xbach, cx):
@@ -285,24 +320,48 @@ def run_result(xbach, cx):
             "convTemplate": cx.scalar("convTemplate")}
 
 
+SIGMA_BAR = 1e-3
+
+
 def accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx=None, uctx=None):
     """Chosen vs plain GPU (acceptance: diff within 1e-3 sigma) and against
     the FP64 oracle on the same frame pair.
 
-    With the learned ranking on, the chosen result is compared with the plain
-    FP64 GPU pipeline running the same ranking (prctx: the same substamp
-    order, so the figures are the precision error alone); the oracle has no
-    ranking, so the mixed pipeline without it (uctx) is compared with the
-    oracle, and ranking_effect gives what the ranking itself changes."""
+    ctx: the chosen pipeline (mixed, ranked when prctx is given); pctx: the
+    plain FP64 GPU pipeline without ranking (the reference's semantics);
+    prctx: the plain pipeline with the same learned ranking (the same
+    substamp picks, so the difference is the precision error alone); uctx:
+    the mixed pipeline without ranking.  The gate is named in the result."""
     from xbach import accuracy as acc
     n_comp, n_bg = acc.layout(params)
     chosen, plain = run_result(xbach, ctx), run_result(xbach, pctx)
-    plain_same = run_result(xbach, prctx) if prctx is not None else plain
-    unranked = run_result(xbach, uctx) if uctx is not None else chosen
-    out = {"chosen_vs_plain": acc.compare(chosen, plain_same, T, S, n_comp, n_bg),
-           "sigma_definition": "sqrt(|target| + |conv| + 2*5^2) ADU, gain 1"}
-    if uctx is not None:
-        out["chosen_vs_plain"]["reference"] = "plain FP64 GPU pipeline with the same ranking"
+    out = {"sigma_definition": "sqrt(|target| + |conv| + 2*5^2) ADU, gain 1"}
+    if prctx is None:
+        out["chosen_vs_plain"] = acc.compare(chosen, plain, T, S, n_comp, n_bg)
+        m = out["chosen_vs_plain"]["diff"]["max_sigma"]
+        out["gate"] = {"uses": "chosen_vs_plain", "max_sigma": m, "bar": SIGMA_BAR,
+                       "pass": bool(m <= SIGMA_BAR)}
+    else:
+        plain_same = run_result(xbach, prctx)
+        unranked = run_result(xbach, uctx)
+        out["chosen_vs_plain_same_ranking"] = acc.compare(chosen, plain_same, T, S, n_comp, n_bg)
+        out["chosen_vs_plain_same_ranking"]["reference"] = (
+            "plain FP64 GPU pipeline with the same learned ranking (same substamp picks)")
+        out["chosen_vs_plain_unranked"] = acc.compare(chosen, plain, T, S, n_comp, n_bg)
+        out["chosen_vs_plain_unranked"]["reference"] = (
+            "plain FP64 GPU pipeline without ranking (the reference's picks): another fit, "
+            "not a precision figure")
+        out["unranked_chosen_vs_plain_unranked"] = acc.compare(unranked, plain, T, S, n_comp, n_bg)
+        m_same = out["chosen_vs_plain_same_ranking"]["diff"]["max_sigma"]
+        m_unr = out["unranked_chosen_vs_plain_unranked"]["diff"]["max_sigma"]
+        out["gate"] = {
+            "uses": "chosen_vs_plain_same_ranking (ranked headline) and "
+                    "unranked_chosen_vs_plain_unranked (chosen_unranked throughput)",
+            "max_sigma_same_ranking": m_same, "max_sigma_unranked": m_unr, "bar": SIGMA_BAR,
+            "pass": bool(m_same <= SIGMA_BAR and m_unr <= SIGMA_BAR),
+            "note": "the ranking picks other substamps, so the ranked chosen image is another "
+                    "valid fit; against the unranked plain image it is compared in "
+                    "chosen_vs_plain_unranked and ranking_effect, not gated"}
         out["ranking_effect"] = acc.compare(chosen, unranked, T, S, n_comp, n_bg)
         out["ranking_effect"]["ksc_refills"] = [int(uctx.scalar("ksc_refills")),
                                                 int(ctx.scalar("ksc_refills"))]
@@ -315,8 +374,9 @@ def accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx=None, uctx=None):
                "solution": oracle_res.array("solution", "float64"),
                "kernSum": oracle_res.scalar("kernSum"),
                "convTemplate": oracle_res.scalar("convTemplate")}
+        mixed = run_result(xbach, uctx) if uctx is not None else chosen
         key = "mixed_unranked_vs_fp64_oracle" if uctx is not None else "chosen_vs_fp64_oracle"
-        out[key] = acc.compare(unranked, ref, T, S, n_comp, n_bg)
+        out[key] = acc.compare(mixed, ref, T, S, n_comp, n_bg)
         out["plain_vs_fp64_oracle"] = acc.compare(plain, ref, T, S, n_comp, n_bg)
     return out
 
@@ -661,8 +721,8 @@ def main():
                  "fill_w", "fill_finish", "gram_qb", "stamp_test_fit", "cd_select", "weights",
                  "stamp_dots", "build_matrix", "build_rhs", "global_lu", "global_lubksb",
                  "kernel_sum", "sigs", "cd_merit", "ksc_check", "conv_sub", "gram",
-                 "global_ldl", "lu_fallback", "global_solve", "mx_build", "mx_scatter",
-                 "rank_score"):
+                 "fill_gram", "gram_scatter", "global_ldl", "lu_fallback", "global_solve",
+                 "mx_build", "mx_scatter", "rank_score"):
         ms, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_total": ms / args.steps, "launches": n / args.steps}
@@ -691,43 +751,51 @@ def main():
 
     # ---- the headline: B frame pairs per step through the batch API ----
     jst = torch.cuda.Stream()
-    if B > 1:
-        batch = xbach.Batch(params, device=local, workers=max(1, min(args.workers, B)))
-        batch.set_stream(jst.cuda_stream)
-        dC = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
-        dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
-        for i in range(batch.n_workers):
-            with_rank(batch.worker(i))
-        if args.mode == "mixed":
-            batch.set_option("ldl_cluster", args.ldl_cluster)
-        if use_graph:
+    dC = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
+    dD = [torch.empty((h, w), dtype=torch.float32, device="cuda") for _ in range(B)]
+
+    def make_batch(bparams, ranked, graphs):
+        bt = xbach.Batch(bparams, device=local, workers=max(1, min(args.workers, B)))
+        bt.set_stream(jst.cuda_stream)
+        if ranked:
+            for i in range(bt.n_workers):
+                ranker.enable(bt.worker(i), rank_w, policy=1, tau=0.5)
+        if bparams.mode == xbach.XB_MODE_MIXED:
+            bt.set_option("ldl_cluster", args.ldl_cluster)
+        if graphs:
             # every worker captures its graph before the timed steps
-            batch.set_option("graph", 1)
-            for i in range(batch.n_workers):
-                batch.worker(i).run_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h,
-                                           dC[0].data_ptr(), dD[0].data_ptr())
+            bt.set_option("graph", 1)
+            for i in range(bt.n_workers):
+                bt.worker(i).run_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h,
+                                        dC[0].data_ptr(), dD[0].data_ptr())
             torch.cuda.synchronize()
 
-        def run_batch():
-            batch.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], [w] * B,
-                           [h] * B, [t.data_ptr() for t in dC], [t.data_ptr() for t in dD],
-                           device=True)
+        def run():
+            bt.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], [w] * B,
+                        [h] * B, [t.data_ptr() for t in dC], [t.data_ptr() for t in dD],
+                        device=True)
+        return bt, run
 
-        for _ in range(args.warmup):
-            run_batch()
+    def time_batch(bt, run, steps, warmup):
+        for _ in range(warmup):
+            run()
         torch.cuda.synchronize()
-        workers = [batch.worker(i) for i in range(batch.n_workers)]
-        l0 = sum(wk.launches() for wk in workers)
+        wks = [bt.worker(i) for i in range(bt.n_workers)]
+        l0 = sum(wk.launches() for wk in wks)
         with ClockSampler(local) as clk:
-            t_max = max_ranks(timed(run_batch, jst, args.steps))
-        launches = sum(wk.launches() for wk in workers) - l0
-        clocks = clk.summary()
+            tm = max_ranks(timed(run, jst, steps))
+        return tm, sum(wk.launches() for wk in wks) - l0, clk.summary()
+
+    if B > 1:
+        batch, run_batch = make_batch(params, use_rank, use_graph)
+        t_max, launches, clocks = time_batch(batch, run_batch, args.steps, args.warmup)
     else:
         with ClockSampler(local) as clk:
             t_max = max_ranks(timed(single, cst, args.steps))
         launches = launches_single
         clocks = clk.summary()
     value = job_value(world, B, args.steps, t_max)
+    d0_headline = dD[0].clone() if B > 1 else None  # later batches reuse the output buffers
 
     # ---- end to end: host frames (pinned) in, host images out ----
     hT = [torch.from_numpy(f[0]).pin_memory() for f in frames]
@@ -757,18 +825,23 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return 0
-    hbm_peak, _, peak_src = measured_peaks()
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
     dominant = max(kernels, key=lambda k: kernels[k]["ms_total"]) if kernels else None
-    roof = None
-    if "conv_sub" in kernels:
-        cs = kernels["conv_sub"]
-        roof = roofline_for("conv_sub", cs["ms_total"] / cs["launches"], n_pix, args.mode, hbm_peak)
-    if roof is not None:
-        roof["peak_source"] = peak_src
-    bf16_peak = measured_peaks()[1]
-    roof_tc = gram_tensor_roofline(kernels, ctx, bf16_peak) if args.mode == "mixed" else None
     fp32_peak, fp64_peak = xbach.measure_fma_peaks(local)
-    roof_pipe = cuda_core_rooflines(kernels, params, n_pix, args.mode, fp32_peak, fp64_peak)
+    stamps = ctx.scalar("nstamps0") + ctx.scalar("nstamps1") + ctx.scalar("ksc_refills")
+    peaks = {"hbm": hbm_peak, "bf16": bf16_peak, "fp32": fp32_peak, "fp64": fp64_peak,
+             "hbm_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+             "bf16_source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)",
+             "fma_source": "measured in this run by xb_measure_fma_peaks (MEASURED_PEAKS.json "
+                           "has no FP32/FP64 CUDA-core entry)"}
+    roofs = rooflines(kernels, params, n_pix, args.mode, stamps, peaks)
+    # the contract's object: the kernel with the most device time per frame
+    roof = dict(roofs.get(dominant, {})) if dominant in roofs else None
+    if roof is not None and "bound" not in roof:
+        roof = dict(next(iter(roof.values())))
+    if roof is not None:
+        roof["kernel"] = dominant
+        roof["traffic"] = None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -786,7 +859,7 @@ def main():
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "ldl_cluster": args.ldl_cluster if args.mode == "mixed" else None},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
-        "roofline_tensor": roof_tc, "roofline_cuda_cores": roof_pipe,
+        "rooflines": roofs,
         "single_frame": {"value": single_value, "unit": UNIT,
                          "ms_per_step": single_ms / args.steps, "gpu_launches": launches_single,
                          "path": "stages, host-driven (per-kernel timers on)"},
@@ -795,26 +868,59 @@ def main():
     }
     oracle_res = None
     if world == 1 and args.cpu_runs > 0:
-        _, threads, times, oracle_res = cpu_frames_per_s(T, S, info, args.cpu_runs)
+        # the first --cpu-runs frame pairs of the batch, one oracle run each
+        times = []
+        threads = os.cpu_count() or 1
+        for i in range(args.cpu_runs):
+            Ti, Si, infoi = frames[i % B]
+            _, threads, ti, res = cpu_frames_per_s(Ti, Si, infoi, 1)
+            times.append(ti[0])
+            if i == 0:
+                oracle_res = res
         med = statistics.median(times)
         line["cpu_baseline"] = {"value": 1.0 / med, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"median of {args.cpu_runs} full 2048x2048 frame pairs "
-                                          f"(FP64 oracle, OpenMP over {threads} host threads)",
+                                "sample": f"median over the batch's first {args.cpu_runs} frame "
+                                          f"pairs, one full 2048x2048 pair each (FP64 oracle, "
+                                          f"OpenMP over {threads} host threads)",
                                 "seconds_per_frame": times}
         if args.cpu_single:
             _, _, t1, _ = cpu_frames_per_s(T, S, info, 1, threads=1)
             line["cpu_baseline"]["single_thread"] = {"value": 1.0 / t1[0], "unit": UNIT,
                                                      "cores": 1, "seconds_per_frame": t1[0]}
-    if args.mode == "mixed":
-        # the plain FP64 GPU pipeline, one pair per step: the denominator of the
-        # chosen-vs-plain ratio, and the acceptance reference
+    if args.mode == "mixed" and world == 1:
+        if B > 1:
+            batch.close()
+            # the chosen pipeline without the learned ranking, same batch
+            if use_rank:
+                ubatch, run_u = make_batch(params, False, use_graph)
+                u_ms, _, u_clk = time_batch(ubatch, run_u, args.steps, args.warmup)
+                line["chosen_unranked"] = {"value": B * args.steps / (u_ms / 1000.0), "unit": UNIT,
+                                           "ms_per_step": u_ms / args.steps, "clocks": u_clk,
+                                           "config": "same batch, frame graphs, no ranking"}
+                ubatch.close()
+            # the plain FP64 GPU pipeline through the same batch API: same
+            # pairs, same workers, stages host-driven (plain mode has no graphs)
+            pparams = frame_params(xbach, info, xbach.XB_MODE_PLAIN)
+            pbatch, run_p = make_batch(pparams, False, False)
+            p_steps = max(1, min(args.steps, 3))
+            p_ms, _, p_clk = time_batch(pbatch, run_p, p_steps, 1)
+            line["plain_gpu_batched"] = {"value": B * p_steps / (p_ms / 1000.0), "unit": UNIT,
+                                         "ms_per_step": p_ms / p_steps, "steps": p_steps,
+                                         "frames_per_step": B, "workers": min(args.workers, B),
+                                         "clocks": p_clk}
+            pbatch.close()
+        # the plain pipeline one pair at a time, and the acceptance reference
         pctx = xbach.Context(frame_params(xbach, info, xbach.XB_MODE_PLAIN), device=local)
         make_pipeline(pctx)()
         p_steps = max(1, min(args.steps, 3))
         p_ms = timed(make_pipeline(pctx), torch.cuda.ExternalStream(pctx.stream()), p_steps)
-        line["plain_gpu"] = {"value": p_steps / (p_ms / 1000.0), "unit": UNIT,
-                             "ms_per_step": p_ms / p_steps, "steps": p_steps}
-        line["chosen_over_plain"] = value / line["plain_gpu"]["value"]
+        line["plain_gpu_single"] = {"value": p_steps / (p_ms / 1000.0), "unit": UNIT,
+                                    "ms_per_step": p_ms / p_steps, "steps": p_steps}
+        plain_ref = line.get("plain_gpu_batched", line["plain_gpu_single"])
+        line["chosen_over_plain"] = value / plain_ref["value"]
+        line["chosen_over_plain_basis"] = ("plain_gpu_batched (same batch API, pairs and workers)"
+                                           if "plain_gpu_batched" in line else "plain_gpu_single")
+        line["chosen_over_plain_single"] = value / line["plain_gpu_single"]["value"]
         make_pipeline(ctx)()
         prctx = uctx = None
         if use_rank:
@@ -826,7 +932,8 @@ def main():
         torch.cuda.synchronize()
         line["accuracy"] = accuracy(xbach, ctx, pctx, oracle_res, T, S, params, prctx, uctx)
         if B > 1:
-            same = bool(torch.equal(dD[0].cpu(), torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))))
+            same = bool(torch.equal(d0_headline.cpu(),
+                                    torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))))
             line["accuracy"]["batch_frame0_equals_single"] = same
     print(json.dumps(line), flush=True)
     if world > 1:
