@@ -1,5 +1,29 @@
 // xbach_oracle.cpp — CPU oracle of the X-BACH difference-imaging path.
 //
+// This file restates, as a checker, the algorithms of D0V4HKIIN/Thesis-EMX-BACH
+// (X-BACH), which is distributed under the following notice:
+//
+//   The MIT License (MIT)
+//
+//   Copyright (c) 2024 MindRoad Öst AB
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of
+//   this software and associated documentation files (the "Software"), to deal in
+//   the Software without restriction, including without limitation the rights to
+//   use, copy, modify, merge, publish, distribute, sublicense, and/or sell copies of
+//   the Software, and to permit persons to whom the Software is furnished to do so,
+//   subject to the following conditions:
+//
+//   The above copyright notice and this permission notice shall be included in all
+//   copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR
+//   IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY, FITNESS
+//   FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE AUTHORS OR
+//   COPYRIGHT HOLDERS BE LIABLE FOR ANY CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER
+//   IN AN ACTION OF CONTRACT, TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN
+//   CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
+//
 // TEST INFRASTRUCTURE ONLY: the checker used by tests/, by the smoke test and
 // by the benchmark's CPU-baseline leg.  It restates, sequentially and in
 // FP64, the host code (src/bach.cpp, src/sssUtil.cpp, src/cmvUtil.cpp,
@@ -15,7 +39,7 @@
 //     doubles is (a < b ? b : a) (OpenCL common-function definition);
 //   * float->int conversions of the histogram index saturate (as the GPU
 //     cvt instruction does) instead of being undefined;
-//   * the substamp threshold loop of findSubStamps (sss.cl:471-557) is capped
+//   * the substamp threshold loop of findSubStamps (sss.cl:404-490) is capped
 //     at 256 passes; it only exceeds ~6 when the sky statistics are NaN, where
 //     the reference would loop forever.
 // OpenMP parallelises over stamps, entries and pixel rows; every output's
@@ -239,7 +263,7 @@ void sigmaClip(const double* data, int count, double* mean, double* stdDev,
 }
 
 // ---------------------------------------------------------------- ran1 ---
-// Numerical Recipes ran1 as written in cl_kern/sss.cl:108-146 (three LCGs
+// Numerical Recipes ran1 as written in cl_kern/sss.cl:52-79 (three LCGs
 // and a 97-entry shuffle table, `long` = 64-bit).
 struct Ran1 {
   int idum;
@@ -277,10 +301,10 @@ struct Ran1 {
 };
 
 // ------------------------------------------------------------ calcStats --
-// src/bachUtil.cpp:130-280: sampleStamp (sss.cl:148-183), pad (:185-192),
-// bitonic sortSamples (:202-217, host loop bachUtil.cpp:229-240), maskStamp
-// (:224-255), per-stamp sigmaClip (bachUtil.cpp:255-266), createHistogram
-// (:257-391).
+// src/bachUtil.cpp:130-280: sampleStamp (sss.cl:81-116), pad (:118-133),
+// bitonic sortSamples (:135-150, host loop bachUtil.cpp:229-240), maskStamp
+// (:157-188), per-stamp sigmaClip (bachUtil.cpp:255-266), createHistogram
+// (:190-324).
 struct AllStamps {
   int n = 0;
   std::vector<int> cx, cy, sx, sy;
@@ -439,8 +463,8 @@ int calcStats(xbo_handle& o, const AllStamps& st, int which,
 }
 
 // -------------------------------------------------------- findSubStamps --
-// src/sssUtil.cpp:40-104 -> cl_kern/sss.cl:448-572 (checkSStamp :393-428,
-// sortSubStamps :430-446).  One stamp at a time; writes only inside the
+// src/sssUtil.cpp:40-104 -> cl_kern/sss.cl:381-505 (checkSStamp :326-361,
+// sortSubStamps :363-379).  One stamp at a time; writes only inside the
 // stamp's own window, so stamps are independent.
 double checkSStamp(xbo_handle& o, const std::vector<double>& img, double sky,
                    double fwhm, int mx, int my, int cx, int cy, int sx, int sy,
@@ -1446,7 +1470,7 @@ int sssPass(xbo_handle& o, AllStamps& st, int passIdx) {
   st.cy.assign(st.n, 0);
   st.sx.assign(st.n, 0);
   st.sy.assign(st.n, 0);
-  // createStampBounds: cl_kern/sss.cl:86-105
+  // createStampBounds: cl_kern/sss.cl:19-38
   for(int id = 0; id < st.n; id++) {
     int sxI = id % o.stampsx, syI = id / o.stampsx;
     int startX = sxI * w / o.stampsx, startY = syI * h / o.stampsy;

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 def stamp_geometry(w, h, nx, ny, fsw):
     """{x, y, width, height} of every grid stamp (createStampBounds,
-    cl_kern/sss.cl:86-105)."""
+    cl_kern/sss.cl:19-38)."""
     g = np.zeros((nx * ny, 4), np.int32)
     for i in range(nx * ny):
         sx, sy = i % nx, i // nx

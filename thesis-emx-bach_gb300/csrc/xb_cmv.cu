@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(FILL_THREADS)
     win[i] = (float)img[(size_t)gx + (size_t)gy * w];
   }
   __syncthreads();
-  // Y pass (cmv.cl:441-477): v accumulates in float, products in double
+  // Y pass (cmv.cl:70-106): v accumulates in float, products in double
   for(int p = tid; p < th * tw; p += FILL_THREADS) {
     const int row = p / tw, col = p % tw;
     float v = 0.0f;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(FILL_THREADS)
     const int n = gMembers[m];
     for(int i = tid; i < fK; i += FILL_THREADS) fx[i] = fX[(size_t)n * fK + i];
     __syncthreads();
-    // X pass (cmv.cl:479-506)
+    // X pass (cmv.cl:108-135)
     for(int p = tid; p < wCols; p += FILL_THREADS) {
       const int row = p / fSS, ii = p % fSS;
       double w0 = 0.0;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(FILL_THREADS)
   }
 }
 
-// convStampOdd (cmv.cl:508-525) and convStampBg (:527-564).
+// convStampOdd (cmv.cl:137-154) and convStampBg (:156-193).
 __global__ void __launch_bounds__(FILL_THREADS)
     k_fill_finish(const int* __restrict__ list, const int* __restrict__ count,
                   const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(FILL_THREADS)
     }
 }
 
-// createQ (cmv.cl:566-586) and createB (:588-619) for one stamp per CTA.
+// createQ (cmv.cl:195-215) and createB (:217-248) for one stamp per CTA.
 // Q: each thread owns up to GQ_E lower-triangle entries and accumulates them
 // over K in ascending order while W tiles stream through shared memory.
 constexpr int GQ_KT = 32, GQ_E = 8;

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(CONV_THREADS)
   }
   __syncthreads();
   if(tid == 0) {
-    // aks: |kernel| summed in the tap order of conv.cl:126-143 (j, i ascending)
+    // aks: |kernel| summed in the tap order of conv.cl:54-70 (j, i ascending)
     double s = 0.0;
     for(int jk = 2 * hK; jk >= 0; jk--)
       for(int ik = 2 * hK; ik >= 0; ik--) s += fabs(kern[ik + jk * fK]);
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(CONV_THREADS)
   }
 }
 
-// Border pixels: conv = diff = 1e-30 (conv.cl:167, sub.cl:209); the mask
+// Border pixels: conv = diff = 1e-30 (conv.cl:95, sub.cl:24); the mask
 // keeps its value plus maskAfterConv's bits.
 // Per-pixel kernel (option convPerPixel; no counterpart in the reference,
 // whose conv.cl evaluates the kernel once per fK x fK block at the block

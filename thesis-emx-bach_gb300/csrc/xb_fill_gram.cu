@@ -12,27 +12,36 @@
 //      lies inside the frame and the frame's rows are 16-byte multiples, else
 //      with clamped loads (the reference clamps at the edge);
 //   2. the Y pass of every unique Y filter (convStampY, cl_kern/cmv.cl:70-106)
-//      into shared memory, eight output rows per thread from one sliding
-//      column of the window, the filter in registers;
+//      into shared memory, eight output rows per thread from one window
+//      column;
 //   3. the X pass of every basis function (convStampX, :108-135), eight
-//      output pixels per thread from one sliding row, the even/even
-//      subtraction (convStampOdd, :137-154) against W[0] kept in shared
-//      memory, the background rows (convStampBg, :156-193) and the image row
-//      of createB (:218-248); W goes to global memory (hi for the chi^2 of
-//      k_sigs_f32, lo as scratch for step 4) while each row's largest |hi|
-//      is collected;
-//   4. the exact sliced Gram of xb_tc.cuh: the CTA's own W comes back from L2
-//      chunk by chunk, is sliced with the row exponents into BF16 digits and
-//      multiplied by tcgen05.mma into TMEM; the int64 epilogue writes G.
-// The arithmetic of steps 2-3 is that of the separate kernels (xb_df.cuh,
-// same operations in the same order) and step 4 is the same code, so G and W
-// are theirs bit for bit (tests/test_gpu_fill_gram.py).
+//      output pixels per thread from one row, the even/even subtraction
+//      (convStampOdd, :137-154) against W[0] kept in shared memory, the
+//      background rows (convStampBg, :156-193) and the image row of createB
+//      (:218-248); W goes to global memory (hi for the chi^2 of k_sigs_f32, lo
+//      as scratch for step 4) while each row's largest |hi| is collected.
+//      Steps 2-3 run in passes of at most FG_GP Y filters (the pass holding
+//      basis function 0 first; the default basis has 21 distinct Y filters,
+//      so 3 passes), so that the Y outputs of one pass fit beside everything
+//      else in ~85 KB;
+//   4. the exact sliced Gram of xb_tc.cuh: each thread loads its units of the
+//      CTA's own W back from L2 chunk by chunk, slices them with the row
+//      exponents into BF16 digits, one thread multiplies them by tcgen05.mma
+//      into TMEM, and the int64 epilogue (shared-memory atomics) writes G.
+// At ~96 KB of shared memory two CTAs share an SM: one's Y/X passes (FP32
+// pipe) overlap the other's Gram (tensor pipe, L2, barriers), and other
+// kernels of concurrent frames fit beside them.  The arithmetic of steps 2-3
+// is that of the separate kernels (xb_df.cuh, same operations in the same
+// order) and step 4 forms the same digits and exact sums, so G and W are
+// theirs bit for bit (tests/test_gpu_fill_gram.py).
 //
 // Limits (else the separate kernels run): FP32 images, kernel half-width 10
-// (the filter loops are unrolled for 21 taps), substamps up to 31 x 31,
-// R = basis + background + 1 <= 64 rows, background order <= 2 (its values
-// are then exact products of two floats), no weighted fit.
+// (FK = 21 taps), substamps up to 31 x 31, R = basis + background + 1 <= 64
+// rows, at most FG_MAXG distinct Y filters, background order <= 2 (its
+// values are then exact products of two floats), no weighted fit.
 #include <cuda.h>
+
+#include <algorithm>
 
 #include "xb_df.cuh"
 #include "xb_internal.h"
@@ -42,15 +51,18 @@ namespace xb {
 
 namespace {
 
-constexpr int FG_THREADS = 512;
-constexpr int FG_HK = 10;  // the kernel half-width the fused kernel is built for
-constexpr int FG_R8 = 8;   // outputs per thread item (rows of the Y pass, pixels of the X pass)
+constexpr int FG_THREADS = 384;
+constexpr int FG_HK = 10;   // the kernel half-width the fused kernel is built for
+constexpr int FG_R8 = 8;    // outputs per thread item (rows of the Y pass, pixels of the X pass)
+constexpr int FG_GP = 7;    // Y filters per pass
+constexpr int FG_MAXPASS = 4;
+constexpr int FG_MAXG = FG_MAXPASS * FG_GP;
 
 // Shared-memory layout of the fill (steps 1-3); the Gram (step 4) and the
 // epilogue reuse the same area from offset 0.
 struct FgLayout {
   int tw, fSS, ldWin, winRows, ldY;
-  size_t oWin, oFy, oFx, oY, oW0, fill, total;
+  size_t oWin, oF, oW0, oY, fill, total;
 };
 __host__ __device__ inline FgLayout fgLayout(int hSS, int hK, int nGroups, int nPSF) {
   FgLayout L;
@@ -60,17 +72,16 @@ __host__ __device__ inline FgLayout fgLayout(int hSS, int hK, int nGroups, int n
   L.winRows = L.tw + FG_R8;           // rows past tw are read only by discarded outputs
   L.ldY = L.tw + FG_R8;               // odd stride: the X items' rows fall on distinct banks
   if(L.ldY % 2 == 0) L.ldY++;
-  const int fK = 2 * hK + 1;
+  const int fK = 2 * hK + 1, gp = nGroups < FG_GP ? nGroups : FG_GP;
   auto al = [](size_t v) { return (v + 127) / 128 * 128; };
   L.oWin = 0;
-  L.oFy = al(L.oWin + (size_t)L.ldWin * L.winRows * 4);
-  L.oFx = al(L.oFy + (size_t)2 * nGroups * fK * 4);
-  L.oY = al(L.oFx + (size_t)2 * nPSF * fK * 4);
-  L.oW0 = al(L.oY + (size_t)nGroups * L.fSS * L.ldY * 4);
-  L.fill = al(L.oW0 + (size_t)2 * L.fSS * L.fSS * 4);
+  L.oF = al(L.oWin + (size_t)L.ldWin * L.winRows * 4);
+  L.oW0 = al(L.oF + (size_t)2 * (nPSF + nGroups) * fK * 4);
+  L.oY = al(L.oW0 + (size_t)2 * L.fSS * L.fSS * 4);
+  L.fill = al(L.oY + (size_t)gp * L.fSS * L.ldY * 4);
   size_t m = L.fill;
-  if((size_t)tc::CHUNK_SMEM > m) m = tc::CHUNK_SMEM;
-  if((size_t)tc::EPI_BYTES > m) m = tc::EPI_BYTES;
+  if((size_t)2 * tc::OPBUF > m) m = 2 * tc::OPBUF;
+  if((size_t)tc::EPI2_BYTES > m) m = tc::EPI2_BYTES;
   L.total = m + 1024;  // 1024-byte alignment of the operand buffers
   return L;
 }
@@ -86,16 +97,22 @@ struct FillGramArgs {
   const int2* ssxy;
   int maxSS;
   const float* fSplit;  // the filters as float pairs (xb_ctx::dFSplit)
-  const int* gStart;    // unique Y filters: members gMembers[gStart[g] .. gStart[g+1])
-  const int* gMembers;
-  int nGroups, g0;      // g0: the group of basis function 0
   const int* kx;
   const int* ky;
-  int nPSF;
+  int nPSF, nGroups;
   const int2* bgXY;
   int nBG;
   int hSS, wRows, ldW;
   int useTma;
+  // pass plan: pass p holds the Y filters gOrder[gBeg[p] .. gBeg[p+1]) in
+  // ytmp slots 0.. (slot[g]) and the X rows rows[rBeg[p] .. rBeg[p+1])
+  // (basis function 0 apart: its filter g0 = gOrder[0] runs first alone)
+  int nPass;
+  int gBeg[FG_MAXPASS + 1], rBeg[FG_MAXPASS + 1];
+  unsigned char gOrder[FG_MAXG];
+  unsigned char slot[FG_MAXG];
+  unsigned char rows[MAX_NPSF];
+  unsigned char groupOf[MAX_NPSF];
   float* W;    // [stamp][wRows][ldW] hi
   float* Wlo;  // [stamp][wRows][ldW] lo
   double* G;   // [list entry][R][R]
@@ -142,16 +159,15 @@ __device__ __forceinline__ void maxBits(unsigned* slot, float m) {
   atomicMax(slot, __float_as_uint(m));  // m >= 0: the bit patterns are ordered
 }
 
-__global__ void __launch_bounds__(FG_THREADS, 1)
-    k_fill_gram(const __grid_constant__ CUtensorMap tmap, const FillGramArgs a) {
+__global__ void __launch_bounds__(FG_THREADS, 2)
+    k_fill_gram(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ FillGramArgs a) {
   using namespace tc;
-  constexpr int HK = FG_HK, FK = 2 * HK + 1;
+  constexpr int NT = FG_THREADS, HK = FG_HK, FK = 2 * HK + 1;
   extern __shared__ __align__(1024) unsigned char fg_s[];
   __shared__ float imgRow[1024];  // K <= 961 pixels, padded to whole chunks
   __shared__ int expo[RB];
   __shared__ unsigned rowMax[RB];
   __shared__ unsigned char evenRow[MAX_NPSF];
-  __shared__ unsigned char groupOf[MAX_NPSF];
   __shared__ unsigned long long bars[3];  // two operand buffers, the window copy
   __shared__ uint32_t tmemBase;
   if(a.liveN && (int)blockIdx.x >= *a.liveN) return;  // before any barrier or TMEM allocation
@@ -163,11 +179,11 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
   double* Gs = a.G + (size_t)t * R * R;
   if(!(a.cur[s] < a.count[s])) {
     // no substamp left: W and G are zero (what the separate kernels give)
-    for(int i = tid; i < a.wRows * ldW; i += FG_THREADS) {
+    for(int i = tid; i < a.wRows * ldW; i += NT) {
       Ws[i] = 0.f;
       Wl[i] = 0.f;
     }
-    for(int i = tid; i < R * R; i += FG_THREADS) Gs[i] = 0.0;
+    for(int i = tid; i < R * R; i += NT) Gs[i] = 0.0;
     return;
   }
   const unsigned long long deadline = timerNs() + WAIT_NS;
@@ -175,13 +191,13 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
   const FgLayout L = fgLayout(a.hSS, HK, a.nGroups, nPSF);
   const int tw = L.tw, ldWin = L.ldWin, ldY = L.ldY;
   float* win = (float*)(buf + L.oWin);
-  float* fyh = (float*)(buf + L.oFy);
-  float* fyl = fyh + a.nGroups * FK;
-  float* fxh = (float*)(buf + L.oFx);
+  float* fxh = (float*)(buf + L.oF);
   float* fxl = fxh + nPSF * FK;
-  float* ytmp = (float*)(buf + L.oY);
+  float* fyh = fxl + nPSF * FK;
+  float* fyl = fyh + a.nGroups * FK;
   float* w0h = (float*)(buf + L.oW0);
   float* w0l = w0h + K;
+  float* ytmp = (float*)(buf + L.oY);
 
   const int2 c = a.ssxy[(size_t)s * a.maxSS + a.cur[s]];
   const int xHalf = a.hSS + HK, wx0 = c.x - xHalf, wy0 = c.y - xHalf;
@@ -205,24 +221,13 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
           : "memory");
     }
   }
-  // filters (hi + lo), basis tables, row maxima; the window by plain loads
-  // when TMA does not apply
   // the filters as float pairs: X [nPSF][FK] hi, lo; Y [group][FK] hi, lo
-  for(int i = tid; i < nPSF * FK; i += FG_THREADS) {
-    fxh[i] = a.fSplit[i];
-    fxl[i] = a.fSplit[nPSF * FK + i];
-  }
-  for(int i = tid; i < a.nGroups * FK; i += FG_THREADS) {
-    fyh[i] = a.fSplit[2 * nPSF * FK + i];
-    fyl[i] = a.fSplit[(2 * nPSF + a.nGroups) * FK + i];
-  }
-  for(int n = tid; n < nPSF; n += FG_THREADS)
+  for(int i = tid; i < 2 * (nPSF + a.nGroups) * FK; i += NT) fxh[i] = a.fSplit[i];
+  for(int n = tid; n < nPSF; n += NT)
     evenRow[n] = (n > 0 && a.kx[n] % 2 == 0 && a.ky[n] % 2 == 0) ? 1 : 0;
-  for(int g = tid; g < a.nGroups; g += FG_THREADS)
-    for(int m = a.gStart[g]; m < a.gStart[g + 1]; m++) groupOf[a.gMembers[m]] = (unsigned char)g;
   if(tid < RB) rowMax[tid] = 0u;
   if(!tma) {
-    for(int i = tid; i < tw * tw; i += FG_THREADS) {
+    for(int i = tid; i < tw * tw; i += NT) {
       const int gx = min(max(wx0 + i % tw, 0), a.w - 1);
       const int gy = min(max(wy0 + i / tw, 0), a.h - 1);
       win[(i / tw) * ldWin + i % tw] = a.conv[(size_t)gx + (size_t)gy * a.w];
@@ -239,22 +244,18 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
     ok = __syncthreads_or(late) == 0;
   }
 
-  // ---- Y pass: item (group, block of 8 output rows, window column) ----------
-  const int nRB = (fSS + FG_R8 - 1) / FG_R8;
-  auto yItem = [&](int g, int rb, int col) {
-    const int r0 = rb * FG_R8;
+  const int nRB = (fSS + FG_R8 - 1) / FG_R8;  // row blocks of the Y pass
+  const int nXB = (fSS + FG_R8 - 1) / FG_R8;  // pixel blocks of the X pass
+  const int yPer = nRB * tw, xPer = fSS * nXB;
+  // Y item i of filter g: rows block i / tw, window column i % tw
+  auto yItem = [&](int g, int i) {
+    const int r0 = (i / tw) * FG_R8, col = i % tw;
     float v[FG_R8];
     yPass8<FK>(win + r0 * ldWin + col + dx, ldWin, fyh + g * FK, fyl + g * FK, v);
-    float* yo = ytmp + ((size_t)g * fSS + r0) * ldY + col;
+    float* yo = ytmp + ((size_t)a.slot[g] * fSS + r0) * ldY + col;
 #pragma unroll
     for(int j = 0; j < FG_R8; j++)
       if(r0 + j < fSS) yo[j * ldY] = v[j];
-  };
-  // ---- X pass: item (basis function, output row, block of 8 pixels) ----------
-  const int nXB = (fSS + FG_R8 - 1) / FG_R8;
-  auto xItem = [&](int n, int row, int xb, float (&hi)[FG_R8], float (&lo)[FG_R8]) {
-    xPass8<FK>(ytmp + ((size_t)groupOf[n] * fSS + row) * ldY + xb * FG_R8, fxh + n * FK,
-               fxl + n * FK, hi, lo);
   };
   // stores 8 outputs of row n starting at pixel p0 (nv of them valid) and
   // folds their largest |hi| into the row maximum
@@ -269,98 +270,102 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
       }
     maxBits(&rowMax[n], m);
   };
+  // X item i of row n: output row i / nXB, pixels from 8 (i % nXB)
+  auto xItem = [&](int n, int i) {
+    const int row = i / nXB, ii0 = (i % nXB) * FG_R8;
+    const int nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+    float hi[FG_R8], lo[FG_R8];
+    xPass8<FK>(ytmp + ((size_t)a.slot[a.groupOf[n]] * fSS + row) * ldY + ii0, fxh + n * FK,
+               fxl + n * FK, hi, lo);
+    if(n == 0) {
+#pragma unroll
+      for(int j = 0; j < FG_R8; j++)
+        if(j < nv) {
+          w0h[p0 + j] = hi[j];
+          w0l[p0 + j] = lo[j];
+        }
+    } else if(evenRow[n]) {
+#pragma unroll
+      for(int j = 0; j < FG_R8; j++)
+        if(j < nv) df::dfSub(hi[j], lo[j], w0h[p0 + j], w0l[p0 + j], hi[j], lo[j]);
+    }
+    putRow(n, p0, nv, hi, lo);
+  };
+  // background row b and the image row: item i of xPer
+  auto bgItem = [&](int b, int i) {
+    // the reference's form: float-normalised coordinates, FP64 powers, each
+    // an exact product of at most two floats at background order <= 2
+    const int row = i / nXB, ii0 = (i % nXB) * FG_R8;
+    const int nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+    const int ex = a.bgXY[b].x, ey = a.bgXY[b].y;
+    const float yf = df::floatNormF(c.y - a.hSS + row, a.h);
+    float hi[FG_R8], lo[FG_R8];
+#pragma unroll
+    for(int j = 0; j < FG_R8; j++) {
+      const float xf = df::floatNormF(c.x - a.hSS + ii0 + j, a.w);
+      float u = 1.f, v = 1.f;  // the two float factors
+      if(ex == 2) u = v = xf;
+      else if(ey == 2) u = v = yf;
+      else {
+        if(ex == 1) u = xf;
+        if(ey == 1) v = yf;
+      }
+      hi[j] = u * v;
+      lo[j] = fmaf(u, v, -hi[j]);  // exact: u v = hi + lo
+    }
+    putRow(nPSF + b, p0, nv, hi, lo);
+  };
+  auto imgItem = [&](int i) {
+    const int row = i / nXB, ii0 = (i % nXB) * FG_R8;
+    const int nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
+    const int gy = min(max(c.y - a.hSS + row, 0), a.h - 1);
+    float m = 0.f;
+    for(int j = 0; j < nv; j++) {
+      const int gx = min(max(c.x - a.hSS + ii0 + j, 0), a.w - 1);
+      const float v = a.other[(size_t)gx + (size_t)gy * a.w];
+      imgRow[p0 + j] = v;
+      m = fmaxf(m, fabsf(v));
+    }
+    maxBits(&rowMax[a.wRows], m);
+  };
 
-  // list A: the Y pass of basis function 0's filter
-  for(int it = tid; it < nRB * tw; it += FG_THREADS) yItem(a.g0, it / tw, it % tw);
+  const int g0 = a.gOrder[0];
+  // pass 0, list A: the Y pass of basis function 0's filter
+  for(int it = tid; it < yPer; it += NT) yItem(g0, it);
   __syncthreads();
-  // list B: W[0] (kept in shared memory for the even/even rows), and the Y
-  // pass of every other filter
+  // list B: W[0] (kept for the even/even rows), the Y pass of the pass's
+  // other filters, the background and image rows, the W and image padding
   {
-    const int nX0 = fSS * nXB, nYo = (a.nGroups - 1) * nRB * tw;
-    for(int it = tid; it < nX0 + nYo; it += FG_THREADS) {
-      if(it < nX0) {
-        const int row = it / nXB, xb = it % nXB;
-        float hi[FG_R8], lo[FG_R8];
-        xItem(0, row, xb, hi, lo);
-        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
-#pragma unroll
-        for(int j = 0; j < FG_R8; j++)
-          if(j < nv) {
-            w0h[p0 + j] = hi[j];
-            w0l[p0 + j] = lo[j];
-          }
-        putRow(0, p0, nv, hi, lo);
-      } else {
-        const int i = it - nX0, col = i % tw, rb = (i / tw) % nRB;
-        int g = i / (tw * nRB);
-        if(g >= a.g0) g++;
-        yItem(g, rb, col);
-      }
+    const int nG = a.gBeg[1] - 1;
+    const int n0 = xPer, n1 = n0 + nG * yPer, n2 = n1 + a.nBG * xPer, n3 = n2 + xPer;
+    for(int it = tid; it < n3; it += NT) {
+      if(it < n0) xItem(0, it);
+      else if(it < n1) yItem(a.gOrder[1 + (it - n0) / yPer], (it - n0) % yPer);
+      else if(it < n2) bgItem((it - n1) / xPer, (it - n1) % xPer);
+      else imgItem(it - n2);
     }
-  }
-  __syncthreads();
-  // list C: every other basis function, the background rows, the image row,
-  // and the zero padding of the W rows
-  {
-    const int nX = (nPSF - 1) * fSS * nXB, nB = a.nBG * fSS * nXB, nI = fSS * nXB;
-    for(int it = tid; it < nX + nB + nI; it += FG_THREADS) {
-      if(it < nX) {
-        const int n = 1 + it / (fSS * nXB), row = (it / nXB) % fSS, xb = it % nXB;
-        float hi[FG_R8], lo[FG_R8];
-        xItem(n, row, xb, hi, lo);
-        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
-        if(evenRow[n]) {
-#pragma unroll
-          for(int j = 0; j < FG_R8; j++)
-            if(j < nv) df::dfSub(hi[j], lo[j], w0h[p0 + j], w0l[p0 + j], hi[j], lo[j]);
-        }
-        putRow(n, p0, nv, hi, lo);
-      } else if(it < nX + nB) {
-        // the reference's form: float-normalised coordinates, FP64 powers,
-        // each an exact product of at most two floats at background order <= 2
-        const int i = it - nX, b = i / (fSS * nXB), row = (i / nXB) % fSS, xb = i % nXB;
-        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
-        const int ex = a.bgXY[b].x, ey = a.bgXY[b].y;
-        const float yf = df::floatNormF(c.y - a.hSS + row, a.h);
-        float hi[FG_R8], lo[FG_R8];
-#pragma unroll
-        for(int j = 0; j < FG_R8; j++) {
-          const float xf = df::floatNormF(c.x - a.hSS + ii0 + j, a.w);
-          float u = 1.f, v = 1.f;  // the two float factors
-          if(ex == 2) u = v = xf;
-          else if(ey == 2) u = v = yf;
-          else {
-            if(ex == 1) u = xf;
-            if(ey == 1) v = yf;
-          }
-          hi[j] = u * v;
-          lo[j] = fmaf(u, v, -hi[j]);  // exact: u v = hi + lo
-        }
-        putRow(nPSF + b, p0, nv, hi, lo);
-      } else {
-        const int i = it - nX - nB, row = i / nXB, xb = i % nXB;
-        const int ii0 = xb * FG_R8, nv = min(FG_R8, fSS - ii0), p0 = row * fSS + ii0;
-        const int gy = min(max(c.y - a.hSS + row, 0), a.h - 1);
-        float m = 0.f;
-        for(int j = 0; j < nv; j++) {
-          const int gx = min(max(c.x - a.hSS + ii0 + j, 0), a.w - 1);
-          const float v = a.other[(size_t)gx + (size_t)gy * a.w];
-          imgRow[p0 + j] = v;
-          m = fmaxf(m, fabsf(v));
-        }
-        maxBits(&rowMax[a.wRows], m);
-      }
-    }
-    // zero padding: W columns K..ldW-1 and the image row up to whole chunks
     const int padW = ldW - K, nChunkK = (K + KC - 1) / KC * KC;
-    for(int i = tid; i < a.wRows * padW; i += FG_THREADS) {
+    for(int i = tid; i < a.wRows * padW; i += NT) {
       const size_t o = (size_t)(i / padW) * ldW + K + i % padW;
       Ws[o] = 0.f;
       Wl[o] = 0.f;
     }
-    for(int k = K + tid; k < nChunkK; k += FG_THREADS) imgRow[k] = 0.f;
+    for(int k = K + tid; k < nChunkK; k += NT) imgRow[k] = 0.f;
   }
-  // the CTA's W stores before its own cp.async reads of them (step 4)
+  __syncthreads();
+  // list C: the pass's other X rows
+  for(int it = tid; it < (a.rBeg[1] - a.rBeg[0]) * xPer; it += NT)
+    xItem(a.rows[a.rBeg[0] + it / xPer], it % xPer);
+  // later passes: their Y filters into the freed slots, then their X rows
+  for(int p = 1; p < a.nPass; p++) {
+    __syncthreads();
+    for(int it = tid; it < (a.gBeg[p + 1] - a.gBeg[p]) * yPer; it += NT)
+      yItem(a.gOrder[a.gBeg[p] + it / yPer], it % yPer);
+    __syncthreads();
+    for(int it = tid; it < (a.rBeg[p + 1] - a.rBeg[p]) * xPer; it += NT)
+      xItem(a.rows[a.rBeg[p] + it / xPer], it % xPer);
+  }
+  // the CTA's W stores before its own reads of them (step 4)
   __syncthreads();
   if(tid < RB) expo[tid] = tid < R ? rowExponent(__uint_as_float(rowMax[tid])) : 0;
   if(warp == 0) tmemAlloc512(&tmemBase);
@@ -368,9 +373,9 @@ __global__ void __launch_bounds__(FG_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
-  if(!gramChunks<FG_THREADS>(Ws, Wl, a.wRows, ldW, R, K, imgRow, expo, buf, bars, tmem, deadline))
+  if(!gramChunksDirect<NT>(Ws, Wl, a.wRows, ldW, R, K, imgRow, expo, buf, bars, tmem, deadline))
     ok = false;
-  epilogue(tmem, (long long*)buf, expo, R, Gs);
+  epilogueAtomic(tmem, (long long*)buf, expo, R, Gs);
   if(tid == 0 && !ok) atomicOr(a.timeout, 1);
 }
 
@@ -401,7 +406,7 @@ bool fillGramFits(const xb_ctx* c) {
   if(g.hK != FG_HK || g.fSS > 31 || g.wRows + 1 > tc::RB || g.nPSF > MAX_NPSF) return false;
   if(c->p.backgroundOrder > 2) return false;
   const int nGroups = (int)c->basis.yGroupStart.size() - 1;
-  if(nGroups < 1 || nGroups > 255) return false;
+  if(nGroups < 1 || nGroups > FG_MAXG) return false;
   int optin = 0;
   if(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess)
     return false;
@@ -412,12 +417,9 @@ bool fillGramFits(const xb_ctx* c) {
 void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv, double* G,
                     const int* liveN) {
   const Geo& g = c->g;
+  const Basis& bs = c->basis;
   StampSetDev& S = c->set[si];
-  const int nGroups = (int)c->basis.yGroupStart.size() - 1;
-  int g0 = 0;
-  for(int gi = 0; gi < nGroups; gi++)
-    for(int m = c->basis.yGroupStart[gi]; m < c->basis.yGroupStart[gi + 1]; m++)
-      if(c->basis.yGroupMembers[m] == 0) g0 = gi;
+  const int nGroups = (int)bs.yGroupStart.size() - 1;
   const FgLayout L = fgLayout(g.hSS, g.hK, nGroups, g.nPSF);
   FillGramArgs a{};
   a.conv = (const float*)c->img[imgConv];
@@ -431,13 +433,10 @@ void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
   a.ssxy = S.ssxy;
   a.maxSS = g.maxSS;
   a.fSplit = c->dFSplit;
-  a.gStart = c->dYGroupStart;
-  a.gMembers = c->dYGroupMembers;
-  a.nGroups = nGroups;
-  a.g0 = g0;
   a.kx = c->dKx;
   a.ky = c->dKy;
   a.nPSF = g.nPSF;
+  a.nGroups = nGroups;
   a.bgXY = buf<int2>(c, "bgXY", g.nBG);
   a.nBG = g.nBG;
   a.hSS = g.hSS;
@@ -447,6 +446,31 @@ void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
   a.Wlo = S.Wlo;
   a.G = G;
   a.timeout = deviceStatus(c) + 1;  // the context's device-timeout word
+  // pass plan: basis function 0's filter first, then the others in order,
+  // FG_GP filters per pass; each pass's X rows are its filters' members
+  std::vector<int> order, groupOf(g.nPSF, 0);
+  for(int gi = 0; gi < nGroups; gi++)
+    for(int m = bs.yGroupStart[gi]; m < bs.yGroupStart[gi + 1]; m++) groupOf[bs.yGroupMembers[m]] = gi;
+  order.push_back(groupOf[0]);
+  for(int gi = 0; gi < nGroups; gi++)
+    if(gi != groupOf[0]) order.push_back(gi);
+  a.nPass = (nGroups + FG_GP - 1) / FG_GP;
+  int nr = 0;
+  for(int p = 0; p < a.nPass; p++) {
+    a.gBeg[p] = p * FG_GP;
+    a.rBeg[p] = nr;
+    const int gEnd = std::min(nGroups, (p + 1) * FG_GP);
+    for(int k = p * FG_GP; k < gEnd; k++) {
+      const int gi = order[k];
+      a.gOrder[k] = (unsigned char)gi;
+      a.slot[gi] = (unsigned char)(k - p * FG_GP);
+      for(int m = bs.yGroupStart[gi]; m < bs.yGroupStart[gi + 1]; m++)
+        if(bs.yGroupMembers[m] != 0) a.rows[nr++] = (unsigned char)bs.yGroupMembers[m];
+    }
+  }
+  a.gBeg[a.nPass] = nGroups;
+  a.rBeg[a.nPass] = nr;
+  for(int n = 0; n < g.nPSF; n++) a.groupOf[n] = (unsigned char)groupOf[n];
   // the window's tile copy: rows of the frame in 16-byte multiples, box
   // ldWin x tw floats (its x start is rounded down to 4 floats in the kernel)
   CUtensorMap tm;

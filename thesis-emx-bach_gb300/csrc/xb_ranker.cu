@@ -2,7 +2,7 @@
 //
 // The reference tries each stamp's substamps in order of brightness
 // (sss.cl:363-379) and replaces a substamp only after the global fit has
-// rejected it (ksc.cl:1-80, cdkscUtil.cpp:686-802), one refit per round of
+// rejected it (ksc.cl:1-72, cdkscUtil.cpp:686-802), one refit per round of
 // rejections.  A small network scores every candidate substamp from
 //   * 16 statistics of the template/science windows around it, and
 //   * the 2 x 31 x 31 window pair itself (sky-subtracted, peak-normalised),

@@ -13,6 +13,7 @@
 #include <climits>
 #include <cmath>
 
+#include "xb_device.cuh"
 #include "xb_internal.h"
 
 namespace xb {
@@ -30,7 +31,7 @@ __device__ __forceinline__ int satFloorToInt(double v) {
   return (int)f;
 }
 
-// Numerical Recipes ran1 (cl_kern/sss.cl:108-146): three LCGs with a
+// Numerical Recipes ran1 (cl_kern/sss.cl:52-79): three LCGs with a
 // 97-entry shuffle table; 64-bit integer state, exact.
 struct Ran1 {
   long long ix1, ix2, ix3;
@@ -69,36 +70,10 @@ struct Ran1 {
   }
 };
 
-// Block-wide exclusive scan of one int per thread (256 threads).
-__device__ __forceinline__ int blockExclusiveScan(int v, int* warpTot, int* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for(int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, o);
-    if(lane >= o) x += y;
-  }
-  if(lane == 31) warpTot[wid] = x;
-  __syncthreads();
-  if(threadIdx.x == 0) {
-    int s = 0;
-    for(int i = 0; i < (int)(blockDim.x >> 5); i++) {
-      int t = warpTot[i];
-      warpTot[i] = s;
-      s += t;
-    }
-    *total = s;
-  }
-  __syncthreads();
-  int r = warpTot[wid] + x - v;
-  __syncthreads();
-  return r;
-}
-
 // ------------------------------------------------------- stamp statistics --
-// One CTA per stamp: sampleStamp + pad + sortSamples (sss.cl:148-217),
-// maskStamp (:224-255), sigmaClip with maxIter 3 (bachUtil.cpp:255-266,
-// bach.cl:129-184) and createHistogram (sss.cl:257-391).
+// One CTA per stamp: sampleStamp + pad + sortSamples (sss.cl:81-150),
+// maskStamp (:157-188), sigmaClip with maxIter 3 (bachUtil.cpp:255-266,
+// bach.cl:129-184) and createHistogram (sss.cl:190-324).
 //
 // Every stamp seeds ran1 with -666, so all stamps draw the same sequence:
 // with `draws` (that sequence, precomputed on the host) the 32 candidates of
@@ -309,7 +284,7 @@ __global__ void __launch_bounds__(ST_THREADS)
     }
     wGood += __popc(__ballot_sync(0xffffffffu, g));
   }
-  const int wBase = blockExclusiveScan(lane == 0 ? wGood : 0, warpTot, &sTotal);
+  const int wBase = blockScanExcl(lane == 0 ? wGood : 0, warpTot, &sTotal);
   const int nGood = sTotal;
   int pos = __shfl_sync(0xffffffffu, wBase, 0);
   for(int b = w0; b < w1; b += 32) {
@@ -464,7 +439,7 @@ __global__ void __launch_bounds__(ST_THREADS)
   const double mean = sMean, invStd = 1.0 / sStd;
   thresholds(mean, invStd);
 
-  // ---- phase D: histogram sky / robust sigma (sss.cl:257-391) ----
+  // ---- phase D: histogram sky / robust sigma (sss.cl:190-324) ----
   if(tid == 0) {
     int sc = sCount;
     double upS = samples[(int)(0.9 * sc)];
@@ -623,11 +598,11 @@ __device__ __forceinline__ void orMask(uint16_t* m, size_t i, uint16_t bits) {
 }
 
 // ---------------------------------------------------------- substamp search --
-// One CTA per (stamp, image): findSubStamps (cl_kern/sss.cl:448-572).  The
+// One CTA per (stamp, image): findSubStamps (cl_kern/sss.cl:381-505).  The
 // reference scans the stamp in raster order, testing each pixel.  Between two
 // accepted substamps the mask does not change, so for every pixel of the stamp window
-// the reference's local-maximum search (sss.cl:494-526) and window check
-// (checkSStamp, :393-428) are tabulated once per mask state:
+// the reference's local-maximum search (sss.cl:427-459) and window check
+// (checkSStamp, :326-361) are tabulated once per mask state:
 //   * a separable sliding-window argmax over the qualifying pixels (largest
 //     value, ties to the first pixel in raster order: row pass keeps the
 //     smallest x, column pass the smallest y), keys compared as the bit
@@ -637,12 +612,12 @@ __device__ __forceinline__ void orMask(uint16_t* m, size_t i, uint16_t bits) {
 // Each pass then looks for the first candidate in raster order whose window
 // passes, in parallel; the scan before it changes nothing, and after an
 // acceptance the maps are rebuilt and the scan resumes at the next pixel.
-// The accepted substamp's value is the sequential sum of sss.cl:421-424; for
+// The accepted substamp's value is the sequential sum of sss.cl:354-357; for
 // FP32 input every summand is a float, all partial sums are exact in FP64
 // whenever sum|v| < 2^52 * (quantum of the smallest |v|), which is checked,
 // and then a parallel sum is the same number.  The reference's writes of the
-// bad-pixel bit for pixels above threshHigh (sss.cl:416-419, :484-487,
-// :512-515) are unreachable: such pixels carry BAD_INPUT from maskInput
+// bad-pixel bit for pixels above threshHigh (sss.cl:349-352, :417-420,
+// :445-448) are unreachable: such pixels carry BAD_INPUT from maskInput
 // (ini.cl:29), which every badMask contains, and that test comes first.
 constexpr int FM_THREADS = 256;
 enum : uint8_t { FL_PRED = 1, FL_NONPOS = 2, FL_KFQ = 4, FL_VPOS = 8 };
@@ -1396,7 +1371,7 @@ __global__ void __launch_bounds__(FS_T, 1)
   }
 }
 
-// removeEmptyStamps (src/sssUtil.cpp:106-197, sss.cl:574-638): keep stamps
+// removeEmptyStamps (src/sssUtil.cpp:106-197, sss.cl:543-571): keep stamps
 // with at least one substamp in ascending original order.  One CTA per image.
 __global__ void __launch_bounds__(256)
     k_compact_stamps(const int* __restrict__ cntAll, const int2* __restrict__ xyAll,
@@ -1409,7 +1384,7 @@ __global__ void __launch_bounds__(256)
   for(int base = 0; base < nAll; base += 256) {
     int s = base + threadIdx.x;
     int keep = (s < nAll && cntAll[s] > 0) ? 1 : 0;
-    int pos = blockExclusiveScan(keep, warpTot, &sTotal) + done;
+    int pos = blockScanExcl(keep, warpTot, &sTotal) + done;
     if(keep) {
       orig[pos] = s;
       count[pos] = cntAll[s];
@@ -1426,7 +1401,7 @@ __global__ void __launch_bounds__(256)
   if(threadIdx.x == 0) *nOut = done;
 }
 
-// createStampBounds (sss.cl:86-105) on the device, for frame graphs: the
+// createStampBounds (sss.cl:19-38) on the device, for frame graphs: the
 // same integer expressions as the host table of stageSss.
 __global__ void k_stamp_geom(int4* __restrict__ geom, int nAll, int stampsx, int stampsy, int w,
                              int h, int fSW) {
@@ -1446,7 +1421,7 @@ __global__ void k_reset_skip(uint16_t* mask, long long n) {
 
 }  // namespace
 
-// The ran1 sequence of seed -666 (the seed of every stamp, sss.cl:81-146),
+// The ran1 sequence of seed -666 (the seed of every stamp, sss.cl:81-116),
 // n draws, generated once per context and size.
 static const double* ran1Draws(xb_ctx* c, int n) {
   const std::string key = "ran1_draws";
@@ -1553,7 +1528,7 @@ void stageSss(xb_ctx* c) {
     throw XbError{XB_ERR_UNSUPPORTED, "substamp parameters above this build's limits"};
   const int nAll = c->stampsx * c->stampsy;
   c->nAll = nAll;
-  // createStampBounds (sss.cl:86-105)
+  // createStampBounds (sss.cl:19-38)
   std::vector<int4> geom(nAll);
   for(int id = 0; id < nAll; id++) {
     int sxI = id % c->stampsx, syI = id / c->stampsx;

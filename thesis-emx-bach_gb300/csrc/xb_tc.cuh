@@ -119,6 +119,15 @@ __device__ __forceinline__ void ld8(uint32_t taddr, float* v) {
 #pragma unroll
   for(int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
+// 32 lanes x 4 consecutive columns; the caller waits with ldWait()
+__device__ __forceinline__ void ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+#pragma unroll
+  for(int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void ldWait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // 512 TMEM columns (one warp; the same warp frees them)
@@ -401,6 +410,163 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, long long* sums, const i
     const double g = v * __longlong_as_double((long long)(1023 + ex) << 52);
     G[ra * R + rb] = g;
     G[rb * R + ra] = g;
+  }
+}
+
+// The K-chunk loop of one stamp without shared-memory staging (for kernels
+// that must leave room for a second CTA on the SM): each thread loads its
+// 8-element units (row r < R, 8 consecutive k) of the chunk straight from
+// global memory (the CTA's own W, just written, so L2) into registers, waits
+// until the chunk's operand buffer is free, slices into it, and one thread
+// issues the products.  Rows R..63 of both operand buffers are zeroed once.
+// Same digits, same products as gramChunks.  Returns false, in every thread,
+// when a wait of any thread ran out of time.
+template <int NT>
+__device__ __forceinline__ bool gramChunksDirect(const float* __restrict__ Ws,
+                                                 const float* __restrict__ Wl, int wRows, int ldW,
+                                                 int R, int K, const float* imgRow, const int* expo,
+                                                 unsigned char* buf, unsigned long long* bars,
+                                                 uint32_t tmem, unsigned long long deadline) {
+  static_assert(2 * NT >= RB * (KC / 8), "two units per thread cover a chunk");
+  const int tid = threadIdx.x;
+  const int nChunk = (K + KC - 1) / KC, nUnits = R * (KC / 8);
+  bool ok = true;
+  // rows R..RB-1 stay zero in both buffers
+  for(int u = tid; u < 2 * (RB - R) * (KC / 8); u += NT) {
+    const int bsel = u / ((RB - R) * (KC / 8)), v = u % ((RB - R) * (KC / 8));
+    const uint32_t zero[NS][4] = {};
+    storeSlices(buf + bsel * OPBUF, R + v / (KC / 8), v % (KC / 8), zero);
+  }
+  for(int ch = 0; ch < nChunk; ch++) {
+    const int b = ch & 1;
+    unsigned char* B = buf + b * OPBUF;
+    float xh[2][8], xl[2][8];
+#pragma unroll
+    for(int i = 0; i < 2; i++) {
+      const int u = tid + i * NT;
+      const int r = u / (KC / 8), kg = u % (KC / 8), k0 = ch * KC + kg * 8;
+#pragma unroll
+      for(int e = 0; e < 8; e++) xh[i][e] = xl[i][e] = 0.f;
+      if(u < nUnits) {
+        if(r < wRows) {
+          if(k0 < ldW) {  // ldW is a multiple of 8: a unit is wholly inside or past it
+            const float4* ph = (const float4*)(Ws + (size_t)r * ldW + k0);
+            const float4* pl = (const float4*)(Wl + (size_t)r * ldW + k0);
+            const float4 h0 = ph[0], h1 = ph[1], l0 = pl[0], l1 = pl[1];
+            xh[i][0] = h0.x; xh[i][1] = h0.y; xh[i][2] = h0.z; xh[i][3] = h0.w;
+            xh[i][4] = h1.x; xh[i][5] = h1.y; xh[i][6] = h1.z; xh[i][7] = h1.w;
+            xl[i][0] = l0.x; xl[i][1] = l0.y; xl[i][2] = l0.z; xl[i][3] = l0.w;
+            xl[i][4] = l1.x; xl[i][5] = l1.y; xl[i][6] = l1.z; xl[i][7] = l1.w;
+          }
+        } else {
+#pragma unroll
+          for(int e = 0; e < 8; e++) xh[i][e] = imgRow[k0 + e];  // zero-padded past K
+        }
+#pragma unroll
+        for(int e = 0; e < 8; e++)
+          if(k0 + e >= K) xh[i][e] = xl[i][e] = 0.f;
+      }
+    }
+    if(ch >= 2 && !waitUntil(smemU32(&bars[b]), ((ch - 2) >> 1) & 1, deadline)) ok = false;
+#pragma unroll
+    for(int i = 0; i < 2; i++) {
+      const int u = tid + i * NT;
+      if(u < nUnits) {
+        const int r = u / (KC / 8), kg = u % (KC / 8);
+        uint32_t q[NS][4];
+        slice8(xh[i], xl[i], expo[r], q);
+        storeSlices(B, r, kg, q);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if(tid == 0) issueChunk(tmem, B, ch == 0, smemU32(&bars[b]));
+  }
+  const int last = nChunk - 1;
+  if(!waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, deadline)) {
+    ok = false;
+    waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, timerNs() + WAIT_NS);
+  }
+  const int failed = __syncthreads_or(ok ? 0 : 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return failed == 0;
+}
+
+// The epilogue of gramChunksDirect in two int64 arrays (sums: EPI2_BYTES):
+// the thread holding (t, a) adds, for each column b, its X parts to SA[a][b]
+// / SB[a][b] and its Y parts to SA[b][a] / SB[b][a] with shared-memory
+// atomics, so SA[a][b] = XA[a][b] + YA[b][a] = A_ab of epilogue() above and
+// likewise SB; every entry of G then follows from its own (a, b), and the
+// two triangles agree because A and B are symmetric exact integers.  TMEM
+// columns come four at a time.  Frees the TMEM (warp 0).
+constexpr int EPI2_BYTES = 2 * RB * ELD * 8;
+__device__ __forceinline__ void epilogueAtomic(uint32_t tmem, long long* sums, const int* expo,
+                                               int R, double* G) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nWarps = blockDim.x >> 5;
+  unsigned long long* SA = (unsigned long long*)sums;
+  unsigned long long* SB = SA + RB * ELD;
+  for(int i = tid; i < 2 * RB * ELD; i += blockDim.x) SA[i] = 0ull;
+  __syncthreads();
+  const int q = warp & 3, part = warp >> 2, nParts = nWarps >> 2;
+  const int a = 32 * (q & 1) + lane;
+  const int t1 = q >> 1, t2 = 2 + (q >> 1);
+  const uint32_t lanes = (uint32_t)(32 * q) << 16;
+  for(int b0 = 4 * part; b0 < RB; b0 += 4 * nParts) {
+    long long xa[4] = {0, 0, 0, 0}, xb[4] = {0, 0, 0, 0}, ya[4] = {0, 0, 0, 0},
+              yb[4] = {0, 0, 0, 0};
+    {
+      float p1[5][4];
+#pragma unroll
+      for(int u = 0; u < 4; u++) ld4(tmem + lanes + 64 * u + b0, p1[u]);
+      ld4(tmem + lanes + 256 + b0, p1[4]);
+      ldWait();
+#pragma unroll
+      for(int i = 0; i < 4; i++)
+#pragma unroll
+        for(int u = 0; u < 5; u++) {
+          const int m = t1 + u;
+          const long long p = (long long)__float2int_rn(p1[u][i]);  // |p| < 2^24: exact
+          const long long v = p * (1ll << (m <= 3 ? 7 * (3 - m) : 7 * (7 - m)));
+          if(m <= 3) xa[i] += v; else xb[i] += v;
+          if(u >= 2) {
+            if(m <= 3) ya[i] += v; else yb[i] += v;
+          }
+        }
+    }
+    {
+      float p2[3][4];
+#pragma unroll
+      for(int j = 0; j < 3; j++) ld4(tmem + lanes + 320 + 64 * j + b0, p2[j]);
+      ldWait();
+#pragma unroll
+      for(int i = 0; i < 4; i++)
+#pragma unroll
+        for(int j = 0; j < 3; j++) {
+          const int m = t2 + 2 + j;  // >= 4
+          const long long v = (long long)__float2int_rn(p2[j][i]) * (1ll << (7 * (7 - m)));
+          xb[i] += v;
+          if(j == 2) yb[i] += v;
+        }
+    }
+#pragma unroll
+    for(int i = 0; i < 4; i++) {
+      const int bcol = b0 + i;
+      atomicAdd(&SA[a * ELD + bcol], (unsigned long long)xa[i]);
+      atomicAdd(&SB[a * ELD + bcol], (unsigned long long)xb[i]);
+      atomicAdd(&SA[bcol * ELD + a], (unsigned long long)ya[i]);
+      atomicAdd(&SB[bcol * ELD + a], (unsigned long long)yb[i]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if(warp == 0) tmemFree512(tmem);
+  for(int e = tid; e < R * R; e += blockDim.x) {
+    const int ra = e / R, rb = e % R;
+    const long long A = (long long)SA[ra * ELD + rb];
+    const long long B = (long long)SB[ra * ELD + rb];
+    const double v = (double)A * 0x1p28 + (double)B;
+    const int ex = expo[ra] + expo[rb] - 63;
+    G[e] = v * __longlong_as_double((long long)(1023 + ex) << 52);
   }
 }
 
