@@ -162,6 +162,17 @@ int xb_ctx_set_params(xb_ctx* ctx, const xb_params* p);
  * "gram_fp64" (0/1, mixed mode): compute the per-stamp Gram matrices with
  * FP64 accumulation on the CUDA cores instead of the exact tensor-core
  * slicing (a cross-check; the results agree to rounding).
+ * "fill_gram" (0/1, default 1, mixed mode): run the substamp fill and the
+ * tensor-core Gram of each stamp as one kernel (window by TMA tile copy, W
+ * written once) where the shape allows; 0 runs the separate fill, finish
+ * and Gram kernels.  The results are the same bit for bit.
+ * "fill_gram_tma" (0/1, default 1): let the fused kernel stage its windows
+ * by TMA tile copies (0: plain loads; the same results).
+ * "test_wait_timeout" (0/1, mixed mode, for tests): every CTA of the fused
+ * fill + Gram kernel first waits on a barrier nothing arrives at, with a
+ * 1 ms bound; the wait runs out, the CTA records a device timeout and goes
+ * on with its real waits, so the frame ends with XB_ERR_DEVICE_TIMEOUT from
+ * cd (or from the frame graph's record) while the context stays usable.
  * "graph" (0/1, mixed mode only): xb_run, xb_run_device and batches replay
  * each frame as one captured CUDA graph.  The host decisions of the stages
  * (kept-stamp counts, the sss retry, the cd test lists and direction, the ksc

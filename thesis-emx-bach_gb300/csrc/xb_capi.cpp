@@ -252,6 +252,8 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->fillGram = value != 0;
   } else if(n == "fill_gram_tma") {
     c->fillGramTma = value != 0;
+  } else if(n == "test_wait_timeout") {
+    c->testWaitTimeout = value != 0;
   } else if(n == "ldl_panel") {
     c->ldlPanel = value != 0;
   } else if(n == "ldl_cluster") {

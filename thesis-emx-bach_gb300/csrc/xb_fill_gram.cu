@@ -104,6 +104,7 @@ struct FillGramArgs {
   int nBG;
   int hSS, wRows, ldW;
   int useTma;
+  int testStall;  // option test_wait_timeout: one bounded wait per CTA runs out (gramChunksDirect)
   // pass plan: pass p holds the Y filters gOrder[gBeg[p] .. gBeg[p+1]) in
   // ytmp slots 0.. (slot[g]) and the X rows rows[rBeg[p] .. rBeg[p+1])
   // (basis function 0 apart: its filter g0 = gOrder[0] runs first alone)
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(FG_THREADS, 2)
   __shared__ int expo[RB];
   __shared__ unsigned rowMax[RB];
   __shared__ unsigned char evenRow[MAX_NPSF];
-  __shared__ unsigned long long bars[3];  // two operand buffers, the window copy
+  __shared__ unsigned long long bars[4];  // two operand buffers, the window copy, the test stall
   __shared__ uint32_t tmemBase;
   if(a.liveN && (int)blockIdx.x >= *a.liveN) return;  // before any barrier or TMEM allocation
   const int t = blockIdx.x, s = a.list[t], tid = threadIdx.x, warp = tid >> 5;
@@ -209,6 +210,7 @@ __global__ void __launch_bounds__(FG_THREADS, 2)
     barInit(smemU32(&bars[0]), 1);
     barInit(smemU32(&bars[1]), 1);
     barInit(winBar, 1);
+    barInit(smemU32(&bars[3]), 1);  // nothing arrives here (test option testStall)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     if(tma) {
       const uint32_t bytes = (uint32_t)(ldWin * tw * 4);
@@ -373,7 +375,8 @@ __global__ void __launch_bounds__(FG_THREADS, 2)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemBase;
-  if(!gramChunksDirect<NT>(Ws, Wl, a.wRows, ldW, R, K, imgRow, expo, buf, bars, tmem, deadline))
+  if(!gramChunksDirect<NT>(Ws, Wl, a.wRows, ldW, R, K, imgRow, expo, buf, bars, tmem, deadline,
+                           a.testStall ? &bars[3] : nullptr))
     ok = false;
   epilogueAtomic(tmem, (long long*)buf, expo, R, Gs);
   if(tid == 0 && !ok) atomicOr(a.timeout, 1);
@@ -446,6 +449,7 @@ void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
   a.Wlo = S.Wlo;
   a.G = G;
   a.timeout = deviceStatus(c) + 1;  // the context's device-timeout word
+  a.testStall = c->testWaitTimeout;
   // pass plan: basis function 0's filter first, then the others in order,
   // FG_GP filters per pass; each pass's X rows are its filters' members
   std::vector<int> order, groupOf(g.nPSF, 0);

@@ -269,6 +269,9 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
   put(c->gramFp64);
   put(c->ldlPanel);
   put(c->ldlCluster);
+  put(c->fillGram);
+  put(c->fillGramTma);
+  put(c->testWaitTimeout);
   const uintptr_t im = (uintptr_t)c->inputMask;  // the mask's content is read at replay
   put(im);
   const int rank = c->rankW ? c->rank : 0;  // the weights are read from the device at replay

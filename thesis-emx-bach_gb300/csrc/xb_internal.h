@@ -169,6 +169,7 @@ struct xb_ctx {
   int gramFp64 = 0;  // mixed mode: FP64 CUDA-core Gram instead of the tensor cores (checks)
   int fillGram = 1;     // mixed mode: fused fill + tensor-core Gram where the shape allows
   int fillGramTma = 1;  // the fused kernel stages its windows by TMA tile copies
+  int testWaitTimeout = 0;  // option "test_wait_timeout": one bounded wait per fused-kernel CTA runs out
   int rank = 0;          // learned substamp order after sss: 1 demote, 2 sort
   int rankTau = 500;     // demotion threshold of the accept probability, 1/1000
   int autotune = 1;      // time the variants of tunable kernels on first use

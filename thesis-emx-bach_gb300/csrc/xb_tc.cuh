@@ -421,12 +421,20 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, long long* sums, const i
 // issues the products.  Rows R..63 of both operand buffers are zeroed once.
 // Same digits, same products as gramChunks.  Returns false, in every thread,
 // when a wait of any thread ran out of time.
+//
+// stallBar (test option, else null): an initialised mbarrier on which nothing
+// ever arrives.  Before the first wait for a commit, every thread waits on it
+// with a TEST_STALL_NS bound, which runs out: the CTA records a timeout and
+// then waits for the real commit with its full bound, as after a real
+// timeout, so the error path runs without a fault and with correct results.
+constexpr unsigned long long TEST_STALL_NS = 1000000ull;
 template <int NT>
 __device__ __forceinline__ bool gramChunksDirect(const float* __restrict__ Ws,
                                                  const float* __restrict__ Wl, int wRows, int ldW,
                                                  int R, int K, const float* imgRow, const int* expo,
                                                  unsigned char* buf, unsigned long long* bars,
-                                                 uint32_t tmem, unsigned long long deadline) {
+                                                 uint32_t tmem, unsigned long long deadline,
+                                                 const unsigned long long* stallBar = nullptr) {
   static_assert(2 * NT >= RB * (KC / 8), "two units per thread cover a chunk");
   const int tid = threadIdx.x;
   const int nChunk = (K + KC - 1) / KC, nUnits = R * (KC / 8);
@@ -467,6 +475,7 @@ __device__ __forceinline__ bool gramChunksDirect(const float* __restrict__ Ws,
           if(k0 + e >= K) xh[i][e] = xl[i][e] = 0.f;
       }
     }
+    if(ch == 2 && stallBar && !waitUntil(smemU32(stallBar), 0, timerNs() + TEST_STALL_NS)) ok = false;
     if(ch >= 2 && !waitUntil(smemU32(&bars[b]), ((ch - 2) >> 1) & 1, deadline)) ok = false;
 #pragma unroll
     for(int i = 0; i < 2; i++) {
@@ -483,6 +492,7 @@ __device__ __forceinline__ bool gramChunksDirect(const float* __restrict__ Ws,
     if(tid == 0) issueChunk(tmem, B, ch == 0, smemU32(&bars[b]));
   }
   const int last = nChunk - 1;
+  if(nChunk <= 2 && stallBar && !waitUntil(smemU32(stallBar), 0, timerNs() + TEST_STALL_NS)) ok = false;
   if(!waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, deadline)) {
     ok = false;
     waitUntil(smemU32(&bars[last & 1]), (last >> 1) & 1, timerNs() + WAIT_NS);
