@@ -170,12 +170,18 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_frames_per_s(T, S, info, runs, threads=None):
+def cpu_frames_per_s(T, S, info, runs, threads=None, params_kw=None):
     import build_native
     build_native.build_oracle()
     from xbach_testlib import Oracle
     o = Oracle()
     p = frame_params(o, info)
+    for k, v in (params_kw or {}).items():
+        if k in ("dg", "bg"):
+            for i, x in enumerate(v):
+                getattr(p, k)[i] = x
+        else:
+            setattr(p, k, v)
     T64, S64 = T.astype("float64"), S.astype("float64")
     threads = threads or os.cpu_count() or 1
     times = []
@@ -497,6 +503,205 @@ def run_config4(args):
     return 0
 
 
+def _make_pair3(frame):
+    sys.path.insert(0, str(PKG))
+    from xbach.synth import make_pair
+    return make_pair(3, frame=frame)
+
+
+def run_config3(args):
+    """Config 3: 3072^2 crowded fields with 4 Gaussians (59 basis functions
+    by the reference's counting rule), kernel order 3, background order 2
+    (587 unknowns), 20x20 stamps.  --pairs3 pairs per step on as many worker
+    contexts, frame graphs, no ranking; the plain FP64 pipeline through the
+    same batch API; accuracy of frame 0 against the plain GPU result and the
+    FP64 oracle; rooflines from one frame with the kernel timers on."""
+    import concurrent.futures
+    import multiprocessing
+    B = max(1, args.pairs3)
+    with concurrent.futures.ProcessPoolExecutor(
+            max_workers=min(16, os.cpu_count() or 1),
+            mp_context=multiprocessing.get_context("spawn")) as ex:
+        frames = list(ex.map(_make_pair3, range(B)))
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    import xbach
+    from xbach.synth import PARAMS_3
+    T, S, info = frames[0]
+    h, w = T.shape
+    n_pix = w * h
+
+    def params_for(mode):
+        return xbach.default_params(stampsx=info["stamps"], stampsy=info["stamps"],
+                                    threshHigh=info["threshHigh"], mode=mode, **PARAMS_3)
+    params = params_for(xbach.XB_MODE_MIXED)
+    dT = [torch.from_numpy(f[0]).cuda() for f in frames]
+    dS = [torch.from_numpy(f[1]).cuda() for f in frames]
+    dC = [torch.empty_like(t) for t in dT]
+    dD = [torch.empty_like(t) for t in dT]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.Stream()
+
+    def timed(run, steps):
+        ms = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            run()
+            e1.record(st)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+        return ms
+
+    def batch_for(bparams, graphs):
+        bt = xbach.Batch(bparams, workers=B)
+        bt.set_stream(st.cuda_stream)
+        if graphs:
+            bt.set_option("graph", 1)
+            for i in range(bt.n_workers):
+                bt.worker(i).run_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h,
+                                        dC[0].data_ptr(), dD[0].data_ptr())
+            torch.cuda.synchronize()
+
+        def run():
+            bt.run_ptrs([t.data_ptr() for t in dT], [t.data_ptr() for t in dS], [w] * B, [h] * B,
+                        [t.data_ptr() for t in dC], [t.data_ptr() for t in dD], device=True)
+        return bt, run
+
+    # one frame, stage by stage with the kernel timers: rooflines
+    ctx = xbach.Context(params)
+    cst = torch.cuda.ExternalStream(ctx.stream())
+
+    def single():
+        ctx.init_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h)
+        for stage in (ctx.sss, ctx.cmv, ctx.cd, ctx.ksc, ctx.conv, ctx.sub):
+            stage()
+    for _ in range(2):
+        single()
+    torch.cuda.synchronize()
+    ctx.set_option("time_kernels", 1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(cst)
+    single()
+    e1.record(cst)
+    e1.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    kernels = {}
+    for name in ("stamp_stats", "find_substamps", "fill_w", "fill_finish", "gram", "fill_gram",
+                 "stamp_test_fit", "sigs", "global_ldl", "global_solve", "mx_build",
+                 "mx_scatter", "conv_sub", "ksc_check", "kernel_sum"):
+        ms, n = ctx.kernel_time(name)
+        if n:
+            kernels[name] = {"ms_total": ms, "launches": n}
+    ctx.set_option("time_kernels", 0)
+    stamps = ctx.scalar("nstamps0") + ctx.scalar("nstamps1") + ctx.scalar("ksc_refills")
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
+    fp32_peak, fp64_peak = xbach.measure_fma_peaks(0)
+    peaks = {"hbm": hbm_peak, "bf16": bf16_peak, "fp32": fp32_peak, "fp64": fp64_peak,
+             "hbm_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+             "bf16_source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)",
+             "fma_source": "measured in this run by xb_measure_fma_peaks"}
+    roofs = rooflines(kernels, params, n_pix, "mixed", stamps, peaks)
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_total"]) if kernels else None
+
+    # the batch: mixed with graphs, then the plain pipeline
+    batch, run = batch_for(params, True)
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    wks = [batch.worker(i) for i in range(batch.n_workers)]
+    l0 = sum(wk.launches() for wk in wks)
+    with ClockSampler(0) as clk:
+        ms = timed(run, args.steps)
+    launches = sum(wk.launches() for wk in wks) - l0
+    d0 = dD[0].clone()
+    hT = [torch.from_numpy(f[0]).pin_memory() for f in frames]
+    hS = [torch.from_numpy(f[1]).pin_memory() for f in frames]
+    hC = [torch.empty((h, w), dtype=torch.float32).pin_memory() for _ in range(B)]
+    hD = [torch.empty((h, w), dtype=torch.float32).pin_memory() for _ in range(B)]
+
+    def run_e2e():
+        batch.run_ptrs([t.data_ptr() for t in hT], [t.data_ptr() for t in hS], [w] * B, [h] * B,
+                       [t.data_ptr() for t in hC], [t.data_ptr() for t in hD])
+    run_e2e()
+    e2e_ms = timed(run_e2e, args.steps)
+    batch.close()
+    pbatch, prun = batch_for(params_for(xbach.XB_MODE_PLAIN), False)
+    prun()
+    torch.cuda.synchronize()
+    p_steps = max(1, min(args.steps, 2))
+    p_ms = timed(prun, p_steps)
+    pbatch.close()
+
+    # accuracy of frame 0: mixed (stage run = the batch's frame 0) against
+    # the plain GPU result and the FP64 oracle
+    from xbach import accuracy as acc
+    pctx = xbach.Context(params_for(xbach.XB_MODE_PLAIN))
+    pctx.init_device(dT[0].data_ptr(), dS[0].data_ptr(), w, h)
+    for stage in (pctx.sss, pctx.cmv, pctx.cd, pctx.ksc, pctx.conv, pctx.sub):
+        stage()
+    single()
+    torch.cuda.synchronize()
+    _, threads, times, ores = cpu_frames_per_s(T, S, info, 1, params_kw=PARAMS_3)
+    ref = {"diff": ores.image("diff"), "conv": ores.image("conv"),
+           "solution": ores.array("solution", "float64"), "kernSum": ores.scalar("kernSum"),
+           "convTemplate": ores.scalar("convTemplate")}
+    n_comp, n_bg = acc.layout(params)
+    mixed_r, plain_r = run_result(xbach, ctx), run_result(xbach, pctx)
+    accuracy = {"chosen_vs_plain": acc.compare(mixed_r, plain_r, T, S, n_comp, n_bg),
+                "chosen_vs_fp64_oracle": acc.compare(mixed_r, ref, T, S, n_comp, n_bg),
+                "plain_vs_fp64_oracle": acc.compare(plain_r, ref, T, S, n_comp, n_bg),
+                "kernel_sum": {"chosen": ctx.scalar("kernSum"), "plain": pctx.scalar("kernSum"),
+                               "oracle": ores.scalar("kernSum"), "generator_flux_ratio": 1.1},
+                "batch_frame0_equals_single": bool(torch.equal(
+                    d0.cpu(), torch.from_numpy(ctx.image(xbach.XB_IMG_DIFF, f64=False))))}
+    m = accuracy["chosen_vs_plain"]["diff"]["max_sigma"]
+    accuracy["gate"] = {"uses": "chosen_vs_plain", "max_sigma": m, "bar": SIGMA_BAR,
+                        "pass": bool(m <= SIGMA_BAR)}
+    value = B * args.steps / (ms / 1000.0)
+    plain_v = B * p_steps / (p_ms / 1000.0)
+    roof = dict(roofs[dominant]) if dominant in roofs else None
+    if roof is not None and "bound" not in roof:
+        roof = dict(next(iter(roof.values())))
+    if roof is not None:
+        roof["kernel"] = dominant
+        roof["traffic"] = None
+    line = {
+        "metric": "difference-images/s at 3072² (config 3), chosen vs plain GPU at ≤1e-3σ",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (preset 3: seeded 3072x3072 crowded fields, one seed per pair)",
+        "config": {"workload": "3072x3072 FP32 pairs, 80k sources, 4 Gaussians (degrees 6/4/3/2, "
+                               "59 basis functions), kernel order 3, background order 2 (587 "
+                               "unknowns), 20x20 stamps",
+                   "mode": "mixed", "frames_per_step": B, "workers": B, "frame_graphs": True,
+                   "learned_ranking": None, "l2": "flushed before every step; inputs exceed L2",
+                   "inputs": "device-resident FP32 T,S"},
+        "e2e": {"value": B * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+                "h2d_bytes_per_step": B * 2 * 4 * n_pix, "d2h_bytes_per_step": B * 2 * 4 * n_pix},
+        "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "rooflines": roofs,
+        "single_frame": {"value": 1000.0 / single_ms, "unit": UNIT, "ms_per_step": single_ms,
+                         "path": "stages, host-driven (per-kernel timers on)"},
+        "dominant_kernel": dominant, "kernels": kernels,
+        "plain_gpu_batched": {"value": plain_v, "unit": UNIT, "ms_per_step": p_ms / p_steps,
+                              "steps": p_steps, "frames_per_step": B},
+        "chosen_over_plain": value / plain_v,
+        "cpu_baseline": {"value": 1.0 / times[0], "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "frame pair 0, one full 3072x3072 pair (FP64 oracle, OpenMP "
+                                   f"over {threads} host threads)"},
+        "accuracy": accuracy,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def _make_pair2(frame):
     sys.path.insert(0, str(PKG))
     from xbach.synth import make_pair
@@ -615,8 +820,10 @@ def main():
                     help="CPU baseline: oracle runs (median reported)")
     ap.add_argument("--cpu-single", type=int, default=1,
                     help="CPU baseline: also time one single-threaded oracle run")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 4],
-                    help="2: the headline 2048^2 workload; 4: 64 pairs of mixed size")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4],
+                    help="2: the headline 2048^2 workload; 3: 3072^2 with 59 basis functions, "
+                         "kernel order 3, background order 2; 4: 64 pairs of mixed size")
+    ap.add_argument("--pairs3", type=int, default=8, help="--config 3: pairs per step")
     ap.add_argument("--pairs", type=int, default=64, help="--config 4: pairs per step")
     ap.add_argument("--rank", type=int, default=1,
                     help="mixed mode: learned substamp order (policy 1, shipped weights) on (1) "
@@ -637,6 +844,8 @@ def main():
         return run_reference(args)
     if args.config == 4:
         return run_config4(args)
+    if args.config == 3:
+        return run_config3(args)
     if args.files > 0:
         return run_files(args)
 

@@ -1,8 +1,15 @@
 """The 3072^2 crowded field with the extended basis (4 Gaussians, degrees
-6/4/3/2 -> 59 functions), kernel order 3 and background order 2: a global
-system of 587 unknowns (16-CTA clusters in both modes) and 66 Gram rows (the
-FP64 CUDA-core Gram in mixed mode).  The mixed result is held to the same
-acceptance as the 2048^2 field."""
+6/4/3/2 -> 59 functions by the reference's counting rule), kernel order 3
+and background order 2: a global system of 587 unknowns (16-CTA clusters in
+both modes), 66 Gram rows (beyond the tensor-core kernel's 64: the mixed path
+takes the FP64 CUDA-core Gram) and 390 W dot products per stamp for the
+global matrix.
+
+The plain path is checked against the FP64 oracle bit for bit in
+tests/test_gpu_parity.py (case config3).  Here the mixed path is held to the
+metric's acceptance against the plain result, and both to the generator's
+truth: the template is the image to convolve and the kernel sum is the
+generator's flux ratio 1.1."""
 import numpy as np
 import pytest
 
@@ -34,38 +41,35 @@ def test_geometry(pair3):
     assert len(ctx.solution()) >= 587 + 1
 
 
-def _diff_rms(ctx, T, S):
+def test_mixed_within_1e3_sigma_of_plain(pair3):
     import xbach
-    d = ctx.image(xbach.XB_IMG_DIFF)
-    c = ctx.image(xbach.XB_IMG_CONV)
-    target = S if ctx.scalar("convTemplate") else T
-    ok = d != 1e-30
-    sigma = np.sqrt(np.abs(target) + np.abs(c) + 2 * SIGMA_RN ** 2)
-    return float(np.sqrt(np.mean((d[ok] / sigma[ok]) ** 2))), float(ok.mean())
-
-
-def test_mixed_fit_is_physical(pair3):
-    """This preset makes the reference's normal equations singular (cond
-    ~2e20 of the cd matrices): the plain path, like the reference's
-    unrefined LU, returns a meaningless fit (wrong direction, kernel sum off
-    by 15 %, ~100 ksc iterations).  The mixed path's LDL^T + refinement
-    returns the physical answer: the template is convolved, the kernel sum
-    equals the generator's flux ratio 1.1, the loop converges, and the
-    difference image is noise-like.  The substamp decisions (sss) are shared
-    and identical in both modes."""
-    import xbach
+    from xbach.accuracy import is_bad
     T, S, out = pair3
     plain, mixed = out[xbach.XB_MODE_PLAIN], out[xbach.XB_MODE_MIXED]
     for k in ("ss_xy0", "ss_xy1", "ss_count0", "ss_count1"):
         assert np.array_equal(plain.array(k, np.int32), mixed.array(k, np.int32)), k
-    rms_m, frac_m = _diff_rms(mixed, T, S)
-    rms_p, _ = _diff_rms(plain, T, S)
-    print(f"3072^2: mixed convT {int(mixed.scalar('convTemplate'))} kernSum "
-          f"{mixed.scalar('kernSum'):.5f} ksc {int(mixed.scalar('ksc_iterations'))} diff rms "
-          f"{rms_m:.3f} sigma; plain convT {int(plain.scalar('convTemplate'))} kernSum "
-          f"{plain.scalar('kernSum'):.5f} ksc {int(plain.scalar('ksc_iterations'))} diff rms "
-          f"{rms_p:.3f} sigma")
-    assert mixed.scalar("convTemplate") == 1
-    assert abs(mixed.scalar("kernSum") / 1.1 - 1) < 0.01
-    assert mixed.scalar("ksc_iterations") < 20
-    assert frac_m > 0.5 and rms_m < 3.0
+    assert plain.scalar("convTemplate") == mixed.scalar("convTemplate") == 1
+    assert plain.scalar("ksc_iterations") == mixed.scalar("ksc_iterations")
+    assert abs(mixed.scalar("kernSum") / plain.scalar("kernSum") - 1) < 1e-5
+    dp, dm = plain.image(xbach.XB_IMG_DIFF), mixed.image(xbach.XB_IMG_DIFF)
+    cp = plain.image(xbach.XB_IMG_CONV)
+    ok = ~is_bad(dp) & ~is_bad(dm)
+    assert ok.mean() > 0.5
+    sigma = np.sqrt(np.abs(S) + np.abs(cp) + 2 * SIGMA_RN ** 2)  # S: the target image
+    err = np.abs(dm - dp)[ok] / sigma[ok]
+    print(f"3072^2: mixed vs plain max {err.max():.2e} sigma, rms {np.sqrt(np.mean(err ** 2)):.2e}")
+    assert err.max() <= 1e-3
+
+
+def test_fit_matches_generator(pair3):
+    """Both modes recover the generator's flux ratio (1.1) and leave a
+    noise-like difference image."""
+    import xbach
+    T, S, out = pair3
+    for mode, ctx in out.items():
+        assert abs(ctx.scalar("kernSum") / 1.1 - 1) < 0.01, mode
+        d, c = ctx.image(xbach.XB_IMG_DIFF), ctx.image(xbach.XB_IMG_CONV)
+        ok = d != 1e-30
+        sigma = np.sqrt(np.abs(S) + np.abs(c) + 2 * SIGMA_RN ** 2)
+        rms = float(np.sqrt(np.mean((d[ok] / sigma[ok]) ** 2)))
+        assert ok.mean() > 0.5 and rms < 3.0, (mode, rms)

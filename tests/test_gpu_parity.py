@@ -22,8 +22,10 @@ def bit_equal(a, b):
 
 # test01_f64 (FP64 frames) and config1_s3 (149-px stamps) take the substamp
 # search through the global-memory map kernel; the others through the
-# shared-memory one.
-CASES = ["test01", "config1", "config2", "test01_f64", "config1_s3"]
+# shared-memory one.  config3 is the 3072^2 field with 4 Gaussians (59 basis
+# functions), kernel order 3 and background order 2: 587 unknowns, 390 dot
+# products per stamp for the global matrix, 16-CTA LU clusters.
+CASES = ["test01", "config1", "config2", "test01_f64", "config1_s3", "config3"]
 
 
 def case_inputs(name, test01):
@@ -37,8 +39,11 @@ def case_inputs(name, test01):
         return T, S, dict(stampsx=3, stampsy=3, threshHigh=info["threshHigh"])
     cfg = int(name[-1])
     T, S, info = make_pair(cfg)
-    return T, S, dict(stampsx=info["stamps"], stampsy=info["stamps"],
-                      threshHigh=info["threshHigh"])
+    kw = dict(stampsx=info["stamps"], stampsy=info["stamps"], threshHigh=info["threshHigh"])
+    if cfg == 3:
+        from xbach.synth import PARAMS_3
+        kw.update(PARAMS_3)
+    return T, S, kw
 
 
 @pytest.fixture(scope="module", params=CASES)

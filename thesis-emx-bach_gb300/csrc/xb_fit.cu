@@ -226,7 +226,7 @@ __global__ void k_weights(const int* __restrict__ list, int nList, const int* __
 //   dots[t][.. + nBG + ib]           W[bg ib] . float(O), column-major
 //                                    (cdkscUtil.cpp:459-469)
 // Every dot runs in ascending pixel order (or the stated order) per thread.
-constexpr int DOT_THREADS = 256, DOT_KT = 32;
+constexpr int DOT_THREADS = 256, DOT_KT = 32, DOT_PAIRS = 4;
 template <class T>
 __global__ void __launch_bounds__(DOT_THREADS)
     k_stamp_dots(const int* __restrict__ list, const int* __restrict__ count,
@@ -245,28 +245,35 @@ __global__ void __launch_bounds__(DOT_THREADS)
   double* om = sub + wCols;                   // wCols pixel weights (weighted fit)
   if(omega)
     for(int i = tid; i < wCols; i += DOT_THREADS) om[i] = omega[(size_t)s * wCols + i];
-  // products: (rowA, rowB) pairs for this thread
+  // products: the (rowA, rowB) pairs tid, tid + DOT_THREADS, ... (up to
+  // DOT_PAIRS per thread; the host checks the bound), each summed over the
+  // pixels in ascending order
   const int nKB = nC1 * nBG, nPairs = nKB + nBG + nBG * nBG;
-  int ra = -1, rb = -1, oi = -1;
-  if(tid < nPairs) {
-    if(tid < nKB) {
-      ra = 1 + tid / nBG;
-      rb = nPSF + tid % nBG;
-      oi = tid;
-    } else if(tid < nKB + nBG) {
-      ra = 0;
-      rb = nPSF + (tid - nKB);
-      oi = tid;
+  int ra[DOT_PAIRS], rb[DOT_PAIRS], oi[DOT_PAIRS];
+  double acc[DOT_PAIRS];
+#pragma unroll
+  for(int q = 0; q < DOT_PAIRS; q++) {
+    const int pi = tid + q * DOT_THREADS;
+    ra[q] = rb[q] = oi[q] = -1;
+    acc[q] = 0.0;
+    if(pi >= nPairs) continue;
+    if(pi < nKB) {
+      ra[q] = 1 + pi / nBG;
+      rb[q] = nPSF + pi % nBG;
+      oi[q] = pi;
+    } else if(pi < nKB + nBG) {
+      ra[q] = 0;
+      rb[q] = nPSF + (pi - nKB);
+      oi[q] = pi;
     } else {
-      int e = tid - nKB - nBG, ib = e / nBG, jb = e % nBG;
+      int e = pi - nKB - nBG, ib = e / nBG, jb = e % nBG;
       if(jb <= ib) {
-        ra = nPSF + ib;
-        rb = nPSF + jb;
-        oi = nKB + nBG + ib * nBG + jb;
+        ra[q] = nPSF + ib;
+        rb[q] = nPSF + jb;
+        oi[q] = nKB + nBG + ib * nBG + jb;
       }
     }
   }
-  double acc = 0.0;
   for(int k0 = 0; k0 < wCols; k0 += DOT_KT) {
     const int kt = min(DOT_KT, wCols - k0);
     for(int i = tid; i < wRows * DOT_KT; i += DOT_THREADS) {
@@ -274,18 +281,24 @@ __global__ void __launch_bounds__(DOT_THREADS)
       tile[r * (DOT_KT + 1) + kk] = kk < kt ? Ws[(size_t)r * wCols + k0 + kk] : 0.0;
     }
     __syncthreads();
-    if(ra >= 0) {
-      const double* pa = tile + ra * (DOT_KT + 1);
-      const double* pb = tile + rb * (DOT_KT + 1);
+#pragma unroll
+    for(int q = 0; q < DOT_PAIRS; q++) {
+      if(ra[q] < 0) continue;
+      const double* pa = tile + ra[q] * (DOT_KT + 1);
+      const double* pb = tile + rb[q] * (DOT_KT + 1);
+      double a = acc[q];
       if(omega) {
-        for(int kk = 0; kk < kt; kk++) acc += pa[kk] * (pb[kk] * om[k0 + kk]);
+        for(int kk = 0; kk < kt; kk++) a += pa[kk] * (pb[kk] * om[k0 + kk]);
       } else {
-        for(int kk = 0; kk < kt; kk++) acc += pa[kk] * pb[kk];
+        for(int kk = 0; kk < kt; kk++) a += pa[kk] * pb[kk];
       }
+      acc[q] = a;
     }
     __syncthreads();
   }
-  if(ra >= 0) out[oi] = acc;
+#pragma unroll
+  for(int q = 0; q < DOT_PAIRS; q++)
+    if(ra[q] >= 0) out[oi[q]] = acc[q];
   // background projections on the other image
   const int base = nKB + nBG + nBG * nBG;
   if(live) {
@@ -961,6 +974,8 @@ static void solveGlobal(xb_ctx* c, int si, const FitBuffers& f, const int* list,
   }
   const double* dots = mixed ? S.dots : f.dots;  // mixed: filled per stamp by the Gram kernel
   if(nList > 0 && !mixed) {
+    if(g.nComp1 * g.nBG + g.nBG + g.nBG * g.nBG > DOT_PAIRS * DOT_THREADS)
+      throw XbError{XB_ERR_UNSUPPORTED, "too many basis and background terms for the dot kernel"};
     const size_t smem = ((size_t)g.wRows * (DOT_KT + 1) + 2 * (size_t)g.wCols) * sizeof(double);
     const double* omega = c->p.fitWeighted ? S.omega : nullptr;
     { KT_SCOPE(c, "stamp_dots");
