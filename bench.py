@@ -427,7 +427,7 @@ def run_config4(args):
         from xbach import ranker
         w_rank = ranker.preset5_weights()
         for i in range(batch.n_workers):
-            ranker.enable(batch.worker(i), w_rank, policy=1, tau=0.5)
+            ranker.enable(batch.worker(i), w_rank, policy=1, tau=args.rank_tau)
     if use_graph:
         batch.set_option("graph", 1)
     st = torch.cuda.Stream()
@@ -466,7 +466,7 @@ def run_config4(args):
     for i in check:
         ctx = xbach.Context(params[i])
         if use_rank:
-            ranker.enable(ctx, w_rank, policy=1, tau=0.5)
+            ranker.enable(ctx, w_rank, policy=1, tau=args.rank_tau)
         ctx.init_device(dT[i].data_ptr(), dS[i].data_ptr(), ws[i], hs[i])
         for stage in (ctx.sss, ctx.cmv, ctx.cd, ctx.ksc, ctx.conv, ctx.sub):
             stage()
@@ -489,7 +489,7 @@ def run_config4(args):
                    "mode": args.mode, "frames_per_step": n_pairs, "workers": args.workers,
                    "frame_graphs": use_graph, "schedule": "fixed, largest first" if use_graph
                    else "shared queue",
-                   "learned_ranking": "policy 1, tau 0.5, xbach/ranker_preset5.npy" if use_rank
+                   "learned_ranking": f"policy 1, tau {args.rank_tau}, xbach/ranker_preset5.npy" if use_rank
                    else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "l2": "flushed before every step; inputs exceed L2",
@@ -752,7 +752,7 @@ def run_files(args):
             from xbach import ranker
             w_rank = ranker.preset5_weights()
             for i in range(pl.n_workers):
-                ranker.enable(pl.worker(i), w_rank, policy=1, tau=0.5)
+                ranker.enable(pl.worker(i), w_rank, policy=1, tau=args.rank_tau)
         if use_graph:
             pl.set_option("graph", 1)
         for _ in range(max(args.warmup, 1)):
@@ -772,7 +772,7 @@ def run_files(args):
         for i in range(min(B, n)):
             ctx = xbach.Context(params)
             if use_rank:
-                ranker.enable(ctx, w_rank, policy=1, tau=0.5)
+                ranker.enable(ctx, w_rank, policy=1, tau=args.rank_tau)
             ctx.run(frames[i][0], frames[i][1])
             same.append(bool(np.array_equal(read_fits(diffs[i]),
                                             ctx.image(xbach.XB_IMG_DIFF, f64=False).astype(np.float64))))
@@ -793,7 +793,7 @@ def run_files(args):
         "config": {"workload": WORKLOAD, "mode": args.mode, "pairs_per_step": n,
                    "distinct_pairs": B, "workers": args.workers, "io_threads": args.io,
                    "frame_graphs": use_graph,
-                   "learned_ranking": "policy 1, tau 0.5" if use_rank else None,
+                   "learned_ranking": f"policy 1, tau {args.rank_tau}" if use_rank else None,
                    "files": "RAM-backed directory (page cache)",
                    "timing": "host wall clock around xb_pipeline_run_files"},
         "thread_ms_per_step": per,
@@ -828,6 +828,9 @@ def main():
     ap.add_argument("--rank", type=int, default=1,
                     help="mixed mode: learned substamp order (policy 1, shipped weights) on (1) "
                          "or off (0)")
+    ap.add_argument("--rank-tau", type=float, default=0.3,
+                    help="learned ranking: accept-probability threshold of policy 1 (0.3 was "
+                         "chosen on validation frames 100-111 of the workload, not the timed ones)")
     ap.add_argument("--graph", type=int, default=1,
                     help="mixed mode: replay every frame as one captured CUDA graph (1) or run "
                          "the stages host-driven (0)")
@@ -869,7 +872,7 @@ def main():
 
     def with_rank(cx):
         if use_rank:
-            ranker.enable(cx, rank_w, policy=1, tau=0.5)
+            ranker.enable(cx, rank_w, policy=1, tau=args.rank_tau)
         return cx
 
     B = max(1, args.batch)
@@ -968,7 +971,7 @@ def main():
         bt.set_stream(jst.cuda_stream)
         if ranked:
             for i in range(bt.n_workers):
-                ranker.enable(bt.worker(i), rank_w, policy=1, tau=0.5)
+                ranker.enable(bt.worker(i), rank_w, policy=1, tau=args.rank_tau)
         if bparams.mode == xbach.XB_MODE_MIXED:
             bt.set_option("ldl_cluster", args.ldl_cluster)
         if graphs:
@@ -1063,8 +1066,8 @@ def main():
                    "l2": "flushed before every step (256 MB write); each step's inputs exceed L2",
                    "inputs": "device-resident FP32 T,S",
                    "frame_graphs": use_graph,
-                   "learned_ranking": "policy 1, tau 0.5, xbach/ranker_preset5.npy" if use_rank
-                   else None,
+                   "learned_ranking": f"policy 1, tau {args.rank_tau}, xbach/ranker_preset5.npy "
+                                      "(BF16 weights)" if use_rank else None,
                    "hw_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "ldl_cluster": args.ldl_cluster if args.mode == "mixed" else None},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,

@@ -154,6 +154,9 @@ int xb_ctx_set_params(xb_ctx* ctx, const xb_params* p);
  * probability is below "rank_tau" (thousandths, default 500) behind the
  * others, keeping the reference's order within each group; 2 sorts all by
  * score.
+ * "rank_candidates" (0..16, default 0 = every candidate): score and reorder
+ * only the first n candidates of each stamp (the reference's brightest
+ * first); the others keep their places after them.
  * "ldl_panel" (0/1, default 1, mixed mode): let the tuner choose among the
  * column LDL^T kernel and its panel variants (identical factors); 0 keeps
  * the column kernel.
@@ -390,10 +393,14 @@ int xb_pipeline_stats_get(const xb_pipeline* pl, xb_pipeline_stats* out);
 /* ---- learned substamp ranking -------------------------------------------- */
 /* No counterpart in the reference.  A small network (a 3-layer CNN over the
  * 2x31x31 template/science window pair plus an MLP over 16 window
- * statistics, 2161 FP32 parameters) scores every candidate substamp; with
+ * statistics, 2161 parameters) scores every candidate substamp; with
  * option "rank" on and weights loaded, xb_sss reorders each stamp's
  * candidates by descending score, so the ones the ksc fit would reject are
- * tried last.  The ksc sigma-clip check still judges every pick. */
+ * tried last.  The ksc sigma-clip check still judges every pick.  The
+ * network computes with BF16 weights and FP32 activations and sums: the
+ * training calls below take FP32 master weights (which Adam updates) and
+ * round each to BF16 (nearest, ties to even) as they load it; xb_ranker_set
+ * stores the context's copy as BF16. */
 int xb_ranker_param_count(void);
 /* Loads the network's parameters (host array of xb_ranker_param_count()). */
 int xb_ranker_set(xb_ctx* ctx, const float* weights, int n);

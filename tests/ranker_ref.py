@@ -12,6 +12,14 @@ SHAPES = [("c1w", (8, 2, 5, 5)), ("c1b", (8,)), ("c2w", (8, 8, 3, 3)), ("c2b", (
           ("hw", (40,)), ("hb", (1,))]
 
 
+def bf16(w):
+    """The weights as the network uses them: each FP32 value rounded to BF16
+    (nearest, ties to even), returned as float64."""
+    u = np.ascontiguousarray(w, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
 def unpack(w):
     out, o = {}, 0
     for name, shp in SHAPES:

@@ -1,5 +1,7 @@
 """The learned substamp ranker: its CUDA forward, backward and Adam kernels
-against the NumPy FP64 restatement (tests/ranker_ref.py), training on the
+against the NumPy FP64 restatement (tests/ranker_ref.py) of the same network
+with the weights rounded to BF16 (the kernels compute with BF16 weights and
+FP32 activations and sums), training on the
 GPU from plain-loop labels, generalisation to held-out fields, and the
 measured effect on the ksc refit loop."""
 import ctypes
@@ -24,7 +26,7 @@ def test_forward_matches_numpy():
     w = ranker.init_weights(1)
     st, px = _rand_inputs(6, 2)
     z = ranker.logits(w, st, px)
-    zr = np.array([R.forward(w.astype(np.float64), st[i], px[i])[0] for i in range(6)])
+    zr = np.array([R.forward(R.bf16(w), st[i], px[i])[0] for i in range(6)])
     assert np.max(np.abs(z - zr)) <= 1e-4 * (1 + np.max(np.abs(zr)))
 
 
@@ -48,7 +50,7 @@ def test_gradient_matches_numpy():
                           torch.cuda.current_stream().cuda_stream)
     assert rc == 0
     torch.cuda.synchronize()
-    ref = [R.grad(w.astype(np.float64), st[i], px[i], float(y[i]), float(sw[i])) for i in range(4)]
+    ref = [R.grad(R.bf16(w), st[i], px[i], float(y[i]), float(sw[i])) for i in range(4)]
     gref = np.mean([r[1] for r in ref], axis=0)
     lref = np.array([r[0] for r in ref])
     gg = g.cpu().numpy()
@@ -57,6 +59,22 @@ def test_gradient_matches_numpy():
     # per-sample gradients too
     for i in range(4):
         assert np.max(np.abs(gper[i].cpu().numpy() - ref[i][1])) <= 1e-4 * np.max(np.abs(ref[i][1])) + 1e-6
+
+
+def test_weights_are_bf16():
+    """The network uses BF16 weights: FP32 weights and their BF16 roundings
+    give the same logits bit for bit, and weights that differ only below
+    BF16 precision give the same logits too."""
+    from xbach import ranker
+    w = ranker.init_weights(7)
+    st, px = _rand_inputs(5, 8)
+    z = ranker.logits(w, st, px)
+    zb = ranker.logits(R.bf16(w).astype(np.float32), st, px)
+    assert np.array_equal(z.view(np.uint32), zb.view(np.uint32))
+    tiny = (w.view(np.uint32) & np.uint32(0xFFFF0000)) | np.uint32(0x1234)  # same BF16 value
+    zt = ranker.logits(tiny.view(np.float32), st, px)
+    lo = (w.view(np.uint32) & np.uint32(0xFFFF0000)).view(np.float32)
+    assert np.array_equal(ranker.logits(lo, st, px).view(np.uint32), zt.view(np.uint32))
 
 
 def test_adam_step_matches_numpy():
@@ -143,11 +161,13 @@ def _ranker_params(info, mode=None):
                                 mode=xbach.XB_MODE_MIXED if mode is None else mode)
 
 
-@pytest.mark.parametrize("policy", [1, 2])
-def test_device_ranking_follows_the_policy(policy):
+@pytest.mark.parametrize("policy,cands", [(1, 0), (2, 0), (1, 5), (2, 2)])
+def test_device_ranking_follows_the_policy(policy, cands):
     """The on-device reorder (features of every slot, scores, per-stamp
     partition or sort) equals the policy applied in NumPy to the scores of the
-    reference-ordered candidates."""
+    reference-ordered candidates; with option rank_candidates = n only the
+    first n candidates of a stamp are reordered (config 5 ranks 5 per stamp)
+    and the others keep their places after them."""
     import xbach
     from xbach import ranker
     from xbach.synth import make_pair
@@ -159,9 +179,11 @@ def test_device_ranking_follows_the_policy(policy):
     ref.sss()
     ctx = xbach.Context(_ranker_params(info), trace=True)
     ranker.enable(ctx, w, policy=policy, tau=tau)
+    ctx.set_option("rank_candidates", cands)
     ctx.init(T, S)
     ctx.sss()
     zt = np.log(np.float32(tau) / (np.float32(1) - np.float32(tau)))
+    reordered_tail = 0
     for si in (0, 1):
         st, px, stamp, slot = ranker.features(ref, si)
         z = ranker.logits(w, st, px)
@@ -171,12 +193,19 @@ def test_device_ranking_follows_the_policy(policy):
         for s in range(len(orig)):
             sel = stamp == s
             k, zz = slot[sel], z[sel]
+            rest = k[k >= cands] if cands else k[:0]
+            if cands:
+                zz, k = zz[k < cands], k[k < cands]
+                reordered_tail += len(rest)
             if policy == 2:
                 order = k[np.argsort(-zz, kind="stable")]
             else:
                 order = np.concatenate([k[zz >= zt], k[~(zz >= zt)]])
+            order = np.concatenate([order, rest])
             want = allxy[orig[s]][order]
             assert np.array_equal(got[s].reshape(6, 2)[:len(order)], want), (si, s)
+    if cands == 2:
+        assert reordered_tail > 0  # some stamps hold more candidates than are ranked
 
 
 def test_ranker_cuts_refits_on_defect_fields():

@@ -272,6 +272,9 @@ int xb_set_option(xb_ctx* c, const char* name, long long value) {
     c->autotune = value != 0;
   } else if(n == "tune_variant") {
     c->tuneForce = value < 0 ? -1 : (int)value;
+  } else if(n == "rank_candidates") {
+    if(value < 0 || value > MAX_MAXSS) return XB_ERR_ARG;
+    c->rankCandidates = (int)value;
   } else if(n == "rank_tau") {
     if(value <= 0 || value >= 1000) return XB_ERR_ARG;
     c->rankTau = (int)value;

@@ -277,6 +277,7 @@ std::string shapeKey(const xb_ctx* c, int w, int h) {
   const int rank = c->rankW ? c->rank : 0;  // the weights are read from the device at replay
   put(rank);
   put(c->rankTau);
+  put(c->rankCandidates);
   return k;
 }
 

@@ -174,7 +174,8 @@ struct xb_ctx {
   int rankTau = 500;     // demotion threshold of the accept probability, 1/1000
   int autotune = 1;      // time the variants of tunable kernels on first use
   int tuneForce = -1;    // >= 0: launch this variant of every tunable kernel
-  float* rankW = nullptr;  // ranker parameters on the device (xb_ranker_set)
+  uint16_t* rankW = nullptr;  // ranker parameters on the device as BF16 bits (xb_ranker_set)
+  int rankCandidates = 0;     // option "rank_candidates": candidates per stamp ranked (0: all)
   int mxTables = 0;        // the mixed build's monomial tables are on the device
   int ldlPanel = 1;        // option "ldl_panel": panel LDL^T kernel (0: the column kernel)
   int ldlCluster = 16;     // option "ldl_cluster": CTAs of the LDL^T cluster (16, or 8)

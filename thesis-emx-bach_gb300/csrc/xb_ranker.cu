@@ -10,7 +10,11 @@
 // ones the fit would reject are tried last.  The ksc sigma-clip check still
 // runs on every pick; the network only changes the order.
 //
-// Network (2161 FP32 parameters, row-major in the order below):
+// Network (2161 parameters, row-major in the order below), computed with
+// BF16 weights and FP32 activations and accumulation: the training kernels
+// take FP32 master weights (Adam updates those) and round each to BF16 as it
+// is loaded, the inference copy in a context is stored as BF16, so both
+// evaluate the same BF16-weight network:
 //   conv1 2->8, 5x5, stride 2   (31 -> 14), ReLU
 //   conv2 8->8, 3x3, stride 2   (14 -> 6),  ReLU
 //   conv3 8->8, 3x3, stride 1   (6 -> 4),   ReLU, mean over the 4x4 map -> 8
@@ -24,6 +28,10 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
 
 #include "xb_internal.h"
 
@@ -41,6 +49,13 @@ constexpr int O_C1W = 0, O_C1B = O_C1W + RK_C * 2 * 25, O_C2W = O_C1B + RK_C,
               O_M1B = O_M1W + RK_H * RK_NS, O_HW = O_M1B + RK_H, O_HB = O_HW + RK_C + RK_H,
               RK_NP = O_HB + 1;
 static_assert(RK_NP == 2161, "parameter layout");
+
+// A weight as the network uses it: the FP32 master rounded to BF16 (nearest,
+// ties to even), or a stored BF16 weight, as a float.
+__device__ __forceinline__ float rkWeight(const float* W, int q) {
+  return __bfloat162float(__float2bfloat16_rn(W[q]));
+}
+__device__ __forceinline__ float rkWeight(const __nv_bfloat16* W, int q) { return __bfloat162float(W[q]); }
 
 // Activations of one sample (shared memory).
 struct RkAct {
@@ -232,12 +247,13 @@ __device__ __forceinline__ void rkLoad(const float* __restrict__ stats, const fl
   for(int q = threadIdx.x; q < RK_NS; q += RK_T) A.st[q] = stats[(size_t)i * RK_NS + q];
 }
 
+template <class WT>
 __global__ void __launch_bounds__(RK_T)
-    k_rank_forward(const float* __restrict__ W, const float* __restrict__ stats,
+    k_rank_forward(const WT* __restrict__ W, const float* __restrict__ stats,
                    const float* __restrict__ pix, int n, float* __restrict__ logit) {
   __shared__ float Ws[RK_NP];
   __shared__ RkAct A;
-  for(int q = threadIdx.x; q < RK_NP; q += RK_T) Ws[q] = W[q];
+  for(int q = threadIdx.x; q < RK_NP; q += RK_T) Ws[q] = rkWeight(W, q);
   for(int i = blockIdx.x; i < n; i += gridDim.x) {
     __syncthreads();
     rkLoad(stats, pix, i, A);
@@ -255,7 +271,7 @@ __global__ void __launch_bounds__(RK_T)
   __shared__ float Ws[RK_NP];
   __shared__ RkAct A;
   __shared__ RkGrad D;
-  for(int q = threadIdx.x; q < RK_NP; q += RK_T) Ws[q] = W[q];
+  for(int q = threadIdx.x; q < RK_NP; q += RK_T) Ws[q] = rkWeight(W, q);
   for(int i = blockIdx.x; i < n; i += gridDim.x) {
     __syncthreads();
     rkLoad(stats, pix, i, A);
@@ -442,9 +458,12 @@ __global__ void __launch_bounds__(RK_T)
 // their scores z, policy 1 moving those below zTau behind the others (each
 // group in the reference's order), policy 2 sorting all by descending score
 // (ties in the reference's order).
+// Reorders the first nRank candidates of every stamp by score (the others
+// keep their places after them).
 __global__ void k_rank_order(int2* __restrict__ ssxy, double* __restrict__ ssval,
                              const float* __restrict__ z, int nBound,
-                             const int* __restrict__ liveN, int maxSS, int policy, float zTau) {
+                             const int* __restrict__ liveN, int maxSS, int nRank, int policy,
+                             float zTau) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = liveN ? min(*liveN, nBound) : nBound;
   if(s >= n) return;
@@ -456,7 +475,7 @@ __global__ void k_rank_order(int2* __restrict__ ssxy, double* __restrict__ ssval
   for(int k = 0; k < maxSS; k++) {
     xy[k] = ssxy[(size_t)s * maxSS + k];
     v[k] = ssval[(size_t)s * maxSS + k];
-    if(xy[k].x != INT_MAX) {
+    if(xy[k].x != INT_MAX && k < nRank) {
       sc[cnt] = z[(size_t)s * maxSS + k];
       order[cnt++] = k;
     }
@@ -556,12 +575,14 @@ void rankSubstamps(xb_ctx* c) {
     XB_LAUNCHED(c);
     {
       KT_SCOPE(c, "rank_score");
-      k_rank_forward<<<std::min(n, c->smCount * 8), RK_T, 0, c->stream>>>(c->rankW, dStats, dPix,
+      k_rank_forward<__nv_bfloat16><<<std::min(n, c->smCount * 8), RK_T, 0, c->stream>>>(
+          (const __nv_bfloat16*)c->rankW, dStats, dPix,
                                                                           n, dLogit);
       XB_LAUNCHED(c);
     }
+    const int nRank = c->rankCandidates > 0 ? std::min(c->rankCandidates, g.maxSS) : g.maxSS;
     k_rank_order<<<(S.n + 127) / 128, 128, 0, c->stream>>>(S.ssxy, S.ssval, dLogit, S.n, S.dN,
-                                                           g.maxSS, c->rank, zTau);
+                                                           g.maxSS, nRank, c->rank, zTau);
     XB_LAUNCHED(c);
   }
 }
@@ -596,8 +617,16 @@ int xb_ranker_set(xb_ctx* c, const float* weights, int n) {
   return rkGuard(c, [&] {
     if(n != kRankParams || !weights) throw XbError{XB_ERR_ARG, "ranker weights: wrong count"};
     XB_CUDA(cudaSetDevice(c->device));
-    c->rankW = buf<float>(c, "rank_weights", kRankParams);
-    XB_CUDA(cudaMemcpyAsync(c->rankW, weights, sizeof(float) * kRankParams,
+    // stored as BF16 (nearest, ties to even), the weights the network computes with
+    std::vector<uint16_t> wb(kRankParams);
+    for(int q = 0; q < kRankParams; q++) {
+      uint32_t u;
+      memcpy(&u, &weights[q], 4);
+      if((u & 0x7F800000u) == 0x7F800000u && (u & 0x7FFFFFu)) wb[q] = (uint16_t)((u >> 16) | 0x40u);
+      else wb[q] = (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+    }
+    c->rankW = buf<uint16_t>(c, "rank_weights", kRankParams);
+    XB_CUDA(cudaMemcpyAsync(c->rankW, wb.data(), sizeof(uint16_t) * kRankParams,
                             cudaMemcpyHostToDevice, c->stream));
     XB_CUDA(cudaStreamSynchronize(c->stream));
   });
@@ -635,7 +664,8 @@ int xb_ranker_forward(const float* dW, const float* dStats, const float* dPix, i
                       float* dLogit, void* stream) {
   if(n < 0 || (n > 0 && (!dW || !dStats || !dPix || !dLogit))) return XB_ERR_ARG;
   if(n == 0) return XB_OK;
-  k_rank_forward<<<std::min(n, 4096), RK_T, 0, (cudaStream_t)stream>>>(dW, dStats, dPix, n, dLogit);
+  k_rank_forward<float><<<std::min(n, 4096), RK_T, 0, (cudaStream_t)stream>>>(dW, dStats, dPix, n,
+                                                                              dLogit);
   return rkLaunched() == cudaSuccess ? XB_OK : XB_ERR_CUDA;
 }
 
