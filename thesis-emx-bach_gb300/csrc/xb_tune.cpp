@@ -5,8 +5,10 @@
 // name + device + a shape number) and a launcher for each of its variants.
 // Variants of one kernel produce identical results and differ only in tile
 // shape, so the choice is free.  The first call for a key times every
-// variant on the context's stream (one warm-up launch, then three timed
-// launches, CUDA events) and keeps the fastest in a process-wide table;
+// variant on the context's stream (one warm-up launch of each, then five
+// rounds timing two launches of each variant in turn with CUDA events; a
+// variant's time is its best round) and keeps the fastest in a process-wide
+// table;
 // other threads that reach the same key meanwhile use the default variant.
 // With XB_TUNE_CACHE set, the table is read from and appended to that file
 // ("key variant" lines), so later processes skip the timing.  Option
@@ -19,6 +21,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "xb_internal.h"
 
@@ -78,24 +81,30 @@ int tunedVariant(xb_ctx* c, const char* kernel, long long shape, int nVariants,
     }
     gTable[key] = -1;  // this thread times it
   }
+  // Every variant once (lazy loading, first-touch costs), then rounds that
+  // time each variant in turn (two launches) and keep its best round, so a
+  // clock still ramping up or a neighbour's burst of work does not decide
+  // for one variant alone.
   cudaEvent_t e0, e1;
   XB_CUDA(cudaEventCreate(&e0));
   XB_CUDA(cudaEventCreate(&e1));
-  int best = 0;
-  float bestMs = 0.f;
-  for(int v = 0; v < nVariants; v++) {
-    launch(v);  // warm-up
-    XB_CUDA(cudaEventRecord(e0, c->stream));
-    for(int r = 0; r < 3; r++) launch(v);
-    XB_CUDA(cudaEventRecord(e1, c->stream));
-    XB_CUDA(cudaEventSynchronize(e1));
-    float ms = 0.f;
-    XB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    c->scalars["tune:" + std::string(kernel) + ":v" + std::to_string(v) + ":ms"] = ms / 3.0;
-    if(v == 0 || ms < bestMs) {
-      best = v;
-      bestMs = ms;
+  for(int v = 0; v < nVariants; v++) launch(v);
+  std::vector<float> bestOf(nVariants, 0.f);
+  constexpr int kRounds = 5, kPerRound = 2;
+  for(int round = 0; round < kRounds; round++)
+    for(int v = 0; v < nVariants; v++) {
+      XB_CUDA(cudaEventRecord(e0, c->stream));
+      for(int r = 0; r < kPerRound; r++) launch(v);
+      XB_CUDA(cudaEventRecord(e1, c->stream));
+      XB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      XB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if(round == 0 || ms < bestOf[v]) bestOf[v] = ms;
     }
+  int best = 0;
+  for(int v = 0; v < nVariants; v++) {
+    c->scalars["tune:" + std::string(kernel) + ":v" + std::to_string(v) + ":ms"] = bestOf[v] / kPerRound;
+    if(bestOf[v] < bestOf[best]) best = v;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
