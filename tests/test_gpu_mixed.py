@@ -53,6 +53,23 @@ SIGMA_BAR = {"test01": 1e-3, "config1": 1e-3, "config2": 1e-3}
 KSUM_BAR = {"test01": 1e-5, "config1": 1e-5, "config2": 1e-5}
 
 
+def test_cd_kernel_sums_and_test_sets(both):
+    """The mixed path solves each stamp's test system by a warp-per-stamp
+    LDL^T (the kernel sum is the only output cd uses); its kernel sums agree
+    with the plain LU's and the cd test lists are the same."""
+    _, _, _, plain, mixed = both
+    for si in (0, 1):
+        a = mixed.array("kernel_sums%d" % si, np.float64)
+        b = plain.array("kernel_sums%d" % si, np.float64)
+        assert a.shape == b.shape and a.size > 0
+        assert np.max(np.abs(a / b - 1)) < 1e-6, (si, np.max(np.abs(a / b - 1)))
+        try:
+            tp = plain.array("cd_test%d" % si, np.int32)
+        except KeyError:
+            continue
+        assert np.array_equal(mixed.array("cd_test%d" % si, np.int32), tp), si
+
+
 def test_kernel_sum_close(both):
     name, _, _, plain, mixed = both
     assert abs(mixed.scalar("kernSum") / plain.scalar("kernSum") - 1) < KSUM_BAR[name]

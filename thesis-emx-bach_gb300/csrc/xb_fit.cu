@@ -167,6 +167,64 @@ __global__ void __launch_bounds__(LU_THREADS)
   if(tid == 0) kernelSums[s] = b[1];
 }
 
+// ------------------------------------------- per-stamp test fit, mixed ----
+// The mixed path only needs each stamp's kernel sum (the first unknown of
+// its test system; cd.cl:46-52) for the sigma clip of cd, and its Q, B already
+// differ from the plain ones at the 1e-11 level, so it solves the symmetric
+// positive definite test system (createTestMat / createTestVec, cd.cl:15-44)
+// by LDL^T without pivoting, one warp per stamp, instead of the reference's
+// LU with partial pivoting.  The kernel-sum unknown is ordered last and the
+// right-hand side rides along as an extra column of the elimination, so after
+// it the kernel sum is that column's last entry over the last pivot (with L D
+// L^T x = b and z = L^-1 b, the last row of L^T x = D^-1 z is x_n = z_n / d_n):
+// no back substitution.  A zero pivot becomes 1e-20, as in the reference's LU.
+constexpr int TF_WARPS = 4;
+__global__ void __launch_bounds__(TF_WARPS * 32)
+    k_stamp_test_fit_ldl(const double* __restrict__ Q, const double* __restrict__ B, int qc,
+                         int nStamps, const int* __restrict__ liveN,
+                         double* __restrict__ kernelSums) {
+  extern __shared__ double tf_s[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * TF_WARPS + warp;
+  const int nLive = liveN ? min(nStamps, *liveN) : nStamps;
+  if(s >= nLive) return;  // whole warps only; the kernel has no block barrier
+  const int n = qc - 1, ld = n + 1;  // unknowns; row stride (column n = the RHS)
+  double* a = tf_s + (size_t)warp * n * ld;
+  const double* Qs = Q + (size_t)s * qc * qc;
+  // unknown order: 2, 3, ..., n, then 1 (the kernel sum)
+  auto unk = [&](int p) { return p < n - 1 ? p + 2 : 1; };
+  for(int e = lane; e < n * ld; e += 32) {
+    const int p = e / ld, q = e % ld, u = unk(p);
+    double v;
+    if(q == n) {
+      v = B[(size_t)s * qc + u];
+    } else {
+      const int t = unk(q);
+      v = Qs[(size_t)max(u, t) * qc + min(u, t)];
+    }
+    a[e] = v;
+  }
+  __syncwarp();
+  for(int k = 0; k < n; k++) {
+    double d = a[k * ld + k];
+    if(d == 0.0) d = 1.0e-20;
+    const double rd = 1.0 / d;
+    const double bk = a[k * ld + n];
+    for(int i = k + 1 + lane; i < n; i += 32) {
+      double* ai = a + i * ld;
+      const double li = ai[k] * rd;
+      for(int j = k + 1; j <= i; j++) ai[j] = fma(-li, a[j * ld + k], ai[j]);
+      ai[n] = fma(-li, bk, ai[n]);
+    }
+    __syncwarp();
+  }
+  if(lane == 0) {
+    double d = a[(n - 1) * ld + n - 1];
+    if(d == 0.0) d = 1.0e-20;
+    kernelSums[s] = a[(n - 1) * ld + n] / d;
+  }
+}
+
 // ------------------------------------------------------------ cd select ---
 // sigmaClip of the kernel sums (10 iterations, cdkscUtil.cpp:74-76) and
 // genCdTestStamps (cd.cl:54-94) in ascending order.
@@ -1108,11 +1166,17 @@ void stageCd(xb_ctx* c) {
   double* merit = buf<double>(c, "cd_merit", 2);
   const int qc = g.qCount;
   const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
+  const size_t smemLdl = (size_t)TF_WARPS * (qc - 1) * qc * sizeof(double);
+  if(mixedMode(c)) XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl, c->device));
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
     if(S.n > 0) {
       { KT_SCOPE(c, "stamp_test_fit");
-      k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, nullptr, ks[si]);
+      if(mixedMode(c))
+        k_stamp_test_fit_ldl<<<(S.n + TF_WARPS - 1) / TF_WARPS, TF_WARPS * 32, smemLdl, c->stream>>>(
+            S.Q, S.B, qc, S.n, nullptr, ks[si]);
+      else
+        k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, nullptr, ks[si]);
       XB_LAUNCHED(c);
       }
     }
@@ -1236,9 +1300,15 @@ void stageCdGraph(xb_ctx* c, long long lCd[2]) {
   double* merit = buf<double>(c, "cd_merit", 2);
   const int qc = g.qCount;
   const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
+  const size_t smemLdl = (size_t)TF_WARPS * (qc - 1) * qc * sizeof(double);
+  if(mixedMode(c)) XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl, c->device));
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
-    k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, S.dN, ks[si]);
+    if(mixedMode(c))
+      k_stamp_test_fit_ldl<<<(S.n + TF_WARPS - 1) / TF_WARPS, TF_WARPS * 32, smemLdl, c->stream>>>(
+          S.Q, S.B, qc, S.n, S.dN, ks[si]);
+    else
+      k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, S.dN, ks[si]);
     XB_LAUNCHED(c);
     k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, S.dN, c->p.sigClipAlpha, c->p.sigKernFit,
                                           f.flags, f.cs, f.cs2, testIdx[si], nTest + si,
