@@ -361,19 +361,33 @@ __global__ void __launch_bounds__(MX_THREADS)
   if(live) {
     const float bgF = (float)sBg;
     float part = 0.f;
-    for(int j = tid; j < pix; j += MX_THREADS) {
-      float sh = 0.f, sl = 0.f;
+    // four consecutive pixels per thread, read as float4 (ldW is a multiple
+    // of 4 and covers pix rounded up), rows unrolled so that several loads
+    // are in flight; each pixel's sum runs over the rows in order
+    for(int j0 = 4 * tid; j0 < pix; j0 += 4 * MX_THREADS) {
+      float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 7
       for(int i = 0; i < nPSF; i++) {
-        const float wv = Ws[(size_t)i * ldW + j];
-        const float ph = cHi[i] * wv;
-        const float pe = fmaf(cHi[i], wv, -ph) + cLo[i] * wv;  // exact low part + lo term
-        const float ts = sh + ph;                             // two-sum of sh and ph
-        const float bp = ts - sh;
-        const float er = (sh - (ts - bp)) + (ph - bp);
-        sh = ts;
-        sl += er + pe;
+        const float4 w4 = *(const float4*)(Ws + (size_t)i * ldW + j0);
+        const float wq[4] = {w4.x, w4.y, w4.z, w4.w};
+        const float ch = cHi[i], cl = cLo[i];
+#pragma unroll
+        for(int q = 0; q < 4; q++) {
+          const float wv = wq[q];
+          const float ph = ch * wv;
+          const float pe = fmaf(ch, wv, -ph) + cl * wv;  // exact low part + lo term
+          const float ts = sh[q] + ph;                   // two-sum of sh and ph
+          const float bp = ts - sh[q];
+          const float er = (sh[q] - (ts - bp)) + (ph - bp);
+          sh[q] = ts;
+          sl[q] += er + pe;
+        }
       }
-      const float m0 = (float)((double)sh + (double)sl);
+#pragma unroll
+      for(int q = 0; q < 4; q++) {
+      const int j = j0 + q;
+      if(j >= pix) break;
+      const float m0 = (float)((double)sh[q] + (double)sl[q]);
       const int ax = j % fSS - fSS / 2 + c.x, ay = j / fSS - fSS / 2 + c.y;
       const size_t ai = (size_t)min(max(ax, 0), w - 1) + (size_t)min(max(ay, 0), h - 1) * w;
       const float sF = (float)sImg[ai];
@@ -385,6 +399,7 @@ __global__ void __launch_bounds__(MX_THREADS)
           part += d * d / ((fabsf((float)tImg[ai]) + fabsf(sF)) * invGain + rn2x2);
           cnt++;
         }
+      }
       }
     }
     acc = (double)part;
