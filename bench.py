@@ -261,7 +261,9 @@ def run_reference(args):
 #     49 x 961 x 21 MAC (2.97 MFLOP, FP32 in mixed mode) and the Gram
 #     1275 x 961 + B 50 x 961 MAC (2.45 MFLOP, tensor cores);
 #   global solve: the reference's LU, 2/3 n^3 FLOP (n = 292); the LDL^T here
-#     executes n^3 / 3 of them.
+#     executes n^3 / 3 of them;
+#   sss (stamp statistics, substamp search): 6 B of HBM per pixel and image
+#     (the pixel and its mask bits), the stamps tiling the frame.
 FILL_PASS_FLOP = 2.0 * (15 * 1581 * 21 + 49 * 961 * 21)
 FILL_GRAM_FLOP = 2.0 * (1275 * 961 + 50 * 961)
 CONV_BYTES_PER_PX = 20
@@ -308,6 +310,16 @@ def rooflines(kernels, params, n_pix, mode, stamps, peaks):
                                 peak_source=peaks["bf16_source"])}
         for v in out["fill_gram"].values():
             v.pop("ms_per_launch")
+    # sss: every stamp pixel and its mask bits once per pass, both images
+    # (the stamps tile the frame): 2 x 6 B per pixel
+    for name in ("stamp_stats", "find_substamps"):
+        if name in kernels:
+            k = kernels[name]
+            byt = 2 * 6 * n_pix
+            out[name] = view("hbm", byt, k["ms_total"], peaks["hbm"], "GB/s", 1e9,
+                             bytes_per_frame=byt, ms_per_frame=k["ms_total"],
+                             peak_source=peaks["hbm_source"])
+            out[name].pop("ms_per_launch")
     if "global_ldl" in kernels:
         k = kernels["global_ldl"]
         ms = k["ms_total"] / k["launches"]
@@ -459,6 +471,67 @@ def run_config4(args):
             e1.synchronize()
             ms += e0.elapsed_time(e1)
     launches = sum(wk.launches() for wk in workers) - l0
+    # end to end: pinned host frames in, host images out, the same batch
+    hT = [torch.from_numpy(f[0]).pin_memory() for f in frames]
+    hS = [torch.from_numpy(f[1]).pin_memory() for f in frames]
+    hC = [torch.empty_like(t).pin_memory() for t in hT]
+    hD = [torch.empty_like(t).pin_memory() for t in hT]
+
+    def run_e2e():
+        batch.run_ptrs([t.data_ptr() for t in hT], [t.data_ptr() for t in hS], ws, hs,
+                       [t.data_ptr() for t in hC], [t.data_ptr() for t in hD])
+    run_e2e()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        run_e2e()
+        e1.record(st)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+    e2e = {"value": n_pairs * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+           "h2d_bytes_per_step": 2 * 4 * pix, "d2h_bytes_per_step": 2 * 4 * pix}
+    # rooflines from the largest pair, one frame with the kernel timers on
+    big = max(range(n_pairs), key=lambda i: ws[i] * hs[i])
+    kctx = xbach.Context(params[big])
+    if use_rank:
+        ranker.enable(kctx, w_rank, policy=1, tau=args.rank_tau)
+
+    def one_big():
+        kctx.init_device(dT[big].data_ptr(), dS[big].data_ptr(), ws[big], hs[big])
+        for stage in (kctx.sss, kctx.cmv, kctx.cd, kctx.ksc, kctx.conv, kctx.sub):
+            stage()
+    one_big()
+    torch.cuda.synchronize()
+    kctx.set_option("time_kernels", 1)
+    one_big()
+    torch.cuda.synchronize()
+    kernels = {}
+    for name in ("stamp_stats", "find_substamps", "fill_gram", "stamp_test_fit", "sigs",
+                 "global_ldl", "global_solve", "mx_build", "conv_sub", "rank_score"):
+        kms, kn = kctx.kernel_time(name)
+        if kn:
+            kernels[name] = {"ms_total": kms, "launches": kn}
+    kctx.set_option("time_kernels", 0)
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
+    fp32_peak, fp64_peak = xbach.measure_fma_peaks(0)
+    stamps = kctx.scalar("nstamps0") + kctx.scalar("nstamps1") + kctx.scalar("ksc_refills")
+    peaks = {"hbm": hbm_peak, "bf16": bf16_peak, "fp32": fp32_peak, "fp64": fp64_peak,
+             "hbm_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+             "bf16_source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)",
+             "fma_source": "measured in this run by xb_measure_fma_peaks"}
+    roofs = rooflines(kernels, params[big], ws[big] * hs[big], args.mode, stamps, peaks)
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_total"]) if kernels else None
+    roof = dict(roofs[dominant]) if dominant in roofs else None
+    if roof is not None and "bound" not in roof:
+        roof = dict(next(iter(roof.values())))
+    if roof is not None:
+        roof.update({"kernel": dominant, "traffic": None,
+                     "pair": f"{ws[big]}x{hs[big]} (the batch's largest)"})
+    kctx.close()
     # a sample of pairs against single contexts run stage by stage
     check = sorted(range(n_pairs), key=lambda i: ws[i] * hs[i])
     check = check[:2] + check[-1:]
@@ -495,7 +568,8 @@ def run_config4(args):
                    "l2": "flushed before every step; inputs exceed L2",
                    "inputs": "device-resident FP32 T,S"},
         "megapixels_per_s": pix * args.steps / (ms / 1000.0) / 1e6,
-        "gpu_launches": launches, "clocks": clk.summary(), "roofline": None, "e2e": None,
+        "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "rooflines": roofs,
+        "kernels_largest_pair": kernels, "e2e": e2e,
         "first_pass_s": capture_s,
         "check_vs_stage_by_stage": {"pairs": check, "identical": same},
     }
