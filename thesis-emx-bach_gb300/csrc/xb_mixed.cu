@@ -1060,13 +1060,38 @@ constexpr int MXB_ROWS = 64, MXB_T = 32, MXB_MAXC = 32;
 
 __device__ __forceinline__ int mxPairRow(int qa, int qb) { return (qa - 1) * qa / 2 - 1 + (qb - 1); }
 
+// The spatial factors of the matrix build for the listed stamps: Y[t][c] =
+// xf^a yf^b of monomial c at stamp t's substamp (0 for a stamp without one)
+// and Y[t][nMono] = 1, split into hi + lo floats; once per build instead of
+// once per row block of k_mx_build.
+__global__ void k_mx_mono(const int* __restrict__ list, int nList, const int* __restrict__ liveN,
+                          const int* __restrict__ count, const int* __restrict__ cur,
+                          const int2* __restrict__ ssxy, int maxSS, const int2* __restrict__ monoExp,
+                          int nMono, int w, int h, float2* __restrict__ Y) {
+  if(liveN) nList = min(nList, *liveN);
+  const int NC = nMono + 1;
+  for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < nList * NC; e += gridDim.x * blockDim.x) {
+    const int t = e / NC, cI = e % NC, st = list[t];
+    double v = 0.0;
+    if(cI == nMono) {
+      v = 1.0;
+    } else if(cur[st] < count[st]) {
+      const int2 c = ssxy[(size_t)st * maxSS + cur[st]];
+      const int2 ex = monoExp[cI];
+      v = ipowD(floatNormD(c.x, w), ex.x) * ipowD(floatNormD(c.y, h), ex.y);
+    }
+    const float hi = (float)v;
+    Y[e] = make_float2(hi, (float)(v - (double)hi));
+  }
+}
+
 __global__ void __launch_bounds__(256)
     k_mx_build(const int* __restrict__ list, int nList, const int* __restrict__ liveN,
                const int* __restrict__ count,
                const int* __restrict__ cur, const int2* __restrict__ ssxy, int maxSS,
                const double* __restrict__ Q, int qc, const double* __restrict__ dots, int stride,
-               const double* __restrict__ B, const int2* __restrict__ monoExp, int nMono, int w,
-               int h, int nC1, int nRows, double* __restrict__ P) {
+               const double* __restrict__ B, const float2* __restrict__ Ytab, int nMono,
+               int nC1, int nRows, double* __restrict__ P) {
   // X and Y as double-float pairs (hi + lo in FP32): the products and sums
   // run on the FP32 pipe with about 48 bits (two-product by FMA, two-sum
   // with a running error term), far below the 2^-36 of the Gram entries
@@ -1103,20 +1128,11 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   for(int e = tid; e < MXB_T * NC; e += 256) {
-    const int tt = e / NC, cI = e % NC, st = sS[tt];
-    double v = 0.0;
-    if(st >= 0) {
-      if(cI == nMono) {
-        v = 1.0;
-      } else if(cur[st] < count[st]) {
-        const int2 c = ssxy[(size_t)st * maxSS + cur[st]];
-        const int2 ex = monoExp[cI];
-        v = ipowD(floatNormD(c.x, w), ex.x) * ipowD(floatNormD(c.y, h), ex.y);
-      }
-    }
-    const float hi = (float)v;
-    YsH[tt][cI] = hi;
-    YsL[tt][cI] = (float)(v - (double)hi);
+    const int tt = e / NC, cI = e % NC;
+    float2 y = make_float2(0.f, 0.f);
+    if(sS[tt] >= 0) y = Ytab[(size_t)(t0 + tt) * NC + cI];
+    YsH[tt][cI] = y.x;
+    YsL[tt][cI] = y.y;
   }
   for(int e = tid; e < MXB_ROWS * MXB_T; e += 256) {
     const int r = e / MXB_T, tt = e % MXB_T, st = sS[tt], code = rowSrc[r];
@@ -1419,9 +1435,13 @@ void buildSystemMixed(xb_ctx* c, int si, const int* dList, int nList, int bgBase
   double* P = buf<double>(c, "mx_partials", (size_t)std::max(nSplit, 1) * nRows * (nMono + 1));
   if(nSplit > 0) {
     KT_SCOPE(c, "mx_build");
+    float2* Ytab = buf<float2>(c, "mx_mono", (size_t)nList * (nMono + 1));
+    k_mx_mono<<<std::min((nList * (nMono + 1) + 255) / 256, c->smCount * 4), 256, 0, c->stream>>>(
+        dList, nList, liveN, S.count, S.cur, S.ssxy, g.maxSS, dExp, nMono, c->w, c->h, Ytab);
+    XB_LAUNCHED(c);
     k_mx_build<<<dim3((nRows + MXB_ROWS - 1) / MXB_ROWS, nSplit), 256, 0, c->stream>>>(
         dList, nList, liveN, S.count, S.cur, S.ssxy, g.maxSS, S.Q, g.qCount, S.dots, stride, S.B,
-        dExp, nMono, c->w, c->h, g.nComp1, nRows, P);
+        Ytab, nMono, g.nComp1, nRows, P);
     XB_LAUNCHED(c);
   }
   {

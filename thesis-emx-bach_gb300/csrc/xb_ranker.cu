@@ -247,14 +247,21 @@ __device__ __forceinline__ void rkLoad(const float* __restrict__ stats, const fl
   for(int q = threadIdx.x; q < RK_NS; q += RK_T) A.st[q] = stats[(size_t)i * RK_NS + q];
 }
 
+// slots (optional): the candidate slots of the stamps, maxSS per stamp; a
+// slot that is empty, past nRank in its stamp or in a stamp past *liveN
+// gets no score (k_rank_order reads none for it).
 template <class WT>
 __global__ void __launch_bounds__(RK_T)
     k_rank_forward(const WT* __restrict__ W, const float* __restrict__ stats,
-                   const float* __restrict__ pix, int n, float* __restrict__ logit) {
+                   const float* __restrict__ pix, int n, float* __restrict__ logit,
+                   const int2* __restrict__ slots = nullptr, int maxSS = 1, int nRank = 1,
+                   const int* __restrict__ liveN = nullptr) {
   __shared__ float Ws[RK_NP];
   __shared__ RkAct A;
   for(int q = threadIdx.x; q < RK_NP; q += RK_T) Ws[q] = rkWeight(W, q);
   for(int i = blockIdx.x; i < n; i += gridDim.x) {
+    if(slots && ((liveN && i / maxSS >= *liveN) || i % maxSS >= nRank || slots[i].x == INT_MAX))
+      continue;  // uniform over the CTA
     __syncthreads();
     rkLoad(stats, pix, i, A);
     __syncthreads();
@@ -562,6 +569,7 @@ void rankSubstamps(xb_ctx* c) {
     float* dStats = buf<float>(c, "rank_stats", (size_t)n * RK_NS);
     float* dPix = buf<float>(c, "rank_pix", (size_t)n * RK_PIX);
     float* dLogit = buf<float>(c, "rank_logit", n);
+    const int nRank = c->rankCandidates > 0 ? std::min(c->rankCandidates, g.maxSS) : g.maxSS;
     if(c->imgIsF64)
       k_rank_features<double><<<n, RK_T, 0, c->stream>>>(
           (const double*)c->img[0], (const double*)c->img[1], c->mask, c->w, c->h, S.orig,
@@ -576,11 +584,9 @@ void rankSubstamps(xb_ctx* c) {
     {
       KT_SCOPE(c, "rank_score");
       k_rank_forward<__nv_bfloat16><<<std::min(n, c->smCount * 8), RK_T, 0, c->stream>>>(
-          (const __nv_bfloat16*)c->rankW, dStats, dPix,
-                                                                          n, dLogit);
+          (const __nv_bfloat16*)c->rankW, dStats, dPix, n, dLogit, S.ssxy, g.maxSS, nRank, S.dN);
       XB_LAUNCHED(c);
     }
-    const int nRank = c->rankCandidates > 0 ? std::min(c->rankCandidates, g.maxSS) : g.maxSS;
     k_rank_order<<<(S.n + 127) / 128, 128, 0, c->stream>>>(S.ssxy, S.ssval, dLogit, S.n, S.dN,
                                                            g.maxSS, nRank, c->rank, zTau);
     XB_LAUNCHED(c);
