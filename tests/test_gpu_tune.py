@@ -1,5 +1,8 @@
 """The autotuner: every tile-shape variant of a tunable kernel gives the same
-images, and the tuner records the variant it chose."""
+images, and the tuner records the variant it chose.  Option tune_variant = v
+forces variant v (or the last one) of every tunable kernel: the conv's blocks
+per CTA, the LDL^T schedule, the fused fill + Gram's threads per CTA and the
+test fit's warps per CTA."""
 import numpy as np
 import pytest
 
@@ -25,4 +28,9 @@ def test_conv_variants_identical_and_choice_recorded():
     ctx = xbach.Context(xbach.default_params(**kw))
     ctx.run_all(T, S)  # autotune on (default)
     assert int(ctx.scalar("tune:conv_sub_f32")) in (0, 1, 2)
+    # the fused fill + Gram (384 or 256 threads) and the warp-per-stamp test
+    # fit (4, 2 or 8 warps) are tuned too; their variants are part of the
+    # forced runs above, which gave the same images
+    assert int(ctx.scalar("tune:fill_gram")) in (0, 1)
+    assert int(ctx.scalar("tune:stamp_test_fit_ldl")) in (0, 1, 2)
     assert np.array_equal(ctx.image(xbach.XB_IMG_DIFF, f64=False), images[0][0])

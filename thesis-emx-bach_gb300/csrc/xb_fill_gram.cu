@@ -51,7 +51,6 @@ namespace xb {
 
 namespace {
 
-constexpr int FG_THREADS = 384;
 constexpr int FG_HK = 10;   // the kernel half-width the fused kernel is built for
 constexpr int FG_R8 = 8;    // outputs per thread item (rows of the Y pass, pixels of the X pass)
 constexpr int FG_GP = 7;    // Y filters per pass
@@ -160,10 +159,11 @@ __device__ __forceinline__ void maxBits(unsigned* slot, float m) {
   atomicMax(slot, __float_as_uint(m));  // m >= 0: the bit patterns are ordered
 }
 
-__global__ void __launch_bounds__(FG_THREADS, 2)
+template <int NT>
+__global__ void __launch_bounds__(NT, 2)
     k_fill_gram(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ FillGramArgs a) {
   using namespace tc;
-  constexpr int NT = FG_THREADS, HK = FG_HK, FK = 2 * HK + 1;
+  constexpr int HK = FG_HK, FK = 2 * HK + 1;
   extern __shared__ __align__(1024) unsigned char fg_s[];
   __shared__ float imgRow[1024];  // K <= 961 pixels, padded to whole chunks
   __shared__ int expo[RB];
@@ -491,9 +491,16 @@ void fillGramLaunch(xb_ctx* c, int si, const int* dList, int nList, int imgConv,
            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
       a.useTma = c->fillGramTma;
   }
-  XB_CUDA(allowMaxDynamicSmem((const void*)k_fill_gram, c->device));
-  k_fill_gram<<<nList, FG_THREADS, L.total, c->stream>>>(tm, a);
-  XB_LAUNCHED(c);
+  // threads per CTA: 384 (variant 0) or 256; both keep two CTAs per SM and
+  // give the same W and G bit for bit (every output's arithmetic is per item)
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_fill_gram<384>, c->device));
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_fill_gram<256>, c->device));
+  auto launch = [&](int v) {
+    if(v == 1) k_fill_gram<256><<<nList, 256, L.total, c->stream>>>(tm, a);
+    else k_fill_gram<384><<<nList, 384, L.total, c->stream>>>(tm, a);
+    XB_LAUNCHED(c);
+  };
+  launch(tunedVariant(c, "fill_gram", (long long)g.fSS * 100000 + g.nPSF * 100 + g.nBG, 2, launch));
 }
 
 }  // namespace xb

@@ -178,7 +178,8 @@ __global__ void __launch_bounds__(LU_THREADS)
 // it the kernel sum is that column's last entry over the last pivot (with L D
 // L^T x = b and z = L^-1 b, the last row of L^T x = D^-1 z is x_n = z_n / d_n):
 // no back substitution.  A zero pivot becomes 1e-20, as in the reference's LU.
-constexpr int TF_WARPS = 4;
+// Warps (stamps) per CTA: 4 (variant 0), 2 or 8; identical results.
+template <int TF_WARPS>
 __global__ void __launch_bounds__(TF_WARPS * 32)
     k_stamp_test_fit_ldl(const double* __restrict__ Q, const double* __restrict__ B, int qc,
                          int nStamps, const int* __restrict__ liveN,
@@ -1153,6 +1154,24 @@ void kernelSumLaunch(xb_ctx* c, const double* dSol, double xf, double yf, int tr
   }
 }
 
+// The mixed path's per-stamp test fits (k_stamp_test_fit_ldl), with the
+// tuned number of warps (stamps) per CTA.
+static void testFitLdl(xb_ctx* c, const StampSetDev& S, int qc, const int* liveN, double* ks) {
+  auto launch = [&](int v) {
+    const int W = v == 1 ? 2 : (v == 2 ? 8 : 4);
+    const size_t smem = (size_t)W * (qc - 1) * qc * sizeof(double);
+    const int grid = (S.n + W - 1) / W;
+    if(W == 2) k_stamp_test_fit_ldl<2><<<grid, 64, smem, c->stream>>>(S.Q, S.B, qc, S.n, liveN, ks);
+    else if(W == 8) k_stamp_test_fit_ldl<8><<<grid, 256, smem, c->stream>>>(S.Q, S.B, qc, S.n, liveN, ks);
+    else k_stamp_test_fit_ldl<4><<<grid, 128, smem, c->stream>>>(S.Q, S.B, qc, S.n, liveN, ks);
+    XB_LAUNCHED(c);
+  };
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<2>, c->device));
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<4>, c->device));
+  XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<8>, c->device));
+  launch(tunedVariant(c, "stamp_test_fit_ldl", (long long)qc, 3, launch));
+}
+
 void stageCd(xb_ctx* c) {
   const Geo& g = c->g;
   const int nMax = std::max(std::max(c->set[0].n, c->set[1].n), 1);
@@ -1166,18 +1185,16 @@ void stageCd(xb_ctx* c) {
   double* merit = buf<double>(c, "cd_merit", 2);
   const int qc = g.qCount;
   const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
-  const size_t smemLdl = (size_t)TF_WARPS * (qc - 1) * qc * sizeof(double);
-  if(mixedMode(c)) XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl, c->device));
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
     if(S.n > 0) {
       { KT_SCOPE(c, "stamp_test_fit");
-      if(mixedMode(c))
-        k_stamp_test_fit_ldl<<<(S.n + TF_WARPS - 1) / TF_WARPS, TF_WARPS * 32, smemLdl, c->stream>>>(
-            S.Q, S.B, qc, S.n, nullptr, ks[si]);
-      else
+      if(mixedMode(c)) {
+        testFitLdl(c, S, qc, nullptr, ks[si]);
+      } else {
         k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, nullptr, ks[si]);
-      XB_LAUNCHED(c);
+        XB_LAUNCHED(c);
+      }
       }
     }
     { KT_SCOPE(c, "cd_select");
@@ -1300,16 +1317,14 @@ void stageCdGraph(xb_ctx* c, long long lCd[2]) {
   double* merit = buf<double>(c, "cd_merit", 2);
   const int qc = g.qCount;
   const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
-  const size_t smemLdl = (size_t)TF_WARPS * (qc - 1) * qc * sizeof(double);
-  if(mixedMode(c)) XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl, c->device));
   for(int si = 0; si < 2; si++) {
     StampSetDev& S = c->set[si];
-    if(mixedMode(c))
-      k_stamp_test_fit_ldl<<<(S.n + TF_WARPS - 1) / TF_WARPS, TF_WARPS * 32, smemLdl, c->stream>>>(
-          S.Q, S.B, qc, S.n, S.dN, ks[si]);
-    else
+    if(mixedMode(c)) {
+      testFitLdl(c, S, qc, S.dN, ks[si]);
+    } else {
       k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, S.dN, ks[si]);
-    XB_LAUNCHED(c);
+      XB_LAUNCHED(c);
+    }
     k_cd_select<<<1, 256, 0, c->stream>>>(ks[si], S.n, S.dN, c->p.sigClipAlpha, c->p.sigKernFit,
                                           f.flags, f.cs, f.cs2, testIdx[si], nTest + si,
                                           stats + 2 * si);
