@@ -21,10 +21,10 @@ def test_conv_variants_identical_and_choice_recorded():
         ctx.set_option("tune_variant", v)
         ctx.run_all(T, S)
         images.append((ctx.image(xbach.XB_IMG_DIFF, f64=False),
-                       ctx.image(xbach.XB_IMG_CONV, f64=False)))
+                       ctx.image(xbach.XB_IMG_CONV, f64=False), ctx.mask()))
     for v in (1, 2):
-        assert np.array_equal(images[0][0], images[v][0]), v
-        assert np.array_equal(images[0][1], images[v][1]), v
+        for i in range(3):
+            assert np.array_equal(images[0][i], images[v][i]), (v, i)
     ctx = xbach.Context(xbach.default_params(**kw))
     ctx.run_all(T, S)  # autotune on (default)
     assert int(ctx.scalar("tune:conv_sub_f32")) in (0, 1, 2)

@@ -1155,9 +1155,25 @@ void kernelSumLaunch(xb_ctx* c, const double* dSol, double xf, double yf, int tr
 }
 
 // The mixed path's per-stamp test fits (k_stamp_test_fit_ldl), with the
-// tuned number of warps (stamps) per CTA.
+// tuned number of warps (stamps) per CTA among those whose factors fit in
+// shared memory (8 warps of a 61-row system do not); systems too large for
+// two warps take the one-CTA-per-stamp LU of the plain path.
 static void testFitLdl(xb_ctx* c, const StampSetDev& S, int qc, const int* liveN, double* ks) {
+  int optin = 0;
+  XB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  const size_t perWarp = (size_t)(qc - 1) * qc * sizeof(double);
+  if(2 * perWarp > (size_t)optin) {
+    const size_t smemLU = ((size_t)qc * qc + 3 * qc) * sizeof(double) + qc * sizeof(int);
+    if(smemLU > (size_t)optin) throw XbError{XB_ERR_UNSUPPORTED, "test fit: system too large"};
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit, c->device));
+    k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, liveN, ks);
+    XB_LAUNCHED(c);
+    return;
+  }
+  // variants: 0 = 4 warps, 1 = 2 warps, 2 = 8 warps
+  const int nVar = 8 * perWarp <= (size_t)optin ? 3 : 2;
   auto launch = [&](int v) {
+    if(v == 0 && 4 * perWarp > (size_t)optin) v = 1;
     const int W = v == 1 ? 2 : (v == 2 ? 8 : 4);
     const size_t smem = (size_t)W * (qc - 1) * qc * sizeof(double);
     const int grid = (S.n + W - 1) / W;
@@ -1169,7 +1185,7 @@ static void testFitLdl(xb_ctx* c, const StampSetDev& S, int qc, const int* liveN
   XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<2>, c->device));
   XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<4>, c->device));
   XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit_ldl<8>, c->device));
-  launch(tunedVariant(c, "stamp_test_fit_ldl", (long long)qc, 3, launch));
+  launch(tunedVariant(c, "stamp_test_fit_ldl", (long long)qc, nVar, launch));
 }
 
 void stageCd(xb_ctx* c) {
@@ -1192,6 +1208,7 @@ void stageCd(xb_ctx* c) {
       if(mixedMode(c)) {
         testFitLdl(c, S, qc, nullptr, ks[si]);
       } else {
+        XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit, c->device));
         k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, nullptr, ks[si]);
         XB_LAUNCHED(c);
       }
@@ -1322,6 +1339,7 @@ void stageCdGraph(xb_ctx* c, long long lCd[2]) {
     if(mixedMode(c)) {
       testFitLdl(c, S, qc, S.dN, ks[si]);
     } else {
+      XB_CUDA(allowMaxDynamicSmem((const void*)k_stamp_test_fit, c->device));
       k_stamp_test_fit<<<S.n, LU_THREADS, smemLU, c->stream>>>(S.Q, S.B, qc, S.dN, ks[si]);
       XB_LAUNCHED(c);
     }

@@ -635,12 +635,32 @@ __global__ void __launch_bounds__(1024)
 
 // -------------------------------------------------- conv + sub in FP32 ----
 // BX kernel blocks (BX*21 columns) x one block row (21 rows) per CTA; each
-// thread produces seven adjacent pixels of one block row, streaming the image
-// row through registers.  BX (2, 4 or 8) is chosen by the autotuner.
+// thread produces a 7 x 3 pixel tile of one block: every image row it loads
+// into registers (27 values) feeds its three output rows through three
+// kernel rows (broadcast float4 reads), 441 FMAs per 27 + 18 shared loads.
+// BX (4, 6 or 8) is chosen by the autotuner; the three give identical
+// images.
 struct ConvArgsF {
   int w, h, hK, fK, nPSF, kOrder, bgOrder, nComp, scaleConv;
   float tH, tL;
+  int xSteps;  // kernel blocks per row (block-centre table of k_conv_sub_f32)
 };
+
+// Normalised centres of the fK x fK kernel blocks, xf of the xSteps block
+// columns then yf of the block rows: (centre - w/2) / (w/2) in FP64, the
+// coordinates of the spatial kernel terms (conv(), src/bach.cpp:339-350).
+__global__ void k_block_centres(int w, int h, int fK, int xSteps, int ySteps,
+                                double* __restrict__ xy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int hK = fK / 2;
+  if(i < xSteps) {
+    const double hx = 0.5 * w;
+    xy[i] = (i * fK + 2 * hK - hx) / hx;
+  } else if(i < xSteps + ySteps) {
+    const double hy = 0.5 * h;
+    xy[i] = ((i - xSteps) * fK + 2 * hK - hy) / hy;
+  }
+}
 
 __device__ __forceinline__ uint16_t convMaskF(float t, float tH, float tL) {
   uint16_t m = 0;
@@ -657,138 +677,236 @@ __device__ __forceinline__ uint16_t afterMaskF(float t, float tH, float tL) {
   return m;
 }
 
-template <int FK, int CV_BX>
-__global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
-    k_conv_sub_f32(const float* __restrict__ I, const float* __restrict__ O,
-                   const double* __restrict__ sol, const double* __restrict__ Kt,
-                   const double* __restrict__ kernSumPtr, ConvArgsF a,
-                   const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
-                   float* __restrict__ convF, float* __restrict__ diffF) {
-  constexpr int HK = FK / 2, NK = FK * FK, PX = 7, TPR = FK / PX;  // threads per block row
-  constexpr int TW = CV_BX * FK + 2 * HK, TH = FK + 2 * HK;
-  // row padding with at most 2-way bank conflicts for the pixel loop's lanes
-  constexpr int TPAD = CV_BX == 4 ? 2 : (CV_BX == 2 ? 0 : 1);
-  __shared__ float tile[TH][TW + TPAD];
-  __shared__ unsigned char bad[TH][TW + TPAD];
-  __shared__ unsigned char rowBad[TH][CV_BX * FK];  // OR of bad over the x window
-  __shared__ float kern[CV_BX][NK];
-  __shared__ double poly[CV_BX][16];
-  __shared__ float aks[CV_BX];
-  __shared__ float bgc[16];  // background coefficients (getBackground), FP32
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  const int xB0 = blockIdx.x * CV_BX, yB = blockIdx.y;
-  const int x0 = xB0 * FK, y0 = yB * FK;   // tile origin; block pixels start at +HK
-  const int nC2 = (a.kOrder + 1) * (a.kOrder + 2) / 2;
-  if(tid < CV_BX) {
-    // spatial terms xf^i yf^j at the block centre (conv(), src/bach.cpp:339-350)
-    const double hx = 0.5 * a.w, hy = 0.5 * a.h;
-    const double xf = ((xB0 + tid) * FK + 2 * HK - hx) / hx, yf = (yB * FK + 2 * HK - hy) / hy;
-    double ax = 1.0;
-    int t = 0;
-    for(int x = 0; x <= a.kOrder; x++) {
-      double ay = 1.0;
-      for(int y = 0; y <= a.kOrder - x; y++) {
-        poly[tid][t++] = ax * ay;
-        ay *= yf;
-      }
-      ax *= xf;
+// Shared-memory layout of k_conv_sub_f32 for BX blocks per CTA.  The tile
+// row stride S is padded so that the window loads of a warp (lanes ordered
+// block, column group, row group) fall in 32 distinct banks.
+template <int FK, int BX>
+struct ConvTileF {
+  static constexpr int HK = FK / 2, NK = FK * FK, PX = 7, RY = 3;
+  static constexpr int TPB = (FK / PX) * (FK / RY);  // threads per kernel block
+  static constexpr int NT = BX * TPB;
+  static constexpr int TW = BX * FK + 2 * HK, TH = FK + 2 * HK;
+  static constexpr int S = TW + (BX == 2 ? 13 : BX == 4 ? 3 : BX == 6 ? 25 : 15);
+  static constexpr int NW = (TW + 31) / 32 + 1;  // bad-flag words per tile row (+1: 64-bit reads)
+  static constexpr int KS = 24;                  // kernel row stride (float4 reads)
+  static constexpr size_t OFF_KERN = ((size_t)TH * S * 4 + 15) / 16 * 16;
+  static constexpr size_t OFF_BITS = OFF_KERN + (size_t)BX * FK * KS * 4;
+  static constexpr size_t OFF_AKS = OFF_BITS + (size_t)TH * NW * 4;
+  static constexpr size_t OFF_FLAG = OFF_AKS + (size_t)(BX + 16) * 4;  // per output pixel
+  static constexpr size_t BYTES = OFF_FLAG + (size_t)BX * NK;
+  // after the sums the kernel rows hold the CTA's conv sums, row-major
+  static_assert((size_t)BX * FK * KS >= (size_t)BX * NK, "staging fits the kernel rows");
+};
+
+// Kernel of each of BX blocks at its centre (conv(), src/bach.cpp:339-350)
+// from the FP64 spatial-term images Kt[t] (t over xf^i yf^j, i outer), one
+// tap per thread for all blocks: the terms of each x power collapsed over yf
+// (shared by the CTA's blocks) by Horner, then Horner in the block's xf;
+// FP64, rounded once to FP32 into rows of KS = 24 floats.
+template <int K, int FK, int BX, int NT>
+__device__ __forceinline__ void convBlockKernels(const double* __restrict__ Kt,
+                                                 const double* __restrict__ xfTab, double yf,
+                                                 int xB0, float* kern) {
+  constexpr int NK = FK * FK, KS = 24;
+  double xfb[BX];
+#pragma unroll
+  for(int b = 0; b < BX; b++) xfb[b] = xfTab[xB0 + b];
+  for(int p = threadIdx.x; p < NK; p += NT) {
+    double cx[K + 1];
+#pragma unroll
+    for(int i = 0; i <= K; i++) {
+      const int t0 = i * (K + 1) - i * (i - 1) / 2;  // term of xf^i yf^0
+      double s = Kt[(size_t)(t0 + K - i) * NK + p];
+#pragma unroll
+      for(int j = K - i - 1; j >= 0; j--) s = fma(s, yf, Kt[(size_t)(t0 + j) * NK + p]);
+      cx[i] = s;
+    }
+    const int row = p / FK, col = p - row * FK;
+#pragma unroll
+    for(int b = 0; b < BX; b++) {
+      double k0 = cx[K];
+#pragma unroll
+      for(int i = K - 1; i >= 0; i--) k0 = fma(k0, xfb[b], cx[i]);
+      kern[(b * FK + row) * KS + col] = (float)k0;
     }
   }
-  for(int i = tid; i < TH * TW; i += nthr) {
-    const int ly = i / TW, lx = i % TW;
+}
+
+// The rounding order of each output is the reference's tap order: over
+// kernel rows jj, then columns ii, one FP32 FMA per tap.
+template <int FK, int BX>
+__global__ void __launch_bounds__(BX * 21, BX == 8 ? 2 : 1)
+    k_conv_sub_f32(const float* __restrict__ I, const float* __restrict__ O,
+                   const double* __restrict__ sol, const double* __restrict__ Kt,
+                   const double* __restrict__ blockXY, const double* __restrict__ kernSumPtr,
+                   ConvArgsF a,
+                   const uint8_t* __restrict__ inMask, uint16_t* __restrict__ mask,
+                   float* __restrict__ convF, float* __restrict__ diffF) {
+  using L = ConvTileF<FK, BX>;
+  static_assert(FK % L::PX == 0 && FK % L::RY == 0 && L::TPB == 21, "tiling");
+  constexpr int HK = L::HK, NK = L::NK, S = L::S, TW = L::TW, TH = L::TH, NW = L::NW, KS = L::KS;
+  constexpr int NT = L::NT, NFULL = NT / 32;  // full warps (ballots, |k| sums)
+  extern __shared__ __align__(16) unsigned char cv_smem[];
+  float* tile = (float*)cv_smem;
+  float* kern = (float*)(cv_smem + L::OFF_KERN);
+  uint32_t* bits = (uint32_t*)(cv_smem + L::OFF_BITS);
+  float* aks = (float*)(cv_smem + L::OFF_AKS);
+  float* bgc = aks + BX;  // background coefficients (getBackground), FP32
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int xB0 = blockIdx.x * BX, yB = blockIdx.y;
+  const int x0 = xB0 * FK, y0 = yB * FK;  // tile origin; block pixels start at +HK
+  const int K = a.kOrder;
+  for(int i = tid; i < TH * TW; i += NT) {
+    const int ly = i / TW, lx = i - ly * TW;
     const int gx = min(x0 + lx, a.w - 1), gy = min(y0 + ly, a.h - 1);
-    const float v = I[(size_t)gx + (size_t)gy * a.w];
-    tile[ly][lx] = v;
-    bad[ly][lx] = ((convMaskF(v, a.tH, a.tL) & BAD_INPUT) ||
-                   (inMask && inMask[(size_t)gx + (size_t)gy * a.w])) ? 1 : 0;
+    tile[ly * S + lx] = I[(size_t)gx + (size_t)gy * a.w];
+  }
+  // kernel of each block (conv(), src/bach.cpp:339-350)
+  {
+    const double yf = blockXY[a.xSteps + yB];
+    switch(K) {
+      case 0: convBlockKernels<0, FK, BX, NT>(Kt, blockXY, yf, xB0, kern); break;
+      case 1: convBlockKernels<1, FK, BX, NT>(Kt, blockXY, yf, xB0, kern); break;
+      case 2: convBlockKernels<2, FK, BX, NT>(Kt, blockXY, yf, xB0, kern); break;
+      default: convBlockKernels<3, FK, BX, NT>(Kt, blockXY, yf, xB0, kern); break;
+    }
   }
   __syncthreads();
-  // kernel of each block from the FP64 spatial-term images, rounded once
-  for(int e = tid; e < CV_BX * NK; e += nthr) {
-    const int b = e / NK, p = e % NK;
-    double k0 = 0.0;
-    for(int t = 0; t < nC2; t++) k0 = fma(poly[b][t], Kt[(size_t)t * NK + p], k0);
-    kern[b][p] = (float)k0;
-  }
-  for(int e = tid; e < TH * CV_BX * FK; e += nthr) {
-    const int ly = e / (CV_BX * FK), lx = e % (CV_BX * FK);
-    unsigned char o = 0;
+  if(warp < NFULL) {
+    // bad-input flags of the tile as bits (word c/32 of a row, bit c%32; the
+    // last word of a row is zero), one row per warp at a time
+    for(int ly = warp; ly < TH; ly += NFULL) {
+      const int gy = min(y0 + ly, a.h - 1);
 #pragma unroll
-    for(int d = 0; d < FK; d++) o |= bad[ly][lx + d];
-    rowBad[ly][lx] = o;
-  }
-  __syncthreads();
-  if(tid < CV_BX) {
-    float s = 0.f;
-    for(int p = 0; p < NK; p++) s += fabsf(kern[tid][p]);
-    aks[tid] = s;
+      for(int wc = 0; wc < NW; wc++) {
+        const int c = wc * 32 + lane;
+        bool bd = false;
+        if(c < TW) {
+          bd = convMaskF(tile[ly * S + c], a.tH, a.tL) & BAD_INPUT;
+          if(inMask) bd |= inMask[(size_t)min(x0 + c, a.w - 1) + (size_t)gy * a.w] != 0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, bd);
+        if(lane == 0) bits[ly * NW + wc] = m;
+      }
+    }
+    // sum of |k| of each block: lane-strided partial sums, then a butterfly
+    for(int b = warp; b < BX; b += NFULL) {
+      float s = 0.f;
+      for(int p = lane; p < NK; p += 32) s += fabsf(kern[(b * FK + p / FK) * KS + p % FK]);
+#pragma unroll
+      for(int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if(lane == 0) aks[b] = s;
+    }
   }
   const int nBgC = (a.bgOrder + 1) * (a.bgOrder + 2) / 2;
-  if(tid < nBgC && tid < 16) bgc[tid] = (float)sol[a.nComp + 2 + tid];
+  if(tid < nBgC) bgc[tid] = (float)sol[a.nComp + 2 + tid];
   __syncthreads();
+  // thread -> (block b, column group k, row group g): 7 columns x 3 rows
+  const int b = tid / L::TPB, r = tid - b * L::TPB, kq = r / 7, g = r - kq * 7;
+  const int ly0 = L::RY * g, lx0 = b * FK + L::PX * kq;
+  const float* kb = kern + b * FK * KS;
+  float acc[3][7];
+#pragma unroll
+  for(int o = 0; o < 3; o++)
+#pragma unroll
+    for(int q = 0; q < 7; q++) acc[o][q] = 0.f;
+  // tile row ly0 + R feeds output row ly0 + o through kernel row jj = R - o
+  for(int R = 0; R < FK + 2; R++) {
+    float win[27];
+    const float* trow = tile + (ly0 + R) * S + lx0;
+#pragma unroll
+    for(int q = 0; q < 27; q++) win[q] = trow[q];
+#pragma unroll
+    for(int o = 0; o < 3; o++) {
+      const int jj = R - o;
+      if(jj < 0 || jj >= FK) continue;
+      const float4* kr4 = (const float4*)(kb + (FK - 1 - jj) * KS);
+      float kf[24];
+#pragma unroll
+      for(int m = 0; m < 6; m++) {
+        const float4 v = kr4[m];
+        kf[4 * m] = v.x;
+        kf[4 * m + 1] = v.y;
+        kf[4 * m + 2] = v.z;
+        kf[4 * m + 3] = v.w;
+      }
+#pragma unroll
+      for(int ii = 0; ii < FK; ii++) {
+        const float kk = kf[FK - 1 - ii];
+#pragma unroll
+        for(int q = 0; q < 7; q++) acc[o][q] = fmaf(kk, win[q + ii], acc[o][q]);
+      }
+    }
+  }
+  // Pixels whose window holds a bad one: the sum of |k| over the good
+  // pixels is the kernel's |k| sum less that over the bad pixels, which are
+  // few (saturated cores); each bad pixel's |k| is added, in row then column
+  // order, to every output pixel of this thread whose window covers it.
+  constexpr unsigned long long WIN = (1ull << FK) - 1, COLS = (1ull << 27) - 1;
+  unsigned long long orw[3] = {0ull, 0ull, 0ull};
+  float badSum[3][7];
+#pragma unroll
+  for(int o = 0; o < 3; o++)
+#pragma unroll
+    for(int q = 0; q < 7; q++) badSum[o][q] = 0.f;
+  for(int R = 0; R < FK + 2; R++) {
+    const uint32_t* br = bits + (ly0 + R) * NW + (lx0 >> 5);
+    unsigned long long wb =
+        (((unsigned long long)br[0] | ((unsigned long long)br[1] << 32)) >> (lx0 & 31)) & COLS;
+    if(wb == 0ull) continue;
+#pragma unroll
+    for(int o = 0; o < 3; o++)
+      if(R - o >= 0 && R - o < FK) orw[o] |= wb;
+    while(wb != 0ull) {
+      const int cI = __ffsll((long long)wb) - 1;  // window column of a bad pixel
+      wb &= wb - 1ull;
+#pragma unroll
+      for(int o = 0; o < 3; o++) {
+        const int jj = R - o;
+        if(jj < 0 || jj >= FK) continue;
+        const float* krow = kb + (FK - 1 - jj) * KS + (FK - 1);
+#pragma unroll
+        for(int q = 0; q < 7; q++) {
+          const int ii = cI - q;
+          if(ii >= 0 && ii < FK) badSum[o][q] += fabsf(krow[-ii]);
+        }
+      }
+    }
+  }
+  __syncthreads();  // every thread is done with the kernel rows
+  float* sv = kern;  // conv sums of the CTA's pixels, row-major (FK rows x BX*FK)
+  unsigned char* cflag = cv_smem + L::OFF_FLAG;  // 0: window clean, 1: OK_CONV, 2: BAD_CONV
+  constexpr int RW = BX * FK;
+#pragma unroll
+  for(int o = 0; o < 3; o++)
+#pragma unroll
+    for(int q = 0; q < 7; q++) {
+      const int e = (ly0 + o) * RW + lx0 + q;
+      sv[e] = acc[o][q];
+      unsigned char f = 0;
+      if(((orw[o] >> q) & WIN) != 0ull) f = ((aks[b] - badSum[o][q]) / aks[b]) < 0.99f ? 2 : 1;
+      cflag[e] = f;
+    }
+  __syncthreads();
+  // one output column per thread, consecutive x across the CTA: coalesced
+  // reads of the other image and writes of mask, conv and difference
   const float hxF = 0.5f * (float)a.w, hyF = 0.5f * (float)a.h;
   const float ihxF = 1.f / hxF, ihyF = 1.f / hyF;
   const float kernSum = (float)*kernSumPtr;
   const float invKernMult = a.scaleConv ? 1.f / kernSum : 1.f;
   const float convFactor = a.scaleConv ? kernSum : 1.f;
   const float finalFactor = a.scaleConv ? -(1.f / kernSum) : 1.f;
-  // thread -> (block b, output row ly, first column lx0)
-  const int perBlock = FK * TPR;
-  if(tid >= CV_BX * perBlock) return;
-  const int b = tid / perBlock, r = tid % perBlock, ly = r / TPR, lx0 = b * FK + (r % TPR) * PX;
-  const float* kb = kern[b];
-  float acc[PX];
-#pragma unroll
-  for(int q = 0; q < PX; q++) acc[q] = 0.f;
-  for(int jj = 0; jj < FK; jj++) {
-    float win[PX + FK - 1];
-#pragma unroll
-    for(int q = 0; q < PX + FK - 1; q++) win[q] = tile[ly + jj][lx0 + q];
-    const float* krow = kb + (FK - 1 - jj) * FK;
-#pragma unroll
-    for(int ii = 0; ii < FK; ii++) {
-      const float kk = krow[FK - 1 - ii];
-#pragma unroll
-      for(int q = 0; q < PX; q++) acc[q] = fmaf(kk, win[q + ii], acc[q]);
-    }
-  }
-  // sum of |k| over the good pixels under the kernel, for pixels whose
-  // window holds a bad one: the same register-blocked pass over 0/1 flags,
-  // in the reference's tap order (adding |k| or 0 rounds like the
-  // conditional sum of the plain kernel)
-  bool anyq[PX];
-  bool need = false;
-#pragma unroll
-  for(int q = 0; q < PX; q++) {
-    unsigned char o = 0;
-    for(int jj = 0; jj < FK; jj++) o |= rowBad[ly + jj][lx0 + q];
-    anyq[q] = o != 0;
-    need |= anyq[q];
-  }
-  float uks[PX];
-#pragma unroll
-  for(int q = 0; q < PX; q++) uks[q] = 0.f;
-  if(need) {
-    for(int jj = 0; jj < FK; jj++) {
-      float gw[PX + FK - 1];
-#pragma unroll
-      for(int q = 0; q < PX + FK - 1; q++) gw[q] = bad[ly + jj][lx0 + q] ? 0.f : 1.f;
-      const float* krow = kb + (FK - 1 - jj) * FK;
-#pragma unroll
-      for(int ii = 0; ii < FK; ii++) {
-        const float kk = fabsf(krow[FK - 1 - ii]);
-#pragma unroll
-        for(int q = 0; q < PX; q++) uks[q] = fmaf(kk, gw[q + ii], uks[q]);
-      }
-    }
-  }
-#pragma unroll
-  for(int q = 0; q < PX; q++) {
-    const int x = x0 + HK + lx0 + q, y = y0 + HK + ly;
-    if(x >= a.w - HK || y >= a.h - HK) continue;
-    // background polynomial (getBackground, cd.cl:444-467) in FP32: the
-    // terms are O(1e3) ADU, so FP32 rounding moves a pixel by ~1e-4 ADU
-    const float bxf = ((float)x - hxF) * ihxF, byf = ((float)y - hyF) * ihyF;
+  static_assert(NT == RW, "one output column per thread");
+  const int x = x0 + HK + tid;
+  if(x >= a.w - HK) return;
+  // background polynomial (getBackground, cd.cl:444-467) in FP32: the terms
+  // are O(1e3) ADU, so FP32 rounding moves a pixel by ~1e-4 ADU
+  const float bxf = ((float)x - hxF) * ihxF;
+  for(int ly = 0; ly < FK; ly++) {
+    const int y = y0 + HK + ly;
+    if(y >= a.h - HK) break;
+    const int e = ly * RW + tid;
+    const float byf = ((float)y - hyF) * ihyF;
     float bgv = 0.f, ax = 1.f;
     int k = 0;
     for(int i = 0; i <= a.bgOrder; i++) {
@@ -799,22 +917,21 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
       }
       ax *= bxf;
     }
-    const float v = (acc[q] + bgv) * invKernMult;
+    const float v = (sv[e] + bgv) * invKernMult;
     const size_t id = (size_t)x + (size_t)y * a.w;
-    const float tc = tile[ly + HK][lx0 + q + HK];
+    const float tc = tile[(ly + HK) * S + tid + HK];
     uint16_t cm = convMaskF(tc, a.tH, a.tL);
     if(inMask && inMask[id]) cm |= INPUT_MASK | BAD_INPUT;
     uint16_t nm = cm;
     if(cm & BAD_INPUT) nm |= BAD_OUTPUT;
-    if(anyq[q]) {
-      if((uks[q] / aks[b]) < 0.99f) nm |= BAD_OUTPUT | BAD_CONV;
-      else nm |= OK_CONV;
-    }
-    const float o = O[id];
-    nm |= afterMaskF(o, a.tH, a.tL);
+    const unsigned char f = cflag[e];
+    if(f == 2) nm |= BAD_OUTPUT | BAD_CONV;
+    else if(f == 1) nm |= OK_CONV;
+    const float ov = O[id];
+    nm |= afterMaskF(ov, a.tH, a.tL);
     mask[id] = nm;
     convF[id] = v;
-    diffF[id] = (nm & BAD_OUTPUT) ? 1e-30f : (v * convFactor - o) * finalFactor;
+    diffF[id] = (nm & BAD_OUTPUT) ? 1e-30f : (v * convFactor - ov) * finalFactor;
   }
 }
 
@@ -824,9 +941,9 @@ __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
 // dP_t = P_t(x, y) - P_t(xc, yc): the block kernel is evaluated in FP64 and
 // rounded once (as k_conv_sub_f32 does), and the FP32 rounding of the
 // term images only scales the small dP_t (|dP| <= ~fK / frame size), so
-// fits whose spatial terms cancel keep the block kernel's accuracy.  Same
-// tiling as k_conv_sub_f32: 7 pixels of one row per thread, the window in
-// registers, one pass over the tile per term.
+// fits whose spatial terms cancel keep the block kernel's accuracy.  Seven
+// pixels of one row per thread, the window in registers, one pass over the
+// tile per term.
 template <int FK, int CV_BX>
 __global__ void __launch_bounds__(CV_BX * FK * (FK / 7))
     k_conv_sub_pp_f32(const float* __restrict__ I, const float* __restrict__ O,
@@ -1460,6 +1577,8 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   if(g.fK != 21) throw XbError{XB_ERR_UNSUPPORTED, "mixed conv is built for 21-px kernels"};
   const int I = c->chosen, O = 1 - c->chosen;
   if(c->imgIsF64) throw XbError{XB_ERR_UNSUPPORTED, "mixed mode takes FP32 images"};
+  if(c->p.kernelOrder > 3 || c->p.backgroundOrder > 4)
+    throw XbError{XB_ERR_UNSUPPORTED, "mixed conv: kernel order <= 3, background order <= 4"};
   const double* Kt = kernelTermsLaunch(c);
   ConvArgsF a{};
   a.w = c->w;
@@ -1474,20 +1593,28 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
   a.tH = (float)c->p.threshHigh;
   a.tL = (float)c->p.threshLow;
   const int xSteps = (c->w + g.fK - 1) / g.fK, ySteps = (c->h + g.fK - 1) / g.fK;
+  a.xSteps = xSteps;
+  double* blockXY = nullptr;
+  if(!c->p.convPerPixel) {
+    blockXY = buf<double>(c, "conv_block_xy", (size_t)(xSteps + ySteps));
+    k_block_centres<<<(xSteps + ySteps + 127) / 128, 128, 0, c->stream>>>(c->w, c->h, g.fK, xSteps,
+                                                                        ySteps, blockXY);
+    XB_LAUNCHED(c);
+  }
   auto launch = [&](int variant) {
     const float *Ii = (const float*)c->img[I], *Oi = (const float*)c->img[O];
     switch(variant) {
       case 0:
-        k_conv_sub_f32<21, 4><<<dim3((xSteps + 3) / 4, ySteps), 4 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
+        k_conv_sub_f32<21, 4><<<dim3((xSteps + 3) / 4, ySteps), 4 * 21, ConvTileF<21, 4>::BYTES, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, blockXY, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
       case 1:
-        k_conv_sub_f32<21, 2><<<dim3((xSteps + 1) / 2, ySteps), 2 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
+        k_conv_sub_f32<21, 6><<<dim3((xSteps + 5) / 6, ySteps), 6 * 21, ConvTileF<21, 6>::BYTES, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, blockXY, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
       default:
-        k_conv_sub_f32<21, 8><<<dim3((xSteps + 7) / 8, ySteps), 8 * 63, 0, c->stream>>>(
-            Ii, Oi, c->dSol, Kt, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
+        k_conv_sub_f32<21, 8><<<dim3((xSteps + 7) / 8, ySteps), 8 * 21, ConvTileF<21, 8>::BYTES, c->stream>>>(
+            Ii, Oi, c->dSol, Kt, blockXY, dKernSum, a, c->inputMask, c->mask, c->convF, c->diffF);
         break;
     }
     XB_LAUNCHED(c);
@@ -1506,7 +1633,10 @@ void convSubMixed(xb_ctx* c, double* dKernSum) {
         c->mask, c->convF, c->diffF);
     XB_LAUNCHED(c);
   } else {
-    // blocks per CTA: 4 (default), 2 or 8; the three give identical images
+    // blocks per CTA: 4 (default), 6 or 8; the three give identical images
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_f32<21, 4>, c->device));
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_f32<21, 6>, c->device));
+    XB_CUDA(allowMaxDynamicSmem((const void*)k_conv_sub_f32<21, 8>, c->device));
     const int v = tunedVariant(c, "conv_sub_f32", (long long)c->w * 100003LL + c->h, 3, launch);
     KT_SCOPE(c, "conv_sub");
     launch(v);
