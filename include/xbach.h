@@ -283,8 +283,9 @@ int xb_get_stream(xb_ctx* ctx, void** stream);
  *   dSky, dFwhm  nStamps doubles each, device memory
  *   stream cudaStream_t to launch on (NULL = legacy default stream); the call
  *          returns after the launch, results are ready when the stream is
- * Limit: nStamps * (9 * fStampWidth^2 + 16 * ceil(fStampWidth^2 / 32)) bytes
- * must fit in 32 MiB (2048^2 with 16x16 stamps of 107 px needs 27 MiB);
+ * Limit: nStamps * (9 * P + 16 * ceil(fStampWidth^2 / 32)) bytes, P =
+ * fStampWidth^2 rounded up to a multiple of 1024, must fit in 32 MiB (2048^2
+ * with 16x16 stamps of 107 px needs 28.4 MiB);
  * larger requests return XB_ERR_UNSUPPORTED and nothing runs.  The first call
  * on each device looks up the array's device address, so make that first call
  * before capturing a stream; the address is kept for the device's context,
@@ -346,6 +347,17 @@ int xb_batch_set_stream(xb_batch* b, void* stream);
  * one FMA = 2 operations; best of three ~10-20 ms launches): the
  * denominators of the roofline figures of kernels bound by those pipes. */
 int xb_measure_fma_peaks(int device, double* fp32Tflops, double* fp64Tflops);
+
+/* The left-to-right FP64 sum of c[0..n) that the stamp statistics use for the
+ * reference's serial sigma-clip sums (bachUtil.cpp:34-128): 32 terms per step
+ * of one warp, equal bit for bit to `s = 0; for(i) s += c[i]` for every input.
+ * _host runs the same steps on the CPU; _device runs the warp on `stream`
+ * over device arrays (dC: n doubles, dOut: one double). */
+double xb_ordered_sum_host(const double* c, int n);
+int xb_ordered_sum_device(const double* dC, int n, double* dOut, void* stream);
+/* The same over FP32 terms, each widened to FP64 before it is added (the
+ * substamp values of the substamp search, sss.cl:396-541). */
+int xb_ordered_sum_device_f32(const float* dC, int n, double* dOut, void* stream);
 
 /* ---- streaming pipeline over FITS files ---------------------------------- */
 /* No counterpart in the reference, whose main (src/main.cpp:16-159) reads

@@ -15,6 +15,7 @@
 
 #include "xb_device.cuh"
 #include "xb_internal.h"
+#include "xb_osum.cuh"
 
 namespace xb {
 
@@ -22,6 +23,7 @@ namespace {
 
 constexpr int NSAMPLES = 100, PADDED = 128;
 constexpr int ST_THREADS = 256;
+constexpr int ST_CHUNKS_SMEM = 1280;  // chunk sums kept in shared memory (stamps <= 40960 px)
 
 __device__ __forceinline__ int satFloorToInt(double v) {
   double f = floor(v);
@@ -86,6 +88,22 @@ struct Ran1 {
 // only pixels within that bound of a bin edge redo it in FP64.  All decisions
 // and sums are those of the reference's order.
 
+// The good-pixel list of a stamp, chunk-interleaved: entry q lives at
+// slot ((q >> 10) << 10) | ((q & 31) << 5) | ((q >> 5) & 31) of the stamp's
+// slice, whose length is fSW^2 rounded up to a multiple of 1024.
+__host__ __device__ __forceinline__ size_t statsSlice(int fSW) {
+  return ((size_t)fSW * fSW + 1023) & ~(size_t)1023;
+}
+__device__ __forceinline__ int listSlot(int q) {
+  return ((q >> 10) << 10) | ((q & 31) << 5) | ((q >> 5) & 31);
+}
+__device__ __forceinline__ int chunkSlot(int c, int l) {  // entry c * 32 + l
+  return ((c >> 5) << 10) | (l << 5) | (c & 31);
+}
+__device__ __forceinline__ int listEntry(int slot) {  // inverse of listSlot
+  return ((slot >> 10) << 10) | ((slot & 31) << 5) | ((slot >> 5) & 31);
+}
+
 // Order-preserving map of doubles (no NaN) to 64-bit keys and back.
 __device__ __forceinline__ unsigned long long dKey(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -134,7 +152,7 @@ __device__ unsigned long long clipEdge(double m, double inv, double alpha, bool 
 }
 
 template <class T>
-__global__ void __launch_bounds__(ST_THREADS)
+__global__ void __launch_bounds__(ST_THREADS, 3)
     k_stamp_stats(const T* __restrict__ img, uint16_t* __restrict__ mask,
                   const int4* __restrict__ geom, int w, int h, int fSW,
                   T* __restrict__ good, uint8_t* __restrict__ clip,
@@ -170,6 +188,7 @@ __global__ void __launch_bounds__(ST_THREADS)
   __shared__ double sMean, sStd, sInv, sSum, sSum2;
   __shared__ int sPrev, sCurr, sClip, sDone;
   __shared__ int bins[256];
+  __shared__ long long hC[257], hCE[257];  // prefix sums of the bin counts (and of index * count)
   __shared__ int okCount;
   __shared__ double hLower, hUpper, hSky, hBinSize, hLowerBinVal;
   __shared__ int hState;  // 0 continue, 1 stop (setFwhm), 2 stop (no fwhm)
@@ -187,11 +206,31 @@ __global__ void __launch_bounds__(ST_THREADS)
       sCount = 0;
     }
     const int numPix = gm.z * gm.w;
+    // with the draws, the candidates of the first PRE rounds (32 each) are
+    // read together
+    constexpr int PRE = 4;
+    double preV[PRE];
+    bool preOk[PRE];
+#pragma unroll
+    for(int r = 0; r < PRE; r++) {
+      preV[r] = 0.0;
+      preOk[r] = false;
+      if(draws && r * 32 + lane < numPix) {
+        const int rx = (int)floor(draws[2 * (r * 32 + lane)] * (int)gm.z);
+        const int ry = (int)floor(draws[2 * (r * 32 + lane) + 1] * (int)gm.w);
+        const int idx = (rx + gm.x) + (ry + gm.y) * w;
+        preV[r] = (double)img[idx];
+        preOk[r] = !(mask[idx] > 0 || fabs(preV[r]) <= 1e-10);
+      }
+    }
     int cnt = 0, iter = 0;
     while(cnt < NSAMPLES && iter < numPix) {
       int b = min(32, numPix - iter);
       int idx = 0;
-      if(draws) {
+      const int round = iter / 32;
+      if(draws && round < PRE) {
+        // taken from preV / preOk below
+      } else if(draws) {
         if(lane < b) {
           const int rx = (int)floor(draws[2 * (iter + lane)] * (int)gm.z);
           const int ry = (int)floor(draws[2 * (iter + lane) + 1] * (int)gm.w);
@@ -210,7 +249,10 @@ __global__ void __launch_bounds__(ST_THREADS)
       }
       bool ok = false;
       double v = 0.0;
-      if(lane < b) {
+      if(draws && round < PRE) {
+        v = round == 0 ? preV[0] : round == 1 ? preV[1] : round == 2 ? preV[2] : preV[3];
+        ok = round == 0 ? preOk[0] : round == 1 ? preOk[1] : round == 2 ? preOk[2] : preOk[3];
+      } else if(lane < b) {
         v = (double)img[idx];
         ok = !(mask[idx] > 0 || fabs(v) <= 1e-10);
       }
@@ -252,8 +294,12 @@ __global__ void __launch_bounds__(ST_THREADS)
   // 32 consecutive pixels at a time; ballots keep the ascending order inside
   // the warp and one block scan over the warp totals orders the warps.  The
   // good pixels are kept as read (FP32 pixels stay FP32).
-  T* gd = good + (size_t)s * fSW * fSW;
-  uint8_t* cl = clip + (size_t)s * fSW * fSW;
+  // The list is stored chunk-interleaved: entry q (chunk q/32, position
+  // q%32) at slot(q), so that the chunk passes, one chunk per thread, read
+  // 32 consecutive chunks' entries at one position with one coalesced load.
+  // A stamp's slice is fSW^2 rounded up to a multiple of 1024 (statsSlice).
+  T* gd = good + (size_t)s * statsSlice(fSW);
+  uint8_t* cl = clip + (size_t)s * statsSlice(fSW);
   const int nPixS = fSW * fSW;
   constexpr int NWARP = ST_THREADS / 32;
   const int perW = ((nPixS + NWARP - 1) / NWARP + 31) & ~31;
@@ -270,44 +316,66 @@ __global__ void __launch_bounds__(ST_THREADS)
     *id = (size_t)xI + (size_t)yI * w;
     return xI < w && yI < h;
   };
+  // each pass loads BB rows of 32 pixels (and their mask words) before it
+  // tests them, in order
+  constexpr int BB = 8;
   int wGood = 0;
-  for(int b = w0; b < w1; b += 32) {
-    const int idxS = b + lane;
-    bool g = false;
-    size_t id;
-    if(idxS < w1 && pixelAt(idxS, &id)) {
-      const T pix = img[id];
-      if(!(mask[id] > 0 || tiny(pix))) {
-        if(isnan(pix)) mask[id] |= NAN_PIXEL | BAD_INPUT;
+  for(int b0 = w0; b0 < w1; b0 += 32 * BB) {
+    T px[BB];
+    uint16_t mk[BB];
+    size_t ids[BB];
+    bool in[BB];
+#pragma unroll
+    for(int u = 0; u < BB; u++) {
+      const int idxS = b0 + u * 32 + lane;
+      in[u] = idxS < w1 && pixelAt(idxS, &ids[u]);
+      px[u] = in[u] ? img[ids[u]] : T(0);
+      mk[u] = in[u] ? mask[ids[u]] : (uint16_t)1;
+    }
+#pragma unroll
+    for(int u = 0; u < BB; u++) {
+      bool g = false;
+      if(in[u] && !(mk[u] > 0 || tiny(px[u]))) {
+        if(isnan(px[u])) mask[ids[u]] |= NAN_PIXEL | BAD_INPUT;
         else g = true;
       }
+      wGood += __popc(__ballot_sync(0xffffffffu, g));
     }
-    wGood += __popc(__ballot_sync(0xffffffffu, g));
   }
   const int wBase = blockScanExcl(lane == 0 ? wGood : 0, warpTot, &sTotal);
   const int nGood = sTotal;
   int pos = __shfl_sync(0xffffffffu, wBase, 0);
-  for(int b = w0; b < w1; b += 32) {
-    const int idxS = b + lane;
-    bool g = false;
-    T pix = 0;
-    size_t id;
-    if(idxS < w1 && pixelAt(idxS, &id)) {
-      pix = img[id];
-      g = !(mask[id] > 0 || tiny(pix));  // NaN pixels carry their mask bits now
+  for(int b0 = w0; b0 < w1; b0 += 32 * BB) {
+    T px[BB];
+    uint16_t mk[BB];
+    bool in[BB];
+#pragma unroll
+    for(int u = 0; u < BB; u++) {
+      const int idxS = b0 + u * 32 + lane;
+      size_t id;
+      in[u] = idxS < w1 && pixelAt(idxS, &id);
+      px[u] = in[u] ? img[id] : T(0);
+      mk[u] = in[u] ? mask[id] : (uint16_t)1;  // NaN pixels carry their mask bits now
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, g);
-    if(g) {
-      const int q = pos + __popc(bal & ((1u << lane) - 1u));
-      gd[q] = pix;
-      cl[q] = 0;
+#pragma unroll
+    for(int u = 0; u < BB; u++) {
+      const bool g = in[u] && !(mk[u] > 0 || tiny(px[u]));
+      const unsigned bal = __ballot_sync(0xffffffffu, g);
+      if(g) {
+        const int q = pos + __popc(bal & ((1u << lane) - 1u));
+        gd[listSlot(q)] = px[u];
+        cl[listSlot(q)] = 0;
+      }
+      pos += __popc(bal);
     }
-    pos += __popc(bal);
   }
 
   // ---- phase C: sigma clip, maxIter 3 (bachUtil.cpp:34-128) ----
-  double* cS = chunkBuf + (size_t)s * 2 * maxChunks;
-  double* cS2 = cS + maxChunks;
+  // the chunk sums, in shared memory when they fit
+  __shared__ double chunkSm[2][ST_CHUNKS_SMEM];
+  const bool chunksInSmem = (nGood + 31) / 32 <= ST_CHUNKS_SMEM;
+  double* cS = chunksInSmem ? chunkSm[0] : chunkBuf + (size_t)s * 2 * maxChunks;
+  double* cS2 = chunksInSmem ? chunkSm[1] : cS + maxChunks;
   if(tid == 0) {
     sPrev = nGood;
     sCurr = 0;
@@ -362,18 +430,33 @@ __global__ void __launch_bounds__(ST_THREADS)
   };
   // chunk sums of the unclipped pixels: 32 consecutive good pixels each, in
   // order (all pixels at first; then fused with each round's clip pass, for
-  // the next round)
-  for(int c = tid; c < nChunks; c += ST_THREADS) {
+  // the next round).  A chunk's pixels and flags are loaded before its sums
+  // start; entries past the list's end count as clipped (adding 0.0 leaves a
+  // sum unchanged).
+  // sums of a chunk's unclipped pixels, 16 loads issued at a time
+  auto chunkSums = [&](int c, int lc, bool all) {
     double a = 0.0, a2 = 0.0;
-    const int lc = min(32, nGood - c * 32);
-    for(int l = 0; l < lc; l++) {
-      const double d = (double)gd[c * 32 + l];
-      a += d;
-      a2 += d * d;
+#pragma unroll
+    for(int h = 0; h < 32; h += 16) {
+      T v[16];
+      bool on[16];
+#pragma unroll
+      for(int l = 0; l < 16; l++) {
+        const int at = chunkSlot(c, h + l);
+        on[l] = h + l < lc && (all || cl[at] == 0);
+        v[l] = h + l < lc ? gd[at] : T(0);
+      }
+#pragma unroll
+      for(int l = 0; l < 16; l++) {
+        const double d = on[l] ? (double)v[l] : 0.0;
+        a += d;
+        a2 += d * d;
+      }
     }
     cS[c] = a;
     cS2[c] = a2;
-  }
+  };
+  for(int c = tid; c < nChunks; c += ST_THREADS) chunkSums(c, min(32, nGood - c * 32), true);
   for(int it = 0; it < 3; it++) {
     if(sDone || sCurr == sPrev) break;
     if(sPrev <= 1) {
@@ -386,15 +469,14 @@ __global__ void __launch_bounds__(ST_THREADS)
     __syncthreads();
     if(tid == 0) sCurr = sPrev;
     __syncthreads();
-    // the two sequential chunk sums run on two warps
-    if(tid == 0) {
-      double sum = 0.0;
-      for(int c = 0; c < nChunks; c++) sum += cS[c];
-      sSum = sum;
-    } else if(tid == 32) {
-      double sum2 = 0.0;
-      for(int c = 0; c < nChunks; c++) sum2 += cS2[c];
-      sSum2 = sum2;
+    // the two sequential chunk sums (the reference's serial FP64 loops, bit
+    // for bit) on two warps
+    if(warp == 0) {
+      const double sum = osum::warpOrderedSum(cS, nChunks);
+      if(lane == 0) sSum = sum;
+    } else if(warp == 1) {
+      const double sum2 = osum::warpOrderedSum(cS2, nChunks);
+      if(lane == 0) sSum2 = sum2;
     }
     __syncthreads();
     if(tid == 0) {
@@ -412,23 +494,29 @@ __global__ void __launch_bounds__(ST_THREADS)
     thresholds(m, inv);
     int myClip = 0;
     for(int c = tid; c < nChunks; c += ST_THREADS) {
-      double a = 0.0, a2 = 0.0;
       const int lc = min(32, nGood - c * 32);
-      for(int l = 0; l < lc; l++) {
-        const int k = c * 32 + l;
-        const T v = gd[k];
-        uint8_t f = cl[k];
-        if(f == 0 && isClippedPix(v, m, inv)) {
-          f = 1;
-          cl[k] = 1;
-          myClip++;
+      // a chunk none of whose pixels is clipped in this round keeps its sums
+      // (the same terms in the same order)
+      bool changed = false;
+#pragma unroll
+      for(int h = 0; h < 32; h += 16) {
+        T v[16];
+        uint8_t fl[16];
+#pragma unroll
+        for(int l = 0; l < 16; l++) {
+          v[l] = h + l < lc ? gd[chunkSlot(c, h + l)] : T(0);
+          fl[l] = h + l < lc ? cl[chunkSlot(c, h + l)] : (uint8_t)1;
         }
-        const double d = f == 0 ? (double)v : 0.0;
-        a += d;
-        a2 += d * d;
+#pragma unroll
+        for(int l = 0; l < 16; l++) {
+          if(fl[l] == 0 && isClippedPix(v[l], m, inv)) {
+            cl[chunkSlot(c, h + l)] = 1;
+            myClip++;
+            changed = true;
+          }
+        }
       }
-      cS[c] = a;
-      cS2[c] = a2;
+      if(changed) chunkSums(c, lc, false);
     }
     if(myClip) atomicAdd(&sClip, myClip);
     __syncthreads();
@@ -479,99 +567,164 @@ __global__ void __launch_bounds__(ST_THREADS)
     // stamp) less the final clip; a warp-uniform trip count lets the lanes of
     // a warp that land in the same bin (most pixels sit in a few sky bins)
     // add to it with one atomic
-    for(int base = 0; base < nGood; base += ST_THREADS) {
-      const int k = base + tid;
-      int index = -1;
-      if(k < nGood) {
-        const T pv = gd[k];
-        if(!isClippedPix(pv, mean, invStd)) {
-          if(!exactAll) {
-            const float q = ((float)pv - fl) * fi;
-            if(q > 300.f) {
-              index = 255;
-            } else if(q < -50.f) {
-              index = 0;
-            } else {
-              const float f0 = floorf(q), fr = q - f0;
-              if(fr > fd && fr < 1.f - fd) index = min(max((int)f0 + 1, 0), 255);
+    constexpr int HB = 8;  // list entries loaded ahead per thread
+    // (the counts do not depend on the order: the slots are read in storage
+    // order, coalesced, each standing for list entry listEntry(slot))
+    const int nSlots = (nGood + 1023) & ~1023;
+    for(int base0 = 0; base0 < nSlots; base0 += ST_THREADS * HB) {
+      T pvs[HB];
+      bool in[HB];
+#pragma unroll
+      for(int u = 0; u < HB; u++) {
+        const int k = base0 + u * ST_THREADS + tid;
+        in[u] = k < nSlots && listEntry(k) < nGood;
+        pvs[u] = in[u] ? gd[k] : T(0);
+      }
+#pragma unroll
+      for(int u = 0; u < HB; u++) {
+        int index = -1;
+        if(in[u]) {
+          const T pv = pvs[u];
+          if(!isClippedPix(pv, mean, invStd)) {
+            if(!exactAll) {
+              const float q = ((float)pv - fl) * fi;
+              if(q > 300.f) {
+                index = 255;
+              } else if(q < -50.f) {
+                index = 0;
+              } else {
+                const float f0 = floorf(q), fr = q - f0;
+                if(fr > fd && fr < 1.f - fd) index = min(max((int)f0 + 1, 0), 255);
+              }
+            }
+            if(index < 0) {
+              const double v = (double)pv;
+              index = satFloorToInt((v - lbv) / bs);
+              index = index == INT_MAX ? INT_MAX : index + 1;
+              index = min(max(index, 0), 255);
             }
           }
-          if(index < 0) {
-            const double v = (double)pv;
-            index = satFloorToInt((v - lbv) / bs);
-            index = index == INT_MAX ? INT_MAX : index + 1;
-            index = min(max(index, 0), 255);
-          }
         }
-      }
-      const unsigned grp = __match_any_sync(0xffffffffu, index);
-      if(index >= 0) {
-        myOk++;
-        if(lane == __ffs(grp) - 1) atomicAdd(&bins[index], __popc(grp));
+        const unsigned grp = __match_any_sync(0xffffffffu, index);
+        if(index >= 0) {
+          myOk++;
+          if(lane == __ffs(grp) - 1) atomicAdd(&bins[index], __popc(grp));
+        }
       }
     }
     if(myOk) atomicAdd(&okCount, myOk);
     __syncthreads();
-    if(tid == 0) {
+    if(warp == 0) {
       const int ok = okCount;
-      double binSize = hBinSize, lowerBinVal = hLowerBinVal;
+      const double binSize = hBinSize, lowerBinVal = hLowerBinVal;
       if(ok == 0 || binSize == 0.0) {
-        hState = 2;
+        if(lane == 0) hState = 2;
       } else {
-        // densest run of bins holding a tenth of the pixels.  The reference
-        // compares the FP64 quotients sumBins / (upper - lower); both are
-        // integer over integer (sums of counts < 2^31, widths 1..254), and two
+        // The reference walks the bins serially (createHistogram,
+        // sss.cl:190-324); every quantity it forms is a prefix sum of the
+        // counts, so one warp scans the 256 bins once and finds each walk's
+        // stopping point by binary search.
+        // The running sums of bin counts (sumBins, sumExpect) are FP64 in the
+        // reference but hold integers below 2^53, so they are int64 here;
+        // S < x for an integer S and a double x is S < ceil(x).
+        long long c8[8], e8[8], tc = 0, te = 0;
+#pragma unroll
+        for(int k = 0; k < 8; k++) {
+          const int i = 8 * lane + k;
+          tc += bins[i];
+          te += (long long)i * bins[i];
+          c8[k] = tc;
+          e8[k] = te;
+        }
+        long long pc = tc, pe = te;  // inclusive scan of the lane totals
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1) {
+          const long long uc = __shfl_up_sync(0xffffffffu, pc, o);
+          const long long ue = __shfl_up_sync(0xffffffffu, pe, o);
+          if(lane >= o) {
+            pc += uc;
+            pe += ue;
+          }
+        }
+#pragma unroll
+        for(int k = 0; k < 8; k++) {  // hC[i] = sum of bins[0..i), hCE[i] = sum of j * bins[j]
+          hC[8 * lane + k + 1] = pc - tc + c8[k];
+          hCE[8 * lane + k + 1] = pe - te + e8[k];
+        }
+        if(lane == 0) hC[0] = hCE[0] = 0;
+        __syncwarp();
+        const long long tenth = (long long)ceil(ok / 10.0);
+        // first i in [lo, hi] with hC[i] >= target, hi when none
+        auto firstAtLeast = [&](int lo, int hi, long long target) {
+          while(lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if(hC[mid] >= target) hi = mid;
+            else lo = mid + 1;
+          }
+          return lo;
+        };
+        // Densest run of bins holding a tenth of the pixels: the serial
+        // window for lower index L ends at U(L) = the first U in [L+1, 255]
+        // with hC[U] - hC[L] >= tenth (255 when none; U(L) never decreases,
+        // so this is where the two-pointer walk stands), and the walk visits
+        // L = 1, 2, ... while the previous window ended below 255.  The
+        // reference compares the FP64 quotients S / (U - L); both are integer
+        // over integer (sums of counts < 2^31, widths 1..254), and two
         // different such fractions differ by more than 2^-47 relative, so
         // their correctly rounded quotients compare like the fractions:
         // S / D > S' / D'  <=>  S * D' > S' * D, exact in 64-bit integers.
-        // The width is never 0: the window is empty only at the top of the
-        // loop, and then the inner loop adds a bin (upper < 255 there).
-        // The running sums of bin counts (sumBins, sumExpect) are FP64 in the
-        // reference but hold integers below 2^53, so they are kept in int64
-        // here (no serial FP64 add chain); S < x for an integer S and a double
-        // x is S < ceil(x).
-        long long S = 0;
-        long long maxNum = 0, maxDen = 1;  // maxDens = 0 at first
-        const long long tenth = (long long)ceil(ok / 10.0);
-        int lowerIndex = 1, upperIndex = 1, maxIndex = -1;
-        while(upperIndex < 255) {
-          while(S < tenth && upperIndex < 255) S += bins[upperIndex++];
-          const long long D = upperIndex - lowerIndex;
-          if(S * maxDen > maxNum * D) {
-            maxNum = S;
-            maxDen = D;
-            maxIndex = lowerIndex;
+        // The walk keeps the first L of the largest density (strict >), from
+        // maxDens = 0.
+        long long bN = 0, bD = 1;
+        int bL = -1;
+        for(int L = 1 + lane; L <= 254; L += 32) {
+          if(L > 1 && firstAtLeast(L, 255, hC[L - 1] + tenth) >= 255) continue;
+          const int U = firstAtLeast(L + 1, 255, hC[L] + tenth);
+          const long long S = hC[U] - hC[L], D = U - L;
+          if(S * bD > bN * D) {
+            bN = S;
+            bD = D;
+            bL = L;
           }
-          S -= bins[lowerIndex++];
         }
-        if(maxIndex < 0 || maxIndex > 255) maxIndex = 0;
-        S = 0;
-        long long E = 0;
-        for(int i = maxIndex; S < tenth && i < 255; i++) {
-          S += bins[i];
-          E += (long long)(i * bins[i]);
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1) {
+          const long long oN = __shfl_xor_sync(0xffffffffu, bN, o);
+          const long long oD = __shfl_xor_sync(0xffffffffu, bD, o);
+          const int oL = __shfl_xor_sync(0xffffffffu, bL, o);
+          const long long lhs = oN * bD, rhs = bN * oD;
+          if(oL >= 0 && (bL < 0 || lhs > rhs || (lhs == rhs && oL < bL))) {
+            bN = oN;
+            bD = oD;
+            bL = oL;
+          }
         }
-        double modeBin = (double)E / (double)S + 0.5;
-        double skyEst = lowerBinVal + binSize * (modeBin - 1.0);
-        double lower = ok * 0.25, upper = ok * 0.75;
-        const long long lowerCeil = (long long)ceil(lower), upperCeil = (long long)ceil(upper);
-        S = 0;
-        int i = 0;
-        while(S < lowerCeil) S += bins[i++];
-        lower = i - ((double)S - lower) / bins[i - 1];
-        while(S < upperCeil) S += bins[i++];
-        upper = i - ((double)S - upper) / bins[i - 1];
-        hSky = skyEst;
-        hLower = lower;
-        hUpper = upper;
-        if(lower < 1.0 || upper > 255.0) {
-          hLowerBinVal = lowerBinVal - 128.0 * binSize;
-          hBinSize = binSize * 2;
-        } else if(upper - lower < 40.0) {
-          hBinSize = binSize / 3.0;
-          hLowerBinVal = skyEst - 128.0 * hBinSize;
-        } else {
-          hState = 1;
+        if(lane == 0) {
+          const int maxIndex = bL < 0 ? 0 : bL;
+          // the mode's walk from maxIndex adds bins while below a tenth
+          const int iEnd = firstAtLeast(maxIndex + 1, 255, hC[maxIndex] + tenth);
+          const long long S = hC[iEnd] - hC[maxIndex], E = hCE[iEnd] - hCE[maxIndex];
+          double modeBin = (double)E / (double)S + 0.5;
+          double skyEst = lowerBinVal + binSize * (modeBin - 1.0);
+          double lower = ok * 0.25, upper = ok * 0.75;
+          const long long lowerCeil = (long long)ceil(lower), upperCeil = (long long)ceil(upper);
+          // the quartile walks from bin 0 (hC[256] = ok bounds both)
+          const int i1 = firstAtLeast(0, 256, lowerCeil);
+          lower = i1 - ((double)hC[i1] - lower) / bins[i1 - 1];
+          const int i2 = firstAtLeast(i1, 256, upperCeil);
+          upper = i2 - ((double)hC[i2] - upper) / bins[i2 - 1];
+          hSky = skyEst;
+          hLower = lower;
+          hUpper = upper;
+          if(lower < 1.0 || upper > 255.0) {
+            hLowerBinVal = lowerBinVal - 128.0 * binSize;
+            hBinSize = binSize * 2;
+          } else if(upper - lower < 40.0) {
+            hBinSize = binSize / 3.0;
+            hLowerBinVal = skyEst - 128.0 * hBinSize;
+          } else {
+            hState = 1;
+          }
         }
       }
     }
@@ -819,7 +972,6 @@ __global__ void __launch_bounds__(FM_THREADS)
   __shared__ int sBest;
   __shared__ double rA[FM_THREADS / 32], rB[FM_THREADS / 32];
   __shared__ double sSum;
-  __shared__ int sExact;
   // static flags: checkSStamp predicate, kernel-fit qualification, v > 0
   for(int p = tid; p < N; p += FM_THREADS) {
     const double v = (double)img[(size_t)(cx + p % n) + (size_t)(cy + p / n) * w];
@@ -1051,13 +1203,15 @@ __global__ void __launch_bounds__(FS_T, 1)
   __shared__ float sfP, sfK, sfLim;
   __shared__ int sDirect;
 
-  for(int ly = warp; ly < n; ly += NW)
-    for(int lx = lane; lx < n; lx += 32) {
-      const size_t a = (size_t)(cx + lx) + (size_t)(cy + ly) * w;
-      V[ly * n + lx] = img[a];
-      bad[ly * n + lx] = (ldMask(mask, a) & badMask) ? 1 : 0;
-    }
-  // exact thresholds of the two static predicates (one warp each)
+  // warps 2.. load the stamp while warps 0 and 1 search the exact
+  // thresholds of the two static predicates
+  if(warp >= 2)
+    for(int ly = warp - 2; ly < n; ly += NW - 2)
+      for(int lx = lane; lx < n; lx += 32) {
+        const size_t a = (size_t)(cx + lx) + (size_t)(cy + ly) * w;
+        V[ly * n + lx] = img[a];
+        bad[ly * n + lx] = (ldMask(mask, a) & badMask) ? 1 : 0;
+      }
   if(warp < 2) {
     auto pr = [&](double v) { return (v - sky) / fwhm > tKF; };
     auto kq = [&](double v) { return !((v - sky) * invFwhm < tKF); };
@@ -1284,48 +1438,50 @@ __global__ void __launch_bounds__(FS_T, 1)
       const int u0 = max(mx - hSS, cx), v0 = max(my - hSS, cy);
       const int u1 = min(mx + hSS, cx + sx - 1), v1 = min(my + hSS, cy + sy - 1);
       const int uw = u1 - u0 + 1, un = uw * (v1 - v0 + 1);
-      // value of the substamp: sum of the thresholded pixels in raster order
+      // value of the substamp: the reference's serial FP64 sum of the
+      // thresholded pixels in raster order.  When they are all positive and
+      // the sum of their magnitudes stays below 2^52 quanta of the smallest
+      // (every pixel is a multiple of that quantum), no partial sum rounds in
+      // any order; otherwise warp 0 forms the serial sum bit for bit (osum;
+      // a pixel below the threshold adds +0.0, which changes nothing).
       double part = 0.0, amin = INFINITY;
       for(int i = tid; i < un; i += FS_T) {
-        const int lx = u0 + i % uw - cx, ly = v0 + i / uw - cy;
-        if(flags[ly * n + lx] & FL_PRED) {
-          const double v = (double)V[ly * n + lx];
+        const int q = (v0 + i / uw - cy) * n + (u0 + i % uw - cx);
+        if(flags[q] & FL_PRED) {
+          const double v = (double)V[q];
           part += v;
           amin = fmin(amin, fabs(v));
         }
       }
 #pragma unroll
       for(int o = 16; o > 0; o >>= 1) {
-        part += __shfl_down_sync(0xffffffffu, part, o);
-        amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
+        part += __shfl_xor_sync(0xffffffffu, part, o);
+        amin = fmin(amin, __shfl_xor_sync(0xffffffffu, amin, o));
       }
       if(lane == 0) {
         rA[warp] = part;
         rB[warp] = amin;
       }
       __syncthreads();
-      if(tid == 0) {
-        double t = 0.0, mn = INFINITY;
-        for(int i = 0; i < NW; i++) {
-          t += rA[i];
-          mn = fmin(mn, rB[i]);
+      if(warp == 0) {
+        double t = lane < NW ? rA[lane] : 0.0, mn = lane < NW ? rB[lane] : INFINITY;
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1) {
+          t += __shfl_xor_sync(0xffffffffu, t, o);
+          mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         }
-        int exact = 0;
+        bool exact = false;
         if(!(okw[m] & OK_NONPOS) && mn > 0.0 && mn < INFINITY) {
           int e;
-          frexp(mn, &e);                           // mn in [2^(e-1), 2^e)
-          const double quantum = ldexp(1.0, e - 1 - 23);
-          exact = t < ldexp(quantum, 52) ? 1 : 0;  // t = sum|v| here (all v > 0)
+          frexp(mn, &e);  // mn in [2^(e-1), 2^e)
+          exact = t < ldexp(1.0, e - 1 - 23 + 52);
         }
-        if(!exact) {
-          t = 0.0;
-          for(int yy = v0; yy <= v1; yy++)
-            for(int xx = u0; xx <= u1; xx++) {
-              const int q = (yy - cy) * n + (xx - cx);
-              if(flags[q] & FL_PRED) t += (double)V[q];
-            }
-        }
-        sSum = t;
+        if(!exact)
+          t = osum::warpOrderedSumOf(un, [&](int i) {
+            const int q = (v0 + i / uw - cy) * n + (u0 + i % uw - cx);
+            return (flags[q] & FL_PRED) ? V[q] : 0.f;
+          });
+        if(lane == 0) sSum = t;
       }
       __syncthreads();
       const double ret = sSum;
@@ -1554,8 +1710,8 @@ void stageSss(xb_ctx* c) {
     S.ssxy = buf<int2>(c, "ssxy" + sfx, (size_t)nAll * g.maxSS);
     S.ssval = buf<double>(c, "ssval" + sfx, (size_t)nAll * g.maxSS);
   }
-  c->goodScratch = buf<double>(c, "goodScratch", (size_t)nAll * fSW * fSW);
-  c->clipScratch = buf<uint8_t>(c, "clipScratch", (size_t)nAll * fSW * fSW);
+  c->goodScratch = buf<double>(c, "goodScratch", (size_t)nAll * statsSlice(fSW));
+  c->clipScratch = buf<uint8_t>(c, "clipScratch", (size_t)nAll * statsSlice(fSW));
   const size_t chunkDoubles = (size_t)nAll * 2 * ((fSW * fSW + 31) / 32);
   c->dWork = buf<double>(c, "chunkScratch", chunkDoubles);
   c->dIWork = buf<int>(c, "iwork", 64);
@@ -1680,13 +1836,17 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
   // scratch carve-up: good pixels (FP64), clip flags (bytes), chunk sums
   const size_t pix = (size_t)fStampWidth * fStampWidth;
   const int maxChunks = (int)((pix + 31) / 32);
-  const size_t goodBytes = alignUp((size_t)nStamps * pix * sizeof(double));
-  const size_t clipBytes = alignUp((size_t)nStamps * pix);
+  if(pix > (size_t)1 << 26)
+    return noallocFail(err, errCap, XB_ERR_UNSUPPORTED, "stamps beyond 8192 px on a side");
+  const size_t slice = xb::statsSlice(fStampWidth);
+  const size_t goodBytes = alignUp((size_t)nStamps * slice * sizeof(double));
+  const size_t clipBytes = alignUp((size_t)nStamps * slice);
   const size_t chunkBytes = alignUp((size_t)nStamps * 2 * maxChunks * sizeof(double));
-  if(pix > (size_t)1 << 26 || goodBytes + clipBytes + chunkBytes > kStatsScratchBytes)
+  if(goodBytes + clipBytes + chunkBytes > kStatsScratchBytes)
     return noallocFail(err, errCap, XB_ERR_UNSUPPORTED,
-                       "stamps need more than the 32 MiB scratch: nStamps * (9 * fStampWidth^2 "
-                       "+ 16 * ceil(fStampWidth^2 / 32)) bytes must fit");
+                       "stamps need more than the 32 MiB scratch: nStamps * (9 * P + 16 * "
+                       "ceil(fStampWidth^2 / 32)) bytes must fit, P = fStampWidth^2 rounded up "
+                       "to a multiple of 1024");
   // An error left pending by the caller's own work is reported as such and
   // left in place (not cleared), so it is not mistaken for this call's.
   const cudaError_t pending = cudaPeekAtLastError();
@@ -1727,4 +1887,33 @@ extern "C" int xb_stamp_stats_noalloc(const float* dImg, uint16_t* dMask, int w,
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return noallocFail(err, errCap, XB_ERR_CUDA, cudaGetErrorString(e));
   return XB_OK;
+}
+
+namespace xb {
+namespace {
+__global__ void k_ordered_sum(const double* __restrict__ c, int n, double* __restrict__ out) {
+  const double s = osum::warpOrderedSum(c, n);
+  if(threadIdx.x == 0) *out = s;
+}
+__global__ void k_ordered_sum_f32(const float* __restrict__ c, int n, double* __restrict__ out) {
+  const double s = osum::warpOrderedSumOf(n, [c](int i) { return c[i]; });
+  if(threadIdx.x == 0) *out = s;
+}
+}  // namespace
+}  // namespace xb
+
+extern "C" double xb_ordered_sum_host(const double* c, int n) {
+  return (c == nullptr || n <= 0) ? 0.0 : xb::osum::orderedSumHost(c, n);
+}
+
+extern "C" int xb_ordered_sum_device(const double* dC, int n, double* dOut, void* stream) {
+  if(dOut == nullptr || n < 0 || (n > 0 && dC == nullptr)) return XB_ERR_ARG;
+  xb::k_ordered_sum<<<1, 32, 0, (cudaStream_t)stream>>>(dC, n, dOut);
+  return cudaGetLastError() == cudaSuccess ? XB_OK : XB_ERR_CUDA;
+}
+
+extern "C" int xb_ordered_sum_device_f32(const float* dC, int n, double* dOut, void* stream) {
+  if(dOut == nullptr || n < 0 || (n > 0 && dC == nullptr)) return XB_ERR_ARG;
+  xb::k_ordered_sum_f32<<<1, 32, 0, (cudaStream_t)stream>>>(dC, n, dOut);
+  return cudaGetLastError() == cudaSuccess ? XB_OK : XB_ERR_CUDA;
 }

@@ -65,7 +65,8 @@ EXPORTS = [
     "xb_ranker_features", "xb_ranker_forward", "xb_ranker_grad", "xb_ranker_adam",
     "xb_pipeline_create", "xb_pipeline_destroy", "xb_pipeline_last_error", "xb_pipeline_worker",
     "xb_pipeline_run_files", "xb_pipeline_stats_get", "xb_pipeline_set_params",
-    "xb_measure_fma_peaks",
+    "xb_measure_fma_peaks", "xb_ordered_sum_host", "xb_ordered_sum_device",
+    "xb_ordered_sum_device_f32",
 ]
 
 
@@ -145,6 +146,10 @@ def lib():
     L.xb_pipeline_stats_get.argtypes = [vp, P(PipelineStats)]
     L.xb_pipeline_set_params.argtypes = [vp, i, vp]
     L.xb_measure_fma_peaks.argtypes = [i, P(d), P(d)]
+    L.xb_ordered_sum_host.argtypes = [vp, i]
+    L.xb_ordered_sum_host.restype = d
+    L.xb_ordered_sum_device.argtypes = [vp, i, vp, vp]
+    L.xb_ordered_sum_device_f32.argtypes = [vp, i, vp, vp]
     _lib = L
     return L
 
@@ -509,6 +514,14 @@ class Pipeline:
         if self.L.xb_pipeline_stats_get(self.h, ctypes.byref(out)):
             raise XbError(5, "xb_pipeline_stats_get failed")
         return {k: getattr(out, k) for k, _ in PipelineStats._fields_}
+
+
+def ordered_sum_host(c):
+    """xb_ordered_sum_host: the left-to-right FP64 sum of c by the warp
+    algorithm's steps, on the CPU."""
+    import numpy as np
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    return lib().xb_ordered_sum_host(c.ctypes.data, len(c))
 
 
 def measure_fma_peaks(device=0):
