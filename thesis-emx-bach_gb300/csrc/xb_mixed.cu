@@ -10,8 +10,8 @@
 //     iterative-refinement step with an FP64 residual;
 //   * the chi^2 model in FP32 (the reference already stores it in FP32,
 //     cl_kern/cd.cl:489-531);
-//   * the full-frame convolution in FP32: four kernel blocks per CTA, seven
-//     pixels per thread held in registers.
+//   * the full-frame convolution in FP32: 4, 6 or 8 kernel blocks per CTA,
+//     a 7 x 3 pixel tile per thread held in registers.
 // Statistics, substamp search and the per-stamp test fits are shared with the
 // plain path.
 
